@@ -1,0 +1,362 @@
+"""GB300 (sm_103a) ADER-DG element path: Python host mirror of the reference's
+Solver<AmrDG<P>> / ModelEquation<Compressible_Euler> surface over the C ABI of
+libadg.so (include/adg.h).
+
+Reference surface mirrored here:
+  Simulation setters      Source/Core/Simulation.h:25-176
+  AmrDG<P>::settings      Source/NumericalMethod/AmrDG/AmrDG.tpp:49-59
+  Solver::init            Source/Core/Solver.h:502-597
+  AmrDG::evolve / ADER    Source/NumericalMethod/AmrDG/AmrDG.h:853-1165
+  AmrDG::set_Dt           Source/NumericalMethod/AmrDG/AmrDG.h:1253-1357
+  Compressible_Euler::settings  Source/Model/CompressibleEuler/Compressible_Euler.cpp:5-48
+
+The compute path is the CUDA library only; there is no CPU fallback.  Loading
+fails loudly when the library is missing.
+"""
+import ctypes
+import os
+from math import comb
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libadg.so")
+
+ADG_OK = 0
+ADG_MEM_HOST = 0
+ADG_MEM_DEVICE = 1
+IC_CODES = {"isentropic_vortex": 0, "vortex": 0, "kh_noise": 1, "kelvin_helmolz_instability": 2,
+            "kh_ref": 2, "blast3d": 3, "const": 4}
+
+
+class AdgConfig(ctypes.Structure):
+    _fields_ = [
+        ("D", ctypes.c_int), ("P", ctypes.c_int),
+        ("gamma", ctypes.c_double), ("c_dt", ctypes.c_double),
+        ("n_cell", ctypes.c_int * 3),
+        ("prob_lo", ctypes.c_double * 3), ("prob_hi", ctypes.c_double * 3),
+        ("periodic", ctypes.c_int * 3),
+        ("ic", ctypes.c_int),
+        ("u_inf", ctypes.c_double), ("v_inf", ctypes.c_double), ("beta", ctypes.c_double),
+        ("xc", ctypes.c_double), ("yc", ctypes.c_double),
+        ("seed", ctypes.c_uint64), ("noise_amp", ctypes.c_double),
+        ("max_grid", ctypes.c_int),
+        ("max_level", ctypes.c_int), ("blocking_factor", ctypes.c_int), ("dtn_regrid", ctypes.c_int),
+        ("tag_kind", ctypes.c_int), ("tag_threshold", ctypes.c_double), ("grid_eff", ctypes.c_double),
+        ("n_error_buf", ctypes.c_int), ("reflux_box_quirk", ctypes.c_int),
+        ("picard_sweeps", ctypes.c_int), ("elems_per_block", ctypes.c_int),
+    ]
+
+
+class AdgError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Load libadg.so (built in-tree by adg_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise AdgError(f"CUDA library not built: {LIB_PATH} (run adg_gb300.build.build())")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)
+    i = ctypes.c_int
+    sig = {
+        "adg_ctx_create": ([ctypes.POINTER(AdgConfig), ctypes.POINTER(vp)], i),
+        "adg_ctx_destroy": ([vp], i),
+        "adg_last_error": ([vp], ctypes.c_char_p),
+        "adg_set_stream": ([vp, vp], i),
+        "adg_init": ([vp], i),
+        "adg_num_levels": ([vp, ctypes.POINTER(i)], i),
+        "adg_level_cells": ([vp, i, ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_get_state": ([vp, i, vp, i], i),
+        "adg_set_state": ([vp, i, vp, i], i),
+        "adg_get_dt": ([vp, dp], i),
+        "adg_set_dt": ([vp, ctypes.c_double], i),
+        "adg_compute_dt": ([vp, dp], i),
+        "adg_get_time": ([vp, dp], i),
+        "adg_ader": ([vp], i),
+        "adg_step": ([vp], i),
+        "adg_advance": ([vp, i, i], i),
+        "adg_predictor": ([vp, i, vp], i),
+        "adg_status": ([vp, ctypes.POINTER(ctypes.c_uint32)], i),
+        "adg_launch_count": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_fp64_peak_probe": ([dp], i),
+        "adg_set_device": ([i], i),
+        "adg_advance_timed": ([vp, i, i, dp], i),
+        "adg_time_kernels": ([vp, i, dp, i], i),
+        "adg_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(vp)], i),
+        "adg_host_free": ([vp], i),
+        "adg_flops_per_element": ([i, i, dp, dp], i),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def exported_symbols():
+    return [n for n in ("adg_ctx_create",) if hasattr(lib(), n)]
+
+
+class Compressible_Euler:
+    """ModelEquation<Compressible_Euler>: model case, gamma and Q
+    (Compressible_Euler.cpp:5-48)."""
+
+    def __init__(self):
+        self.model_case = "isentropic_vortex"
+        self.gamma_adiab = 1.4
+        self.ic_params = {}
+
+    def settings(self, euler_case, **ic_params):
+        self.model_case = euler_case
+        self.gamma_adiab = 5.0 / 3.0 if euler_case == "keplerian_disc" else 1.4
+        self.ic_params = dict(ic_params)
+        return self
+
+    def Q_model(self, D):
+        return D + 2
+
+
+class AmrDG:
+    """Solver<AmrDG<P>> on one GB300.
+
+    Typical use (mirrors Simulation::run):
+        model = Compressible_Euler().settings("kh_noise", seed=12345)
+        s = AmrDG(P=3, D=2)
+        s.setGeometrySettings(prob_lo=(0, 0), prob_hi=(1, 1), n_cell=(256, 256))
+        s.settings(T=1.0, c_dt=0.5)
+        s.init(model)
+        s.evolve(nsteps=100)
+    """
+
+    def __init__(self, P, D=2):
+        self.P, self.D = int(P), int(D)
+        self.Q = self.D + 2
+        self.Np_s = comb(self.P + self.D, self.D)
+        self.Np_st = comb(self.P + self.D + 1, self.D + 1)
+        self.cfg = AdgConfig()
+        c = self.cfg
+        c.D, c.P, c.gamma, c.c_dt = self.D, self.P, 1.4, 0.5
+        for d in range(3):
+            c.n_cell[d] = 1
+            c.prob_lo[d], c.prob_hi[d] = 0.0, 1.0
+            c.periodic[d] = 1
+        c.u_inf, c.v_inf, c.beta, c.xc, c.yc = 1.0, 0.0, 5.0, 5.0, 5.0
+        c.seed, c.noise_amp = 12345, 1e-3
+        c.max_grid, c.max_level, c.blocking_factor, c.dtn_regrid = 32, 0, 8, 4
+        c.tag_kind, c.tag_threshold, c.grid_eff, c.n_error_buf = 0, 0.1, 0.7, 1
+        c.reflux_box_quirk, c.picard_sweeps, c.elems_per_block = 1, 0, 0
+        self.T = None
+        self.ctx = None
+        self._L = lib()
+
+    # ------------------------------------------------------------ settings
+    def settings(self, T=None, c_dt=0.5, picard_sweeps=0, elems_per_block=0):
+        """AmrDG<P>::settings(T, c_dt, ...) (AmrDG.tpp:49-59)."""
+        self.T = T
+        self.cfg.c_dt = float(c_dt)
+        self.cfg.picard_sweeps = int(picard_sweeps)
+        self.cfg.elems_per_block = int(elems_per_block)
+        return self
+
+    def setGeometrySettings(self, prob_lo, prob_hi, n_cell, max_level=0, periodic=None, max_grid=32,
+                            blocking_factor=8, dtn_regrid=4):
+        """Simulation::setGeometrySettings (Simulation.h:120-140)."""
+        c = self.cfg
+        for d in range(3):
+            if d < self.D:
+                c.prob_lo[d], c.prob_hi[d] = float(prob_lo[d]), float(prob_hi[d])
+                c.n_cell[d] = int(n_cell[d])
+                c.periodic[d] = 1 if periodic is None else int(periodic[d])
+            else:
+                c.prob_lo[d], c.prob_hi[d], c.n_cell[d], c.periodic[d] = 0.0, 1.0, 1, 1
+        c.max_level, c.max_grid = int(max_level), int(max_grid)
+        c.blocking_factor, c.dtn_regrid = int(blocking_factor), int(dtn_regrid)
+        return self
+
+    def setAmrSettings(self, tag_kind=0, tag_threshold=0.1, grid_eff=0.7, n_error_buf=1, reflux_box_quirk=1):
+        c = self.cfg
+        c.tag_kind, c.tag_threshold, c.grid_eff = int(tag_kind), float(tag_threshold), float(grid_eff)
+        c.n_error_buf, c.reflux_box_quirk = int(n_error_buf), int(reflux_box_quirk)
+        return self
+
+    # ------------------------------------------------------------ lifecycle
+    def _check(self, rc, what):
+        if rc != ADG_OK:
+            msg = self._L.adg_last_error(self.ctx).decode() if self.ctx else ""
+            raise AdgError(f"{what} failed (status {rc}): {msg}")
+
+    def init(self, model=None):
+        """Solver::init: element matrices, layout, initial condition, first Dt."""
+        if model is not None:
+            self.cfg.gamma = model.gamma_adiab
+            self.cfg.ic = IC_CODES[model.model_case]
+            for k, v in model.ic_params.items():
+                setattr(self.cfg, k, v)
+        h = ctypes.c_void_p()
+        rc = self._L.adg_ctx_create(ctypes.byref(self.cfg), ctypes.byref(h))
+        if rc != ADG_OK:
+            raise AdgError(f"adg_ctx_create failed (status {rc})")
+        self.ctx = h
+        self._check(self._L.adg_init(self.ctx), "adg_init")
+        return self
+
+    def close(self):
+        if self.ctx:
+            self._L.adg_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ stepping
+    def set_Dt(self):
+        """Recompute Dt from the current state (AmrDG.h:1253-1357)."""
+        v = ctypes.c_double()
+        self._check(self._L.adg_compute_dt(self.ctx, ctypes.byref(v)), "adg_compute_dt")
+        return v.value
+
+    @property
+    def Dt(self):
+        v = ctypes.c_double()
+        self._check(self._L.adg_get_dt(self.ctx, ctypes.byref(v)), "adg_get_dt")
+        return v.value
+
+    @Dt.setter
+    def Dt(self, value):
+        self._check(self._L.adg_set_dt(self.ctx, float(value)), "adg_set_dt")
+
+    @property
+    def time(self):
+        v = ctypes.c_double()
+        self._check(self._L.adg_get_time(self.ctx, ctypes.byref(v)), "adg_get_time")
+        return v.value
+
+    def ADER(self):
+        """One predictor-corrector step with the current Dt (AmrDG.h:1071-1165)."""
+        self._check(self._L.adg_ader(self.ctx), "adg_ader")
+
+    def time_integration(self):
+        """One evolve-loop body: ADER, AMR sync, t += Dt, new Dt."""
+        self._check(self._L.adg_step(self.ctx), "adg_step")
+
+    def advance(self, nsteps, use_graph=True):
+        self._check(self._L.adg_advance(self.ctx, int(nsteps), int(bool(use_graph))), "adg_advance")
+
+    def evolve(self, nsteps=None, T=None):
+        """AmrDG::evolve: fixed step count, or until T with the last step clamped."""
+        T = T if T is not None else self.T
+        if nsteps is not None:
+            self.advance(nsteps)
+            return
+        while self.time < T:
+            if T - self.time < self.Dt:
+                self.Dt = T - self.time
+            self.time_integration()
+
+    # ------------------------------------------------------------ state
+    def num_levels(self):
+        n = ctypes.c_int()
+        self._check(self._L.adg_num_levels(self.ctx, ctypes.byref(n)), "adg_num_levels")
+        return n.value
+
+    def level_cells(self, lev=0):
+        n = ctypes.c_int64()
+        self._check(self._L.adg_level_cells(self.ctx, lev, ctypes.byref(n)), "adg_level_cells")
+        return n.value
+
+    def get_U_w(self, lev=0):
+        n = self.level_cells(lev)
+        out = np.empty((n, self.Q, self.Np_s))
+        self._check(self._L.adg_get_state(self.ctx, lev, out.ctypes.data, ADG_MEM_HOST), "adg_get_state")
+        return out
+
+    def set_U_w(self, arr, lev=0):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        assert a.size == self.level_cells(lev) * self.Q * self.Np_s
+        self._check(self._L.adg_set_state(self.ctx, lev, a.ctypes.data, ADG_MEM_HOST), "adg_set_state")
+
+    def get_U_w_device(self, lev, dev_ptr):
+        self._check(self._L.adg_get_state(self.ctx, lev, ctypes.c_void_p(dev_ptr), ADG_MEM_DEVICE), "adg_get_state")
+
+    def set_U_w_device(self, lev, dev_ptr):
+        self._check(self._L.adg_set_state(self.ctx, lev, ctypes.c_void_p(dev_ptr), ADG_MEM_DEVICE), "adg_set_state")
+
+    def predictor(self, lev, dev_ptr):
+        """Predictor H_w of the valid cells of level lev into a device buffer."""
+        self._check(self._L.adg_predictor(self.ctx, lev, ctypes.c_void_p(dev_ptr)), "adg_predictor")
+
+    def status(self):
+        v = ctypes.c_uint32()
+        self._check(self._L.adg_status(self.ctx, ctypes.byref(v)), "adg_status")
+        return v.value
+
+    def launch_count(self):
+        v = ctypes.c_int64()
+        self._check(self._L.adg_launch_count(self.ctx, ctypes.byref(v)), "adg_launch_count")
+        return v.value
+
+    def advance_timed(self, nsteps, use_graph=True):
+        """n steps bracketed by CUDA events on the context's stream; returns ms."""
+        v = ctypes.c_double()
+        self._check(self._L.adg_advance_timed(self.ctx, int(nsteps), int(bool(use_graph)), ctypes.byref(v)),
+                    "adg_advance_timed")
+        return v.value
+
+    def time_kernels(self, nsteps=3):
+        """Average per-step duration (ms) of each kernel kind, CUDA events."""
+        out = (ctypes.c_double * 5)()
+        self._check(self._L.adg_time_kernels(self.ctx, int(nsteps), out, 5), "adg_time_kernels")
+        return {"predictor": out[0], "numflux": out[1], "corrector": out[2], "dt": out[3], "amr_sync": out[4]}
+
+    def set_stream(self, stream_handle):
+        self._check(self._L.adg_set_stream(self.ctx, ctypes.c_void_p(stream_handle)), "adg_set_stream")
+
+
+def set_device(dev):
+    rc = lib().adg_set_device(int(dev))
+    if rc != ADG_OK:
+        raise AdgError(f"adg_set_device({dev}) failed")
+
+
+class PinnedArray:
+    """numpy view of a page-locked host buffer allocated by the library."""
+
+    def __init__(self, shape):
+        n = int(np.prod(shape)) * 8
+        self._p = ctypes.c_void_p()
+        if lib().adg_host_alloc(n, ctypes.byref(self._p)) != ADG_OK:
+            raise AdgError("adg_host_alloc failed")
+        buf = (ctypes.c_double * int(np.prod(shape))).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=np.float64).reshape(shape)
+
+    def free(self):
+        if self._p:
+            lib().adg_host_free(self._p)
+            self._p = None
+
+
+def fp64_peak_gflops():
+    v = ctypes.c_double()
+    rc = lib().adg_fp64_peak_probe(ctypes.byref(v))
+    if rc != ADG_OK:
+        raise AdgError(f"adg_fp64_peak_probe failed ({rc})")
+    return v.value
+
+
+def flops_per_element(D, P):
+    a, b = ctypes.c_double(), ctypes.c_double()
+    rc = lib().adg_flops_per_element(D, P, ctypes.byref(a), ctypes.byref(b))
+    if rc != ADG_OK:
+        raise AdgError("unsupported (D, P)")
+    return a.value, b.value

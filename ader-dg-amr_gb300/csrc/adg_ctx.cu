@@ -1,0 +1,634 @@
+// Host side of the GB300 ADER-DG element path: context, device buffers,
+// element/face tables of the layout, step sequencing (with CUDA-graph replay)
+// and the C ABI declared in include/adg.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "adg.h"
+#include "adg_kernelset.hpp"
+#include "adg_layout.hpp"
+
+namespace adg {
+
+// Device buffer that grows on demand and is freed with the context.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// t += Dt; Dt = c_dt * min; reset the accumulator (AmrDG.h:1019, 1356).
+__global__ void k_dt_finalize(double* dt, double* t, unsigned long long* min_bits, double c_dt, int advance_time) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    if (advance_time) *t += *dt;
+    *dt = c_dt * __longlong_as_double((long long)*min_bits);
+    *min_bits = (unsigned long long)__double_as_longlong(1.0e300);
+  }
+}
+
+// FP64 throughput probe: independent DFMA chains.
+__global__ void k_fp64_probe(double* out, int iters) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  double a0 = tid * 1e-9, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+  const double b = 0.999, c = 0.001;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+      a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+    }
+  }
+  out[tid] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+}  // namespace adg
+
+using namespace adg;
+
+struct adg_ctx {
+  adg_config cfg{};
+  const KernelSet* ks = nullptr;
+  int E = 0;  // elements per predictor block
+  int sweeps = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  long long launches = 0;
+
+  Hierarchy hier;       // host layout (levels, boxes, element and face tables)
+  bool initialised = false;
+  bool tables_dirty = true;
+
+  // device state
+  DevBuf<double> Uw, Rvol, Tr, Fnum, Hw_dbg;
+  DevBuf<int> face_left, face_right, elem_face, elem_cell;
+  DevBuf<int8_t> elem_level;
+  DevBuf<double> scal;  // [0] Dt, [1] t
+  DevBuf<unsigned long long> min_bits;
+  DevBuf<unsigned int> status;
+
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_kernels = 0;
+
+  ~adg_ctx() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    Uw.release(); Rvol.release(); Tr.release(); Fnum.release(); Hw_dbg.release();
+    face_left.release(); face_right.release(); elem_face.release(); elem_cell.release();
+    elem_level.release(); scal.release(); min_bits.release(); status.release();
+    if (own_stream && stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+int fail(adg_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(adg_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, ADG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define ADG_CUDA(call, where)                  \
+  do {                                         \
+    cudaError_t _e = (call);                   \
+    if (_e != cudaSuccess) return cuda_fail(ctx, _e, where); \
+  } while (0)
+
+LevelGeom level_geom(const adg_ctx* ctx) {
+  LevelGeom g{};
+  for (int l = 0; l < kMaxLevels; ++l)
+    for (int d = 0; d < 3; ++d) {
+      int n = ctx->cfg.n_cell[d] << l;
+      g.dx[l][d] = (d < ctx->cfg.D) ? (ctx->cfg.prob_hi[d] - ctx->cfg.prob_lo[d]) / n : 1.0;
+    }
+  return g;
+}
+
+// Upload element and face tables of the current layout and size the work
+// buffers.
+int upload_tables(adg_ctx* ctx) {
+  const Hierarchy& H = ctx->hier;
+  const KernelSet* ks = ctx->ks;
+  const int D = ctx->cfg.D, Q = ks->Q;
+  const size_t ne = H.n_elem();
+  const size_t nf = H.face_left.size();
+  ADG_CUDA(ctx->Rvol.ensure(ne * Q * ks->Np_s), "alloc Rvol");
+  ADG_CUDA(ctx->Tr.ensure(ne * 2 * D * (2 * Q + 1) * (size_t)ks->NQ_BD), "alloc traces");
+  ADG_CUDA(ctx->Fnum.ensure(nf * Q * (size_t)ks->NQ_BD), "alloc Fnum");
+  ADG_CUDA(ctx->face_left.ensure(nf), "alloc faces");
+  ADG_CUDA(ctx->face_right.ensure(nf), "alloc faces");
+  ADG_CUDA(ctx->elem_face.ensure(ne * 2 * D), "alloc elem faces");
+  ADG_CUDA(ctx->elem_cell.ensure(ne * 3), "alloc elem cells");
+  ADG_CUDA(ctx->elem_level.ensure(ne), "alloc elem levels");
+  cudaStream_t s = ctx->stream;
+  ADG_CUDA(cudaMemcpyAsync(ctx->face_left.p, H.face_left.data(), nf * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
+  ADG_CUDA(cudaMemcpyAsync(ctx->face_right.p, H.face_right.data(), nf * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
+  ADG_CUDA(cudaMemcpyAsync(ctx->elem_face.p, H.elem_face.data(), H.elem_face.size() * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
+  ADG_CUDA(cudaMemcpyAsync(ctx->elem_cell.p, H.elem_cell.data(), H.elem_cell.size() * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
+  ADG_CUDA(cudaMemcpyAsync(ctx->elem_level.p, H.elem_level.data(), H.elem_level.size(), cudaMemcpyHostToDevice, s), "h2d");
+  ADG_CUDA(cudaStreamSynchronize(s), "sync tables");
+  ctx->tables_dirty = false;
+  if (ctx->graph_exec) {
+    cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+  }
+  if (ctx->graph) {
+    cudaGraphDestroy(ctx->graph);
+    ctx->graph = nullptr;
+  }
+  return ADG_OK;
+}
+
+// ADER of every level with the current device Dt (AmrDG.h:1071-1165).
+int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
+  const Hierarchy& H = ctx->hier;
+  const KernelSet* ks = ctx->ks;
+  const int D = ctx->cfg.D;
+  PredictorArgs pa{};
+  pa.Uw = ctx->Uw.p;
+  pa.n_elem = (int)H.n_elem();
+  pa.elem_level = H.nlevels() > 1 ? ctx->elem_level.p : nullptr;
+  pa.geom = level_geom(ctx);
+  pa.gamma = ctx->cfg.gamma;
+  pa.dt = ctx->scal.p;
+  pa.sweeps = ctx->sweeps;
+  pa.Rvol = ctx->Rvol.p;
+  pa.Tr = ctx->Tr.p;
+  pa.Hw_out = hw_out;
+  if (ev) cudaEventRecord(ev[0], ctx->stream);
+  cudaError_t e = ks->predictor(pa, ctx->E, ctx->stream);
+  if (ev) cudaEventRecord(ev[1], ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "predictor launch");
+  ctx->launches++;
+
+  FaceArgs fa{};
+  fa.Tr = ctx->Tr.p;
+  fa.face_left = ctx->face_left.p;
+  fa.face_right = ctx->face_right.p;
+  for (int d = 0; d <= 3; ++d) fa.face_off[d] = (d <= D) ? H.face_off[d] : H.face_off[D];
+  fa.Fnum = ctx->Fnum.p;
+  e = ks->numflux(fa, (long long)H.face_left.size(), ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "numflux launch");
+  ctx->launches++;
+  if (ev) cudaEventRecord(ev[2], ctx->stream);
+
+  CorrectorArgs ca{};
+  ca.Uw = ctx->Uw.p;
+  ca.Rvol = ctx->Rvol.p;
+  ca.Fnum = ctx->Fnum.p;
+  ca.elem_face = ctx->elem_face.p;
+  ca.n_valid = (int)H.n_valid();
+  ca.elem_level = pa.elem_level;
+  ca.geom = pa.geom;
+  ca.dt = ctx->scal.p;
+  e = ks->corrector(ca, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "corrector launch");
+  ctx->launches++;
+  if (ev) cudaEventRecord(ev[3], ctx->stream);
+  return ADG_OK;
+}
+
+// Dt from the current state; advance_time adds the old Dt to t first.
+int launch_dt(adg_ctx* ctx, int advance_time) {
+  const Hierarchy& H = ctx->hier;
+  DtArgs da{};
+  da.Uw = ctx->Uw.p;
+  da.n_valid = (int)H.n_valid();
+  da.elem_level = H.nlevels() > 1 ? ctx->elem_level.p : nullptr;
+  LevelGeom g = level_geom(ctx);
+  for (int l = 0; l < kMaxLevels; ++l) {
+    double s = 0.0;
+    for (int d = 0; d < ctx->cfg.D; ++d) s += g.dx[l][d];
+    da.dx_avg[l] = s / (double)ctx->cfg.D;
+  }
+  da.gamma = ctx->cfg.gamma;
+  da.min_bits = ctx->min_bits.p;
+  da.status = ctx->status.p;
+  cudaError_t e = ctx->ks->dt_reduce(da, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "dt launch");
+  k_dt_finalize<<<1, 32, 0, ctx->stream>>>(ctx->scal.p, ctx->scal.p + 1, ctx->min_bits.p, ctx->cfg.c_dt, advance_time);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "dt finalize launch");
+  ctx->launches += 2;
+  return ADG_OK;
+}
+
+int launch_step(adg_ctx* ctx, cudaEvent_t* ev = nullptr) {
+  int rc = launch_ader(ctx, nullptr, ev);
+  if (rc) return rc;
+  rc = launch_dt(ctx, 1);
+  if (ev) cudaEventRecord(ev[4], ctx->stream);
+  return rc;
+}
+
+int check_ready(adg_ctx* ctx) {
+  if (!ctx) return ADG_ERR_ARG;
+  if (!ctx->initialised) return fail(ctx, ADG_ERR_STATE, "adg_init has not been called");
+  if (ctx->tables_dirty) return upload_tables(ctx);
+  return ADG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int adg_ctx_create(const adg_config* cfg, adg_ctx** out) {
+  if (!cfg || !out) return ADG_ERR_ARG;
+  *out = nullptr;
+  const KernelSet* ks = kernel_set(cfg->D, cfg->P);
+  if (!ks) return ADG_ERR_ARG;
+  for (int d = 0; d < cfg->D; ++d)
+    if (cfg->n_cell[d] <= 0 || !(cfg->prob_hi[d] > cfg->prob_lo[d])) return ADG_ERR_ARG;
+  if (cfg->max_level < 0 || cfg->max_level >= kMaxLevels) return ADG_ERR_ARG;
+  if (!(cfg->gamma > 1.0) || !(cfg->c_dt > 0.0)) return ADG_ERR_ARG;
+  adg_ctx* ctx = new adg_ctx();
+  ctx->cfg = *cfg;
+  ctx->ks = ks;
+  ctx->sweeps = cfg->picard_sweeps > 0 ? cfg->picard_sweeps : cfg->P;
+  if (ctx->sweeps < 1) ctx->sweeps = 1;
+  std::vector<int> ch = ks->elems_per_block_choices();
+  ctx->E = (cfg->elems_per_block > 0 && std::find(ch.begin(), ch.end(), cfg->elems_per_block) != ch.end())
+               ? cfg->elems_per_block
+               : (cfg->D == 2 ? 16 : 8);
+  cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return ADG_ERR_CUDA;
+  }
+  ctx->own_stream = true;
+  if (ctx->scal.ensure(2) != cudaSuccess || ctx->min_bits.ensure(1) != cudaSuccess || ctx->status.ensure(1) != cudaSuccess) {
+    delete ctx;
+    return ADG_ERR_CUDA;
+  }
+  double z[2] = {0.0, 0.0};
+  unsigned long long big = 0;
+  double huge = 1.0e300;
+  std::memcpy(&big, &huge, sizeof(big));
+  unsigned int zero = 0;
+  if (cudaMemcpy(ctx->scal.p, z, sizeof(z), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->min_bits.p, &big, sizeof(big), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->status.p, &zero, sizeof(zero), cudaMemcpyHostToDevice) != cudaSuccess) {
+    delete ctx;
+    return ADG_ERR_CUDA;
+  }
+  *out = ctx;
+  return ADG_OK;
+}
+
+int adg_ctx_destroy(adg_ctx* ctx) {
+  if (!ctx) return ADG_ERR_ARG;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  delete ctx;
+  return ADG_OK;
+}
+
+const char* adg_last_error(const adg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int adg_set_stream(adg_ctx* ctx, void* stream) {
+  if (!ctx) return ADG_ERR_ARG;
+  if (ctx->own_stream && ctx->stream) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+  }
+  ctx->stream = (cudaStream_t)stream;
+  ctx->own_stream = false;
+  if (ctx->graph_exec) {
+    cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+  }
+  return ADG_OK;
+}
+
+int adg_init(adg_ctx* ctx) {
+  if (!ctx) return ADG_ERR_ARG;
+  const adg_config& c = ctx->cfg;
+  std::string msg;
+  if (!ctx->hier.build_single_level(c, &msg)) return fail(ctx, ADG_ERR_LAYOUT, msg);
+  const KernelSet* ks = ctx->ks;
+  const size_t ne = ctx->hier.n_elem();
+  ADG_CUDA(ctx->Uw.ensure(ne * ks->Q * ks->Np_s), "alloc Uw");
+  int rc = upload_tables(ctx);
+  if (rc) return rc;
+  ICArgs ia{};
+  ia.Uw = ctx->Uw.p;
+  ia.elem_cell = ctx->elem_cell.p;
+  ia.elem_level = nullptr;
+  ia.n_elem = (int)ne;
+  ia.geom = level_geom(ctx);
+  for (int d = 0; d < 3; ++d) {
+    ia.prob_lo[d] = c.prob_lo[d];
+    ia.n_cell0[d] = c.n_cell[d];
+  }
+  ia.gamma = c.gamma;
+  ia.icp.ic = c.ic;
+  ia.icp.u_inf = c.u_inf;
+  ia.icp.v_inf = c.v_inf;
+  ia.icp.beta = c.beta;
+  ia.icp.xc = c.xc;
+  ia.icp.yc = c.yc;
+  ia.icp.seed = c.seed;
+  ia.icp.noise_amp = c.noise_amp;
+  cudaError_t e = ks->init_ic(ia, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "init_ic launch");
+  ctx->launches++;
+  ctx->initialised = true;
+  rc = launch_dt(ctx, 0);
+  if (rc) return rc;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "init sync");
+  return ADG_OK;
+}
+
+int adg_num_levels(const adg_ctx* ctx, int* nlev) {
+  if (!ctx || !nlev) return ADG_ERR_ARG;
+  *nlev = ctx->hier.nlevels();
+  return ADG_OK;
+}
+
+int adg_level_cells(const adg_ctx* ctx, int lev, int64_t* ncells) {
+  if (!ctx || !ncells || lev < 0 || lev >= ctx->hier.nlevels()) return ADG_ERR_ARG;
+  *ncells = (int64_t)ctx->hier.level_valid_count(lev);
+  return ADG_OK;
+}
+
+int adg_get_state(adg_ctx* ctx, int lev, double* dst, int mem) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!dst || lev < 0 || lev >= ctx->hier.nlevels()) return fail(ctx, ADG_ERR_ARG, "bad level or pointer");
+  const size_t per = (size_t)ctx->ks->Q * ctx->ks->Np_s;
+  const size_t off = ctx->hier.level_valid_offset(lev) * per;
+  const size_t cnt = ctx->hier.level_valid_count(lev) * per;
+  ADG_CUDA(cudaMemcpyAsync(dst, ctx->Uw.p + off, cnt * sizeof(double),
+                           mem == ADG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream),
+           "get_state copy");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "get_state sync");
+  return ADG_OK;
+}
+
+int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!src || lev < 0 || lev >= ctx->hier.nlevels()) return fail(ctx, ADG_ERR_ARG, "bad level or pointer");
+  const size_t per = (size_t)ctx->ks->Q * ctx->ks->Np_s;
+  const size_t off = ctx->hier.level_valid_offset(lev) * per;
+  const size_t cnt = ctx->hier.level_valid_count(lev) * per;
+  ADG_CUDA(cudaMemcpyAsync(ctx->Uw.p + off, src, cnt * sizeof(double),
+                           mem == ADG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream),
+           "set_state copy");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "set_state sync");
+  return ADG_OK;
+}
+
+int adg_get_dt(adg_ctx* ctx, double* dt) {
+  if (!ctx || !dt) return ADG_ERR_ARG;
+  ADG_CUDA(cudaMemcpyAsync(dt, ctx->scal.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "get_dt");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "get_dt sync");
+  return ADG_OK;
+}
+
+int adg_set_dt(adg_ctx* ctx, double dt) {
+  if (!ctx || !(dt > 0.0)) return ADG_ERR_ARG;
+  ADG_CUDA(cudaMemcpyAsync(ctx->scal.p, &dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "set_dt");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "set_dt sync");
+  return ADG_OK;
+}
+
+int adg_compute_dt(adg_ctx* ctx, double* dt) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  rc = launch_dt(ctx, 0);
+  if (rc) return rc;
+  if (dt) return adg_get_dt(ctx, dt);
+  return ADG_OK;
+}
+
+int adg_get_time(adg_ctx* ctx, double* t) {
+  if (!ctx || !t) return ADG_ERR_ARG;
+  ADG_CUDA(cudaMemcpyAsync(t, ctx->scal.p + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "get_time");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "get_time sync");
+  return ADG_OK;
+}
+
+int adg_ader(adg_ctx* ctx) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  rc = launch_ader(ctx, nullptr);
+  if (rc) return rc;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "ader sync");
+  return ADG_OK;
+}
+
+int adg_step(adg_ctx* ctx) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  rc = launch_step(ctx);
+  if (rc) return rc;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "step sync");
+  return ADG_OK;
+}
+
+int adg_advance(adg_ctx* ctx, int nsteps, int use_graph) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (nsteps < 0) return fail(ctx, ADG_ERR_ARG, "negative step count");
+  if (!use_graph) {
+    for (int s = 0; s < nsteps; ++s) {
+      rc = launch_step(ctx);
+      if (rc) return rc;
+    }
+    return ADG_OK;
+  }
+  if (!ctx->graph_exec) {
+    long long before = ctx->launches;
+    ADG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    rc = launch_step(ctx);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "end capture");
+    ctx->graph = g;
+    ADG_CUDA(cudaGraphInstantiate(&ctx->graph_exec, g, 0), "graph instantiate");
+    ctx->graph_kernels = (int)(ctx->launches - before);
+    ctx->launches = before;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    ADG_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream), "graph launch");
+    ctx->launches += ctx->graph_kernels;
+  }
+  return ADG_OK;
+}
+
+int adg_set_device(int device) {
+  return cudaSetDevice(device) == cudaSuccess ? ADG_OK : ADG_ERR_CUDA;
+}
+
+int adg_advance_timed(adg_ctx* ctx, int nsteps, int use_graph, double* ms) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!ms) return ADG_ERR_ARG;
+  if (use_graph && !ctx->graph_exec) {  // capture outside the timed region
+    rc = adg_advance(ctx, 0, 1);
+    if (rc) return rc;
+  }
+  cudaEvent_t e0, e1;
+  ADG_CUDA(cudaEventCreate(&e0), "event");
+  ADG_CUDA(cudaEventCreate(&e1), "event");
+  cudaEventRecord(e0, ctx->stream);
+  rc = adg_advance(ctx, nsteps, use_graph);
+  cudaEventRecord(e1, ctx->stream);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float f = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&f, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "timed advance");
+  *ms = f;
+  return ADG_OK;
+}
+
+int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!ms || nkinds < 1 || nsteps < 1) return ADG_ERR_ARG;
+  const int NEV = 5;
+  std::vector<cudaEvent_t> ev((size_t)NEV * nsteps);
+  for (auto& x : ev) ADG_CUDA(cudaEventCreate(&x), "event");
+  for (int s = 0; s < nsteps && rc == ADG_OK; ++s) rc = launch_step(ctx, &ev[(size_t)s * NEV]);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  double acc[5] = {0, 0, 0, 0, 0};
+  if (rc == ADG_OK && e == cudaSuccess) {
+    for (int s = 0; s < nsteps; ++s)
+      for (int k = 0; k < 4; ++k) {
+        float f = 0.f;
+        cudaEventElapsedTime(&f, ev[(size_t)s * NEV + k], ev[(size_t)s * NEV + k + 1]);
+        acc[k] += f;
+      }
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "time kernels");
+  for (int k = 0; k < nkinds; ++k) ms[k] = (k < 5) ? acc[k] / nsteps : 0.0;
+  return ADG_OK;
+}
+
+int adg_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return ADG_ERR_ARG;
+  return cudaHostAlloc(ptr, bytes, cudaHostAllocDefault) == cudaSuccess ? ADG_OK : ADG_ERR_CUDA;
+}
+
+int adg_host_free(void* ptr) { return cudaFreeHost(ptr) == cudaSuccess ? ADG_OK : ADG_ERR_CUDA; }
+
+int adg_predictor(adg_ctx* ctx, int lev, double* dst_dev) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!dst_dev || lev < 0 || lev >= ctx->hier.nlevels()) return fail(ctx, ADG_ERR_ARG, "bad level or pointer");
+  const size_t ne = ctx->hier.n_elem();
+  const size_t per = (size_t)ctx->ks->Q * ctx->ks->Np_st;
+  ADG_CUDA(ctx->Hw_dbg.ensure(ne * per), "alloc Hw");
+  // Run the ADER stages on a scratch copy of the state so the state is unchanged.
+  DevBuf<double> save;
+  ADG_CUDA(save.ensure(ctx->Uw.n), "alloc save");
+  ADG_CUDA(cudaMemcpyAsync(save.p, ctx->Uw.p, ctx->Uw.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream), "save");
+  rc = launch_ader(ctx, ctx->Hw_dbg.p);
+  if (rc) {
+    save.release();
+    return rc;
+  }
+  ADG_CUDA(cudaMemcpyAsync(ctx->Uw.p, save.p, ctx->Uw.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream), "restore");
+  const size_t off = ctx->hier.level_valid_offset(lev) * per;
+  const size_t cnt = ctx->hier.level_valid_count(lev) * per;
+  ADG_CUDA(cudaMemcpyAsync(dst_dev, ctx->Hw_dbg.p + off, cnt * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream), "hw copy");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "predictor sync");
+  save.release();
+  return ADG_OK;
+}
+
+int adg_status(adg_ctx* ctx, uint32_t* st) {
+  if (!ctx || !st) return ADG_ERR_ARG;
+  unsigned int v = 0, zero = 0;
+  ADG_CUDA(cudaMemcpyAsync(&v, ctx->status.p, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream), "status");
+  ADG_CUDA(cudaMemcpyAsync(ctx->status.p, &zero, sizeof(zero), cudaMemcpyHostToDevice, ctx->stream), "status clear");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "status sync");
+  *st = v;
+  return ADG_OK;
+}
+
+int adg_launch_count(const adg_ctx* ctx, int64_t* n) {
+  if (!ctx || !n) return ADG_ERR_ARG;
+  *n = ctx->launches;
+  return ADG_OK;
+}
+
+int adg_fp64_peak_probe(double* gflops) {
+  if (!gflops) return ADG_ERR_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return ADG_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ADG_ERR_CUDA;
+  const int blocks = sms * 8, threads = 256, iters = 1000;
+  double* out = nullptr;
+  if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return ADG_ERR_CUDA;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fp64_probe<<<blocks, threads>>>(out, 16);
+  float best = 1e30f;
+  for (int r = 0; r < 3; ++r) {
+    cudaEventRecord(e0);
+    k_fp64_probe<<<blocks, threads>>>(out, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess) return ADG_ERR_CUDA;
+  const double flops = 2.0 * 32.0 * iters * (double)blocks * threads;
+  *gflops = flops / (best * 1e-3) / 1e9;
+  return ADG_OK;
+}
+
+int adg_flops_per_element(int D, int P, double* algorithmic, double* issued) {
+  const KernelSet* ks = kernel_set(D, P);
+  if (!ks) return ADG_ERR_ARG;
+  const double Q = ks->Q, Nps = ks->Np_s, Npst = ks->Np_st, qst = ks->NQ_ST, qbd = ks->NQ_BD;
+  // Dense matvec count of the method (stage-wise reference formulation,
+  // Mk_pred U hoisted out of the sweep loop).
+  const double Fp = 2 * Q * Npst * Nps + P * 2 * Q * (qst * Npst + D * Npst * qst + Npst * Npst);
+  const double Fc = 2 * Q * qst * Npst + 2 * D * 2 * Q * qbd * Npst + 2 * Q * (D * Nps * qst + 2 * D * Nps * qbd) + 2 * Q * Nps;
+  if (algorithmic) *algorithmic = Fp + Fc;
+  if (issued) *issued = Q * (double)ks->linear_fp64_per_column;
+  return ADG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,96 @@
+// One (D, P) instantiation of the kernel set.  The build compiles this file
+// once per configuration with -DADG_D, -DADG_HDR (generated operator header),
+// -DADG_NS (its namespace) and -DADG_FACTORY (factory function name).
+#include "adg_kernelset.hpp"
+#include ADG_HDR
+
+namespace adg {
+namespace {
+
+using O = ADG_NS::Ops;
+
+template <int E>
+constexpr size_t smem_bytes() {
+  constexpr int a = O::D * O::NQ_ST, b = 2 * O::D * O::NQ_BD;
+  return (size_t)(a > b ? a : b) * (E * O::Q + 1) * sizeof(double);
+}
+
+template <int E>
+cudaError_t launch_predictor(const PredictorArgs& a, cudaStream_t s) {
+  constexpr size_t smem = smem_bytes<E>();
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_predictor<O, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const int grid = (a.n_elem + E - 1) / E;
+  k_predictor<O, E><<<grid, E * O::Q, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+struct Impl final : KernelSet {
+  Impl() {
+    D = O::D;
+    P = O::P;
+    Q = O::Q;
+    Np_s = O::NP_S;
+    Np_st = O::NP_ST;
+    NQ_ST = O::NQ_ST;
+    NQ_BD = O::NQ_BD;
+    NQ_S = O::NQ_S;
+    linear_fp64_per_column = O::LINEAR_FP64_PER_COLUMN;
+  }
+#if ADG_D == 2
+  std::vector<int> elems_per_block_choices() const override { return {8, 16, 32}; }
+  size_t predictor_smem(int E) const override {
+    return E == 8 ? smem_bytes<8>() : E == 16 ? smem_bytes<16>() : smem_bytes<32>();
+  }
+  cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s) const override {
+    if (E == 8) return launch_predictor<8>(a, s);
+    if (E == 16) return launch_predictor<16>(a, s);
+    return launch_predictor<32>(a, s);
+  }
+#else
+  std::vector<int> elems_per_block_choices() const override { return {4, 8, 16}; }
+  size_t predictor_smem(int E) const override {
+    return E == 4 ? smem_bytes<4>() : E == 8 ? smem_bytes<8>() : smem_bytes<16>();
+  }
+  cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s) const override {
+    if (E == 4) return launch_predictor<4>(a, s);
+    if (E == 8) return launch_predictor<8>(a, s);
+    return launch_predictor<16>(a, s);
+  }
+#endif
+  cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s) const override {
+    const long long n = nface * O::NQ_BD;
+    const int bs = 256;
+    k_numflux<O><<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const override {
+    const long long n = (long long)a.n_valid * O::Q;
+    const int bs = 128;
+    k_corrector<O><<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  cudaError_t dt_reduce(const DtArgs& a, cudaStream_t s) const override {
+    const int bs = 256;
+    k_dt_reduce<O><<<(a.n_valid + bs - 1) / bs, bs, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const override {
+    const int bs = 64;
+    k_init_ic<O><<<(a.n_elem + bs - 1) / bs, bs, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+};
+
+}  // namespace
+
+const KernelSet* ADG_FACTORY() {
+  static Impl impl;
+  return &impl;
+}
+
+}  // namespace adg

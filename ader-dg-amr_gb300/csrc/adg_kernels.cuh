@@ -1,0 +1,392 @@
+// sm_103a kernels of the ADER-DG element path.
+//
+// Data layout (HBM, FP64):
+//   Uw    [elem][q][n]                 n < Np_s   (spatial modes)
+//   Rvol  [elem][q][n]                 M U + sum_d (Dt/dx_d) Sk_corr[d] F_d
+//   Tr    [elem][face 2d+s][field][m]  field: u_q (Q), f_q (Q), |un|+c (1); m < NQ_BD
+//   Fnum  [face][q][m]                 local Lax-Friedrichs flux at face points
+// Element-level work is organised in "columns": one thread owns one
+// (element, variable) pair and runs the generated straight-line FP64
+// operators on it; point-wise physics runs one thread per (element, point).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "adg_device.cuh"
+
+namespace adg {
+
+constexpr int kMaxLevels = 8;
+
+struct LevelGeom {
+  double dx[kMaxLevels][3];
+};
+
+struct PredictorArgs {
+  const double* Uw;
+  int n_elem;                 // elements that need a predictor (valid + ghost)
+  const int8_t* elem_level;   // nullptr: all level 0
+  LevelGeom geom;
+  double gamma;
+  const double* dt;           // device scalar
+  int sweeps;
+  double* Rvol;
+  double* Tr;
+  double* Hw_out;             // optional: final H_w per element [elem][q][Np_st]
+};
+
+// Point-wise flux stage: H at NQ points of E elements (shared, [point][col])
+// -> F_d for every direction d, written over H (d = 0) and into the next
+// NQ x ld slabs (d >= 1).
+template <class O, int E, int NQ>
+__device__ __forceinline__ void flux_stage(double* sm, int ld, double gm1) {
+  constexpr int Q = O::Q, D = O::D;
+  for (int it = threadIdx.x; it < E * NQ; it += blockDim.x) {
+    const int m = it % NQ;
+    const int e = it / NQ;
+    double* base = sm + m * ld + e * Q;
+    double u[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) u[q] = base[q];
+    double F[D * Q];
+    euler_flux_all<D>(u, gm1, F);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+#pragma unroll
+      for (int q = 0; q < Q; ++q) base[d * NQ * ld + q] = F[d * Q + q];
+  }
+}
+
+template <class O, int E>
+__global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NP_ST = O::NP_ST;
+  constexpr int NQ = O::NQ_ST, NB = O::NQ_BD, NI = O::NQ_INIT;
+  constexpr int NCOL = E * Q;
+  constexpr int LD = NCOL + 1;  // odd stride: conflict-free point-major access
+  extern __shared__ double sm[];
+
+  const int col = threadIdx.x;
+  const int el = col / Q;
+  const int q = col % Q;
+  const int e_raw = blockIdx.x * E + el;
+  const bool live = e_raw < a.n_elem;
+  const int e = live ? e_raw : (a.n_elem - 1);
+  const int lev = a.elem_level ? a.elem_level[e] : 0;
+  const double dt = *a.dt;
+  double c[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) c[d] = dt / a.geom.dx[lev][d];
+  const double gm1 = a.gamma - 1.0;
+
+  double u[NP_S];
+  const double* src = a.Uw + ((size_t)e * Q + q) * NP_S;
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) u[n] = src[n];
+
+  double wu[NP_ST];
+  O::wu(RegIn{u}, RegOut{wu});
+  double hw[NP_ST];
+
+  // ---- sweep 1: the reference's initial guess H_w = [U_w, 0, ...]
+  // (AmrDG.tpp:520-533) does not depend on x_0; evaluate on the (x_1.., t) grid.
+  O::vol_eval_init(RegIn{u}, ColOut{sm + col, LD});
+  __syncthreads();
+  flux_stage<O, E, NI>(sm, LD, gm1);
+  __syncthreads();
+#pragma unroll
+  for (int n = 0; n < NP_ST; ++n) hw[n] = wu[n];
+  {
+    double y[NP_ST];
+    O::template proj_init<0>(ColIn{sm + col, LD}, RegOut{y});
+#pragma unroll
+    for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[0], y[n], hw[n]);
+    O::template proj_init<1>(ColIn{sm + NI * LD + col, LD}, RegOut{y});
+#pragma unroll
+    for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[1], y[n], hw[n]);
+    if constexpr (D == 3) {
+      O::template proj_init<2>(ColIn{sm + 2 * NI * LD + col, LD}, RegOut{y});
+#pragma unroll
+      for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[2], y[n], hw[n]);
+    }
+  }
+  __syncthreads();
+
+  // ---- remaining Picard sweeps (AmrDG.h:1103-1119)
+  for (int s = 1; s < a.sweeps; ++s) {
+    O::vol_eval(RegIn{hw}, ColOut{sm + col, LD});
+    __syncthreads();
+    flux_stage<O, E, NQ>(sm, LD, gm1);
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < NP_ST; ++n) hw[n] = wu[n];
+    double y[NP_ST];
+    O::template proj<0>(ColIn{sm + col, LD}, RegOut{y});
+#pragma unroll
+    for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[0], y[n], hw[n]);
+    O::template proj<1>(ColIn{sm + NQ * LD + col, LD}, RegOut{y});
+#pragma unroll
+    for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[1], y[n], hw[n]);
+    if constexpr (D == 3) {
+      O::template proj<2>(ColIn{sm + 2 * NQ * LD + col, LD}, RegOut{y});
+#pragma unroll
+      for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[2], y[n], hw[n]);
+    }
+    __syncthreads();
+  }
+
+  if (a.Hw_out && live) {
+    double* dst = a.Hw_out + ((size_t)e * Q + q) * NP_ST;
+#pragma unroll
+    for (int n = 0; n < NP_ST; ++n) dst[n] = hw[n];
+  }
+
+  // ---- corrector volume term (AmrDG.tpp:696-709): M U + sum_d c_d Sk_corr[d] F_d
+  O::vol_eval(RegIn{hw}, ColOut{sm + col, LD});
+  __syncthreads();
+  flux_stage<O, E, NQ>(sm, LD, gm1);
+  __syncthreads();
+  {
+    double R[NP_S], v[NP_S];
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) R[n] = O::mdiag(n) * u[n];
+    O::template vol_term<0>(ColIn{sm + col, LD}, RegOut{v});
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[0], v[n], R[n]);
+    O::template vol_term<1>(ColIn{sm + NQ * LD + col, LD}, RegOut{v});
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[1], v[n], R[n]);
+    if constexpr (D == 3) {
+      O::template vol_term<2>(ColIn{sm + 2 * NQ * LD + col, LD}, RegOut{v});
+#pragma unroll
+      for (int n = 0; n < NP_S; ++n) R[n] = fma(c[2], v[n], R[n]);
+    }
+    if (live) {
+      double* dst = a.Rvol + ((size_t)e * Q + q) * NP_S;
+#pragma unroll
+      for (int n = 0; n < NP_S; ++n) dst[n] = R[n];
+    }
+  }
+  __syncthreads();
+
+  // ---- face traces of H (AmrDG.tpp:437-493) and face physics (AmrDG.h:1207-1251)
+  O::template face_eval<0, 0>(RegIn{hw}, ColOut{sm + 0 * NB * LD + col, LD});
+  O::template face_eval<0, 1>(RegIn{hw}, ColOut{sm + 1 * NB * LD + col, LD});
+  O::template face_eval<1, 0>(RegIn{hw}, ColOut{sm + 2 * NB * LD + col, LD});
+  O::template face_eval<1, 1>(RegIn{hw}, ColOut{sm + 3 * NB * LD + col, LD});
+  if constexpr (D == 3) {
+    O::template face_eval<2, 0>(RegIn{hw}, ColOut{sm + 4 * NB * LD + col, LD});
+    O::template face_eval<2, 1>(RegIn{hw}, ColOut{sm + 5 * NB * LD + col, LD});
+  }
+  __syncthreads();
+  constexpr int NF = 2 * D;
+  constexpr int NFIELD = 2 * Q + 1;
+  const int e0 = blockIdx.x * E;
+  for (int it = threadIdx.x; it < E * NF * NB; it += blockDim.x) {
+    const int m = it % NB;
+    const int f = (it / NB) % NF;
+    const int ee = it / (NB * NF);
+    if (e0 + ee >= a.n_elem) continue;
+    const double* h = sm + (f * NB + m) * LD + ee * Q;
+    double uu[Q], F[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) uu[k] = h[k];
+    const double df = euler_flux_normal<D>(f >> 1, uu, a.gamma, F);
+    double* t = a.Tr + (((size_t)(e0 + ee) * NF + f) * NFIELD) * NB + m;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      t[k * NB] = uu[k];
+      t[(Q + k) * NB] = F[k];
+    }
+    t[2 * Q * NB] = df;
+  }
+}
+
+// Local Lax-Friedrichs flux at every face point (AmrDG_NumericalFlux.tpp:4-41).
+// Face f separates left element face_left[f] (its high face in d) and right
+// element face_right[f] (its low face).
+struct FaceArgs {
+  const double* Tr;
+  const int* face_left;
+  const int* face_right;
+  int face_off[4];  // faces of direction d: [face_off[d], face_off[d+1])
+  double* Fnum;
+};
+
+template <class O>
+__global__ void k_numflux(FaceArgs a) {
+  constexpr int D = O::D, Q = O::Q, NB = O::NQ_BD, NF = 2 * D, NFIELD = 2 * Q + 1;
+  const int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nface = a.face_off[D];
+  if (it >= nface * NB) return;
+  const int m = (int)(it % NB);
+  const int f = (int)(it / NB);
+  int d = 0;
+#pragma unroll
+  for (int k = 1; k < D; ++k)
+    if (f >= a.face_off[k]) d = k;
+  const int L = a.face_left[f], R = a.face_right[f];
+  const double* tl = a.Tr + (((size_t)L * NF + 2 * d + 1) * NFIELD) * NB + m;
+  const double* tr = a.Tr + (((size_t)R * NF + 2 * d + 0) * NFIELD) * NB + m;
+  const double C = fmax(fabs(tl[2 * Q * NB]), fabs(tr[2 * Q * NB]));
+  double* out = a.Fnum + (size_t)f * Q * NB + m;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const double uL = tl[q * NB], uR = tr[q * NB];
+    const double fL = tl[(Q + q) * NB], fR = tr[(Q + q) * NB];
+    out[q * NB] = 0.5 * fma(-C, uR - uL, fL + fR);
+  }
+}
+
+// Corrector update of the valid elements (AmrDG.tpp:711-738):
+// U_w = (Rvol - sum_d (Dt/dx_d) (Mkbdp[d] Fnum_hi - Mkbdm[d] Fnum_lo)) / M.
+struct CorrectorArgs {
+  double* Uw;
+  const double* Rvol;
+  const double* Fnum;
+  const int* elem_face;  // [elem][2D]: face index of (d, side)
+  int n_valid;
+  const int8_t* elem_level;
+  LevelGeom geom;
+  const double* dt;
+};
+
+template <class O>
+__global__ void k_corrector(CorrectorArgs a) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NB = O::NQ_BD, NF = 2 * D;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)a.n_valid * Q) return;
+  const int e = (int)(t / Q);
+  const int q = (int)(t % Q);
+  const int lev = a.elem_level ? a.elem_level[e] : 0;
+  const double dt = *a.dt;
+  double R[NP_S];
+  const double* rv = a.Rvol + ((size_t)e * Q + q) * NP_S;
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) R[n] = rv[n];
+  double bp[NP_S], bm[NP_S];
+  const int* ef = a.elem_face + (size_t)e * NF;
+#define ADG_BD(DD)                                                                      \
+  {                                                                                     \
+    const double cd = dt / a.geom.dx[lev][DD];                                          \
+    const double* flo = a.Fnum + ((size_t)ef[2 * DD + 0] * Q + q) * NB;                 \
+    const double* fhi = a.Fnum + ((size_t)ef[2 * DD + 1] * Q + q) * NB;                 \
+    O::template bd_term<DD, 1>(RegIn{fhi}, RegOut{bp});                                 \
+    O::template bd_term<DD, 0>(RegIn{flo}, RegOut{bm});                                 \
+    _Pragma("unroll") for (int n = 0; n < NP_S; ++n) R[n] = fma(-cd, bp[n] - bm[n], R[n]); \
+  }
+  ADG_BD(0)
+  ADG_BD(1)
+  if constexpr (D == 3) ADG_BD(2)
+#undef ADG_BD
+  double* dst = a.Uw + ((size_t)e * Q + q) * NP_S;
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) dst[n] = R[n] * O::minv(n);
+}
+
+// Time step (AmrDG.h:1253-1357): dt_cell = CFL * dx_avg / lambda(U at spatial
+// quadrature point 0); block minimum then a global atomic minimum on the
+// IEEE bit pattern (positive doubles order like their bits).
+struct DtArgs {
+  const double* Uw;
+  int n_valid;
+  const int8_t* elem_level;
+  double dx_avg[kMaxLevels];
+  double gamma;
+  unsigned long long* min_bits;
+  unsigned int* status;
+};
+
+template <class O>
+__global__ void k_dt_reduce(DtArgs a) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  double dtc = 1.0e300;
+  unsigned int st = 0;
+  if (e < a.n_valid) {
+    const int lev = a.elem_level ? a.elem_level[e] : 0;
+    double u[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      double v;
+      O::u_pt0(RegIn{a.Uw + ((size_t)e * Q + q) * NP_S}, RegOut{&v});
+      u[q] = v;
+    }
+    const double lam = euler_cfl_lambda<D>(u, a.gamma);
+    dtc = O::CFL * (a.dx_avg[lev] / lam);
+    if (!(u[0] > 0.0)) st |= kStatusNonPositiveDensity;
+    if (!(dtc == dtc) || !(lam == lam)) {
+      st |= kStatusNaN;
+      dtc = 1.0e300;
+    }
+  }
+  // warp then block minimum
+  for (int o = 16; o > 0; o >>= 1) dtc = fmin(dtc, __shfl_xor_sync(0xffffffffu, dtc, o));
+  __shared__ double wmin[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) wmin[wid] = dtc;
+  __syncthreads();
+  if (wid == 0) {
+    double v = (lane < (int)(blockDim.x + 31) / 32) ? wmin[lane] : 1.0e300;
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) atomicMin(a.min_bits, (unsigned long long)__double_as_longlong(v));
+  }
+  if (st) atomicOr(a.status, st);
+}
+
+// L2 projection of the initial condition at the spatial GL points
+// (AmrDG.h:782-836); one thread per element.
+struct ICArgs {
+  double* Uw;
+  const int* elem_cell;  // [elem][3] cell index within its level
+  const int8_t* elem_level;
+  int n_elem;
+  LevelGeom geom;
+  double prob_lo[3];
+  int n_cell0[3];  // level-0 cells (noise hash index)
+  double gamma;
+  ICParams icp;
+};
+
+template <class O>
+__global__ void k_init_ic(ICArgs a) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NS = O::NQ_S, N = O::N;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.n_elem) return;
+  const int lev = a.elem_level ? a.elem_level[e] : 0;
+  int ijk[3] = {a.elem_cell[3 * e], a.elem_cell[3 * e + 1], a.elem_cell[3 * e + 2]};
+  // level-0 linear index of the covering level-0 cell, periodically wrapped
+  uint64_t lin = 0, mul = 1;
+  for (int d = 0; d < D; ++d) {
+    int w = ijk[d] >> lev;
+    w = ((w % a.n_cell0[d]) + a.n_cell0[d]) % a.n_cell0[d];
+    lin += (uint64_t)w * mul;
+    mul *= (uint64_t)a.n_cell0[d];
+  }
+  double vals[Q][NS];
+  for (int m = 0; m < NS; ++m) {
+    double x[3] = {0, 0, 0};
+    int rem = m;
+    int idx[3] = {0, 0, 0};
+    for (int d = D - 1; d >= 0; --d) {
+      idx[d] = rem % N;
+      rem /= N;
+    }
+    for (int d = 0; d < D; ++d) {
+      const double dx = a.geom.dx[lev][d];
+      const double xc = a.prob_lo[d] + (ijk[d] + 0.5) * dx;
+      x[d] = (dx / 2.0) * O::node(idx[d]) + xc;
+    }
+    double v[5];
+    pde_ic(x, D, a.gamma, a.icp, lin, m, v);
+    for (int q = 0; q < Q; ++q) vals[q][m] = v[q];
+  }
+  for (int q = 0; q < Q; ++q) {
+    double s[NP_S];
+    O::ic_proj(RegIn{vals[q]}, RegOut{s});
+    double* dst = a.Uw + ((size_t)e * Q + q) * NP_S;
+    for (int n = 0; n < NP_S; ++n) dst[n] = s[n] * O::minv(n);
+  }
+}
+
+}  // namespace adg

@@ -1,0 +1,41 @@
+// Per-(D, P) kernel set: the host-side view of one instantiation of the
+// sm_103a kernels (adg_inst.cu compiled once per configuration).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "adg_kernels.cuh"
+
+namespace adg {
+
+struct KernelSet {
+  int D, P, Q, Np_s, Np_st, NQ_ST, NQ_BD, NQ_S;
+  int linear_fp64_per_column;
+  virtual ~KernelSet() = default;
+  virtual std::vector<int> elems_per_block_choices() const = 0;
+  virtual size_t predictor_smem(int E) const = 0;
+  virtual cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s) const = 0;
+  virtual cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s) const = 0;
+  virtual cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t dt_reduce(const DtArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const = 0;
+};
+
+const KernelSet* kernels_D2P1();
+const KernelSet* kernels_D2P2();
+const KernelSet* kernels_D2P3();
+const KernelSet* kernels_D3P1();
+const KernelSet* kernels_D3P2();
+
+inline const KernelSet* kernel_set(int D, int P) {
+  if (D == 2 && P == 1) return kernels_D2P1();
+  if (D == 2 && P == 2) return kernels_D2P2();
+  if (D == 2 && P == 3) return kernels_D2P3();
+  if (D == 3 && P == 1) return kernels_D3P1();
+  if (D == 3 && P == 2) return kernels_D3P2();
+  return nullptr;
+}
+
+}  // namespace adg

@@ -1,0 +1,726 @@
+#!/usr/bin/env python3
+"""Build-time generator of the per-element FP64 operators of the ADER-DG path.
+
+For one (D, P) it computes every element matrix the method needs, exactly
+(rational arithmetic on the double-valued Gauss-Legendre tables, one rounding
+at the end), factorises each operator into a chain of sparse tensor-product
+stages (sum factorisation over the total-degree Legendre basis), checks every
+chain against the dense operator, and emits straight-line CUDA device code in
+which every structural zero is skipped and every coefficient is an exact
+double literal.  One thread of a kernel runs one operator on one
+(element, conserved variable) column, so all 32 lanes of a warp issue the
+same FP64 instruction stream.
+
+Operators (reference definitions, Source/NumericalMethod/AmrDG/...):
+  V            space-time modes -> space-time GL points   (AmrDG_ElementMatrix.tpp:7-19)
+  Vinv         unweighted pseudo-inverse of V              (AmrDG_ElementMatrix.tpp:21-25)
+  Mk_h_w, Mk_pred, Sk_pred[d]                               (AmrDG_ElementMatrix.tpp:32-58)
+  Sk_corr[d], Mkbdm/Mkbdp[d], quadmat                       (AmrDG_ElementMatrix.tpp:63-197)
+  P_cf, P_fc, Minv                                          (AmrDG_Interpolater.tpp:157-231)
+  P_flux_fc_low/high                                        (AmrDG_Interpolater.tpp:85-155)
+Predictor update (AmrDG.tpp:744-827) is folded as
+  H_w <- W U_w - sum_d (Dt/dx_d) A_d F_d,  W = Mk_h_w^-1 Mk_pred,
+  A_d = Mk_h_w^-1 Sk_pred[d] Vinv = C_d V^T,  C_d = Mk_h_w^-1 Sk_pred[d] (V^T V)^-1.
+"""
+import argparse
+import itertools
+import math
+import os
+import sys
+from fractions import Fraction
+
+# ----------------------------------------------------------------------------
+# Gauss-Legendre rule, same arithmetic as the reference (AmrDG.h:151-318)
+# ----------------------------------------------------------------------------
+
+
+def cx_cos(x):
+    result, term = 1.0, 1.0
+    for n in range(1, 31):
+        term *= -x * x / ((2 * n - 1) * (2 * n))
+        result += term
+    return result
+
+
+def cx_legendre(n, x):
+    if n == 0:
+        return 1.0
+    if n == 1:
+        return x
+    p0, p1 = 1.0, x
+    for k in range(2, n + 1):
+        p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k
+        p0, p1 = p1, p2
+    return p1
+
+
+def cx_dlegendre(n, x):
+    if n == 0:
+        return 0.0
+    p0, p1, dp1 = 1.0, x, 1.0
+    for k in range(2, n + 1):
+        p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k
+        dp2 = k * p1 + x * dp1
+        p0, p1, dp1 = p1, p2, dp2
+    return dp1
+
+
+def gl_rule(P):
+    N = P + 1
+    nodes = [0.0] * N
+    idx = 0
+    for i in range(1, N // 2 + 1):
+        theta = 3.14159265358979323846 * (i - 0.25) / (N + 0.5)
+        x = cx_cos(theta)
+        for _ in range(30):
+            dx = cx_legendre(N, x) / cx_dlegendre(N, x)
+            x -= dx
+            if abs(dx) < 1e-16:
+                break
+        nodes[idx] = x
+        nodes[idx + 1] = -x
+        idx += 2
+    if N % 2:
+        nodes[idx] = 0.0
+    weights = []
+    for q in range(N):
+        x = nodes[q]
+        dp = cx_dlegendre(N, x)
+        weights.append(2.0 / ((1.0 - x * x) * dp * dp))
+    return nodes, weights
+
+
+def multi_index(P, Dtot):
+    out = []
+
+    def rec(prefix, left, depth):
+        if depth == Dtot:
+            out.append(tuple(prefix))
+            return
+        for v in range(0, left + 1):
+            rec(prefix + [v], left - v, depth + 1)
+
+    rec([], P, 0)
+    return out
+
+
+# ----------------------------------------------------------------------------
+# Small exact linear algebra on Fractions
+# ----------------------------------------------------------------------------
+
+def fr(x):
+    return Fraction(x) if not isinstance(x, Fraction) else x
+
+
+def mat_mul(A, B):
+    n, k, m = len(A), len(B), len(B[0])
+    out = [[Fraction(0)] * m for _ in range(n)]
+    for i in range(n):
+        Ai = A[i]
+        for t in range(k):
+            a = Ai[t]
+            if a == 0:
+                continue
+            Bt = B[t]
+            row = out[i]
+            for j in range(m):
+                if Bt[j]:
+                    row[j] += a * Bt[j]
+    return out
+
+
+def transpose(A):
+    return [list(r) for r in zip(*A)]
+
+
+def mat_inv(A):
+    n = len(A)
+    M = [list(map(fr, r)) + [Fraction(int(i == j)) for j in range(n)] for i, r in enumerate(A)]
+    for c in range(n):
+        p = next(r for r in range(c, n) if M[r][c] != 0)
+        M[c], M[p] = M[p], M[c]
+        pv = M[c][c]
+        M[c] = [v / pv for v in M[c]]
+        for r in range(n):
+            if r != c and M[r][c] != 0:
+                f = M[r][c]
+                M[r] = [a - f * b for a, b in zip(M[r], M[c])]
+    return [r[n:] for r in M]
+
+
+def to_float(A):
+    return [[float(v) for v in r] for r in A]
+
+
+# ----------------------------------------------------------------------------
+# Element definition
+# ----------------------------------------------------------------------------
+
+
+class Element:
+    def __init__(self, D, P):
+        self.D, self.P, self.N = D, P, P + 1
+        self.nodes, self.weights = gl_rule(P)
+        N = self.N
+        self.val = [[cx_legendre(k, self.nodes[q]) for q in range(N)] for k in range(P + 1)]
+        self.dval = [[cx_dlegendre(k, self.nodes[q]) for q in range(N)] for k in range(P + 1)]
+        self.bd = [[cx_legendre(k, -1.0), cx_legendre(k, 1.0)] for k in range(P + 1)]
+        self.slo = [[cx_legendre(k, 0.5 * self.nodes[q] - 0.5) for q in range(N)] for k in range(P + 1)]
+        self.shi = [[cx_legendre(k, 0.5 * self.nodes[q] + 0.5) for q in range(N)] for k in range(P + 1)]
+        self.mi_s = multi_index(P, D)
+        self.mi_st = multi_index(P, D + 1)
+        self.Np_s, self.Np_st = len(self.mi_s), len(self.mi_st)
+        self.pts_st = list(itertools.product(range(N), repeat=D + 1))  # d=0 slowest
+        self.pts_s = list(itertools.product(range(N), repeat=D))
+        self.pts_bd = list(itertools.product(range(N), repeat=D))  # free dims: spatial != d, then time
+        self._build_matrices()
+
+    # 1D exact integrals of Legendre polynomials on [-1, 1]
+    @staticmethod
+    def int_pp(a, b):
+        return Fraction(2, 2 * a + 1) if a == b else Fraction(0)
+
+    @staticmethod
+    def int_p_dp(a, b):  # int P_a P_b'
+        return Fraction(2) if (b > a and (a + b) % 2 == 1) else Fraction(0)
+
+    def ms(self, j):  # diagonal spatial mass of a (space or space-time) mode, spatial part only
+        m = Fraction(1)
+        for d in range(self.D):
+            m *= Fraction(2, 2 * j[d] + 1)
+        return m
+
+    def _build_matrices(self):
+        D, P = self.D, self.P
+        st, s = self.mi_st, self.mi_s
+        nst, ns = self.Np_st, self.Np_s
+        # V with double entries formed as the reference does (product d = 0..D in order)
+        V = []
+        for pt in self.pts_st:
+            row = []
+            for n in st:
+                phi = 1.0
+                for d in range(D + 1):
+                    phi *= self.val[n[d]][pt[d]]
+                row.append(phi)
+            V.append(row)
+        self.V = V
+        Vf = [[fr(v) for v in r] for r in V]
+        G = mat_mul(transpose(Vf), Vf)
+        Ginv = mat_inv(G)
+        self.Ginv = Ginv
+        Vinv = mat_mul(Ginv, transpose(Vf))
+        # Mk_h_w, Mk_pred, Sk_pred (exact)
+        Mkhw = [[Fraction(0)] * nst for _ in range(nst)]
+        Sk = [[[Fraction(0)] * nst for _ in range(nst)] for _ in range(D)]
+        Mkpred = [[Fraction(0)] * ns for _ in range(nst)]
+        for jj, j in enumerate(st):
+            for ii, i in enumerate(st):
+                if j[:D] == i[:D]:
+                    Mkhw[jj][ii] = self.ms(j) * (1 - self.int_p_dp(i[D], j[D]))
+                if j[D] == i[D]:
+                    tm = Fraction(2, 2 * j[D] + 1)
+                    for d in range(D):
+                        ok = all(j[a] == i[a] for a in range(D) if a != d)
+                        if not ok:
+                            continue
+                        v = Fraction(1)
+                        for a in range(D):
+                            if a != d:
+                                v *= Fraction(2, 2 * j[a] + 1)
+                        v *= self.int_p_dp(j[d], i[d])
+                        Sk[d][jj][ii] = tm * v
+            for ii, i in enumerate(s):
+                if j[:D] == i[:D]:
+                    Mkpred[jj][ii] = (-1) ** j[D] * self.ms(j)
+        Mkhw_inv = mat_inv(Mkhw)
+        self.W = to_float(mat_mul(Mkhw_inv, Mkpred))
+        self.A = []
+        self.C = []
+        for d in range(D):
+            KS = mat_mul(Mkhw_inv, Sk[d])
+            self.A.append(to_float(mat_mul(KS, Vinv)))
+            self.C.append(to_float(mat_mul(KS, Ginv)))
+        self.Mdiag = [float(self.ms(n)) for n in s]
+        self.Minv = [float(1 / self.ms(n)) for n in s]
+
+    # ---- dense reference operators (rows = outputs) for chain verification
+    def dense_vol_eval(self):
+        return self.V
+
+    def dense_sk_corr(self, d):
+        D, N = self.D, self.N
+        out = []
+        for n in self.mi_s:
+            row = []
+            for pt in self.pts_st:
+                w = 1.0
+                for a in range(D + 1):
+                    w *= self.weights[pt[a]]
+                ph = 1.0
+                for a in range(D):
+                    ph *= (self.dval if a == d else self.val)[n[a]][pt[a]]
+                row.append(ph * w)
+            out.append(row)
+        return out
+
+    def bd_point_coords(self, d, pt):
+        """face point pt (free dims: spatial dims != d in order, then time) ->
+        dict dim -> node index"""
+        free = [a for a in range(self.D) if a != d] + [self.D]
+        return {a: pt[i] for i, a in enumerate(free)}
+
+    def dense_face_eval(self, d, side):
+        out = []
+        for pt in self.pts_bd:
+            c = self.bd_point_coords(d, pt)
+            row = []
+            for n in self.mi_st:
+                phi = 1.0
+                for a in range(self.D + 1):
+                    phi *= self.bd[n[a]][side] if a == d else self.val[n[a]][c[a]]
+                row.append(phi)
+            out.append(row)
+        return out
+
+    def dense_bd_term(self, d, side):
+        out = []
+        for n in self.mi_s:
+            row = []
+            for pt in self.pts_bd:
+                c = self.bd_point_coords(d, pt)
+                w = 1.0
+                for a in c:
+                    w *= self.weights[c[a]]
+                phi = 1.0
+                for a in range(self.D):
+                    phi *= self.bd[n[a]][side] if a == d else self.val[n[a]][c[a]]
+                row.append(phi * w)
+            out.append(row)
+        return out
+
+
+# ----------------------------------------------------------------------------
+# Sparse stage chains over tuple index spaces
+# ----------------------------------------------------------------------------
+
+
+class Stage:
+    """out[r] = sum_c coef * in[c]; rows: list of lists of (col, coef)."""
+
+    def __init__(self, n_in, n_out, rows):
+        self.n_in, self.n_out, self.rows = n_in, n_out, rows
+
+    def nnz(self):
+        return sum(len(r) for r in self.rows)
+
+
+def stage_from_map(in_keys, out_keys, fn):
+    """fn(out_key) -> list of (in_key, coef)"""
+    pos = {k: i for i, k in enumerate(in_keys)}
+    rows = []
+    for ok in out_keys:
+        terms = [(pos[ik], c) for ik, c in fn(ok) if ik in pos and c != 0.0]
+        rows.append(terms)
+    return Stage(len(in_keys), len(out_keys), rows)
+
+
+def chain_dense(stages):
+    M = None
+    for st in stages:
+        S = [[0.0] * st.n_in for _ in range(st.n_out)]
+        for r, terms in enumerate(st.rows):
+            for c, v in terms:
+                S[r][c] += v
+        if M is None:
+            M = S
+        else:
+            M = [[sum(S[i][k] * M[k][j] for k in range(len(M))) for j in range(len(M[0]))] for i in range(len(S))]
+    return M
+
+
+def check_chain(stages, dense, name, tol=1e-12):
+    M = chain_dense(stages)
+    scale = max(abs(v) for r in dense for v in r) or 1.0
+    err = max(abs(M[i][j] - dense[i][j]) for i in range(len(dense)) for j in range(len(dense[0])))
+    if err > tol * scale:
+        raise SystemExit(f"chain check failed for {name}: {err / scale}")
+
+
+def prefixes(P, length):
+    return [t for t in itertools.product(range(P + 1), repeat=length) if sum(t) <= P]
+
+
+class Chains:
+    def __init__(self, el):
+        self.el = el
+
+    # keys are tuples with entries ('m', a) mode or ('q', k) point index
+    def eval_chain(self, order, start_keys, dim_tables, n_dims):
+        """Evaluate a modal expansion at tensor points by contracting
+        positions in `order`; dim_tables[pos] = table T[a][k] (k may be a
+        single pseudo point 0 for a fixed face dimension)."""
+        stages = []
+        keys = start_keys
+        for pos in order:
+            T = dim_tables[pos]
+            npts = len(T[0])
+            new_keys = sorted({tuple(('q', k) if i == pos else e for i, e in enumerate(key))
+                               for key in keys for k in range(npts)})
+
+            def fn(ok, pos=pos, T=T):
+                k = ok[pos][1]
+                terms = []
+                for a in range(self.el.P + 1):
+                    ik = tuple(('m', a) if i == pos else e for i, e in enumerate(ok))
+                    terms.append((ik, T[a][k]))
+                return terms
+
+            stages.append(stage_from_map(keys, new_keys, fn))
+            keys = new_keys
+        return stages, keys
+
+    def project_chain(self, order, start_keys, dim_tables, mode_ok):
+        """Transposed contraction: point indices -> mode indices.  mode_ok(key)
+        filters partially contracted keys (total degree <= P)."""
+        stages = []
+        keys = start_keys
+        for pos in order:
+            T = dim_tables[pos]  # T[a][k]
+            new_keys = sorted({tuple(('m', a) if i == pos else e for i, e in enumerate(key))
+                               for key in keys for a in range(len(T))})
+            new_keys = [k for k in new_keys if mode_ok(k)]
+
+            def fn(ok, pos=pos, T=T):
+                a = ok[pos][1]
+                return [(tuple(('q', k) if i == pos else e for i, e in enumerate(ok)), T[a][k])
+                        for k in range(len(T[0]))]
+
+            stages.append(stage_from_map(keys, new_keys, fn))
+            keys = new_keys
+        return stages, keys
+
+
+def degree_ok(P):
+    def ok(key):
+        return sum(e[1] for e in key if e[0] == 'm') <= P
+    return ok
+
+
+def build_ops(el):
+    D, P, N = el.D, el.P, el.N
+    ch = Chains(el)
+    ops = {}
+    st_keys = [tuple(('m', a) for a in n) for n in el.mi_st]
+    pt_keys_st = [tuple(('q', k) for k in pt) for pt in el.pts_st]
+    # ---- vol_eval: st modes -> st points; contract time first, then D-1..0
+    order = list(range(D, -1, -1))
+    stages, keys = ch.eval_chain(order, st_keys, {p: el.val for p in range(D + 1)}, D + 1)
+    stages.append(stage_from_map(keys, pt_keys_st, lambda ok: [(ok, 1.0)]))
+    check_chain(stages, el.dense_vol_eval(), "vol_eval")
+    ops["vol_eval"] = (stages, el.Np_st, len(pt_keys_st))
+
+    # ---- vol_eval_init: U_w placed in st modes 0..Np_s-1 (the reference's
+    # predictor initial guess, AmrDG.tpp:520-533).  Those are exactly the
+    # st modes with a_0 == 0, so the expansion does not depend on x_0 and is
+    # evaluated on the (x_1.., t) grid only.
+    init_modes = el.mi_st[:el.Np_s]
+    assert all(n[0] == 0 for n in init_modes)
+    init_keys = [tuple(('m', a) for a in n[1:]) for n in init_modes]
+    order = list(range(D - 1, -1, -1))  # positions in the reduced tuple (x_1.., t)
+    tabs = {p: el.val for p in range(D)}
+    stages, keys = ch.eval_chain(order, init_keys, tabs, D)
+    grid_keys = [tuple(('q', k) for k in pt) for pt in itertools.product(range(N), repeat=D)]
+    stages.append(stage_from_map(keys, grid_keys, lambda ok: [(ok, 1.0)]))
+    dense = [[el.V[el.pts_st.index((0,) + pt)][i] for i in range(el.Np_s)]
+             for pt in itertools.product(range(N), repeat=D)]
+    check_chain(stages, dense, "vol_eval_init")
+    ops["vol_eval_init"] = (stages, el.Np_s, len(grid_keys))
+
+    # ---- proj[d]: F at st points -> st modes, A_d = C_d V^T
+    order = list(range(0, D + 1))
+    vt_stages, keys = ch.project_chain(order, pt_keys_st, {p: el.val for p in range(D + 1)}, degree_ok(P))
+    mode_pos = {tuple(('m', a) for a in n): i for i, n in enumerate(el.mi_st)}
+    perm = stage_from_map(keys, [tuple(('m', a) for a in n) for n in el.mi_st], lambda ok: [(ok, 1.0)])
+    for d in range(D):
+        Cd = el.C[d]
+        cst = Stage(el.Np_st, el.Np_st, [[(c, Cd[r][c]) for c in range(el.Np_st) if Cd[r][c] != 0.0]
+                                         for r in range(el.Np_st)])
+        stages = vt_stages + [perm, cst]
+        check_chain(stages, el.A[d], f"proj{d}", tol=1e-11)
+        dense_A = Stage(len(pt_keys_st), el.Np_st,
+                        [[(c, el.A[d][r][c]) for c in range(len(pt_keys_st)) if el.A[d][r][c] != 0.0]
+                         for r in range(el.Np_st)])
+        f_nnz = sum(s.nnz() for s in stages)
+        ops[f"proj{d}"] = (stages if f_nnz < dense_A.nnz() else [dense_A], len(pt_keys_st), el.Np_st)
+
+    # ---- proj_init[d]: F given on the (x_1.., t) grid (x_0-independent)
+    Ssum = [sum(el.val[a][k] for k in range(N)) for a in range(P + 1)]
+    # stage 1: replicate + contract x_0: g[(a0, q1.., qt)] = Ssum[a0] * F[(q1.., qt)]
+    g1_keys = sorted({(('m', a),) + k for a in range(P + 1) for k in grid_keys if Ssum[a] != 0.0})
+    st1 = stage_from_map(grid_keys, g1_keys, lambda ok: [(ok[1:], Ssum[ok[0][1]])])
+    rest, keys = ch.project_chain(list(range(1, D + 1)), g1_keys, {p: el.val for p in range(D + 1)}, degree_ok(P))
+    mode_keys_all = [tuple(('m', a) for a in n) for n in el.mi_st]
+    perm_i = stage_from_map(keys, mode_keys_all, lambda ok: [(ok, 1.0)])
+    for d in range(D):
+        Cd = el.C[d]
+        cst = Stage(el.Np_st, el.Np_st, [[(c, Cd[r][c]) for c in range(el.Np_st) if Cd[r][c] != 0.0]
+                                         for r in range(el.Np_st)])
+        stages = [st1] + rest + [perm_i, cst]
+        dense = [[sum(el.A[d][r][el.pts_st.index((i,) + pt)] for i in range(N))
+                  for pt in itertools.product(range(N), repeat=D)] for r in range(el.Np_st)]
+        check_chain(stages, dense, f"proj_init{d}", tol=1e-11)
+        ops[f"proj_init{d}"] = (stages, len(grid_keys), el.Np_st)
+
+    # ---- W U: (Np_s) -> (Np_st)
+    ops["wu"] = ([Stage(el.Np_s, el.Np_st, [[(c, el.W[r][c]) for c in range(el.Np_s) if el.W[r][c] != 0.0]
+                                           for r in range(el.Np_st)])], el.Np_s, el.Np_st)
+
+    # ---- vol_term[d]: Sk_corr[d] (st points -> s modes)
+    for d in range(D):
+        tabs = {}
+        for p in range(D):
+            base = el.dval if p == d else el.val
+            tabs[p] = [[base[a][k] * el.weights[k] for k in range(N)] for a in range(P + 1)]
+        tabs[D] = [[el.weights[k] for k in range(N)]]  # time: weighted sum to a single "mode"
+        order = [D] + list(range(0, D))
+        stages, keys = ch.project_chain(order, pt_keys_st, tabs, degree_ok(P))
+        s_keys = [tuple(('m', a) for a in n) + (('m', 0),) for n in el.mi_s]
+        stages.append(stage_from_map(keys, s_keys, lambda ok: [(ok, 1.0)]))
+        check_chain(stages, el.dense_sk_corr(d), f"vol_term{d}")
+        ops[f"vol_term{d}"] = (stages, len(pt_keys_st), el.Np_s)
+
+    # ---- face_eval[d][side]: st modes -> face points (free spatial dims, time)
+    bd_pt_keys = [tuple(('q', k) for k in pt) for pt in el.pts_bd]
+    for d in range(D):
+        for side in range(2):
+            tabs = {p: el.val for p in range(D + 1)}
+            tabs[d] = [[el.bd[a][side]] for a in range(P + 1)]
+            order = [d] + [p for p in range(D, -1, -1) if p != d]
+            stages, keys = ch.eval_chain(order, st_keys, tabs, D + 1)
+            # drop the singleton point of dim d; order free dims as (spatial != d, time)
+            free = [a for a in range(D) if a != d] + [D]
+
+            def fn(ok, free=free):
+                full = [None] * (D + 1)
+                full[d] = ('q', 0)
+                for i, a in enumerate(free):
+                    full[a] = ok[i]
+                return [(tuple(full), 1.0)]
+
+            stages.append(stage_from_map(keys, bd_pt_keys, fn))
+            check_chain(stages, el.dense_face_eval(d, side), f"face_eval{d}{side}")
+            ops[f"face_eval{d}{side}"] = (stages, el.Np_st, len(bd_pt_keys))
+
+    # ---- bd_term[d][side]: Mkbd{m,p}[d] (face points -> s modes)
+    for d in range(D):
+        for side in range(2):
+            free = [a for a in range(D) if a != d] + [D]
+            # contract time (weights), then free spatial dims with val*w, then expand dim d with bd
+            nf = len(free)
+            tabs = {}
+            for i, a in enumerate(free):
+                if a == D:
+                    tabs[i] = [[el.weights[k] for k in range(N)]]
+                else:
+                    tabs[i] = [[el.val[m][k] * el.weights[k] for k in range(N)] for m in range(P + 1)]
+            order = [nf - 1] + list(range(0, nf - 1))
+            stages, keys = ch.project_chain(order, bd_pt_keys, tabs, degree_ok(P))
+            s_keys = [tuple(('m', a) for a in n) for n in el.mi_s]
+
+            def fn(ok, free=free, side=side, d=d):
+                sub = tuple(ok[a] for a in free if a != D) + (('m', 0),)
+                return [(sub, el.bd[ok[d][1]][side])]
+
+            stages.append(stage_from_map(keys, s_keys, fn))
+            check_chain(stages, el.dense_bd_term(d, side), f"bd_term{d}{side}")
+            ops[f"bd_term{d}{side}"] = (stages, len(bd_pt_keys), el.Np_s)
+
+    # ---- spatial modes at spatial GL point 0 (set_Dt, AmrDG.h:1275,1306)
+    row = []
+    for n in el.mi_s:
+        phi = 1.0
+        for d in range(D):
+            phi *= el.val[n[d]][0]
+        row.append(phi)
+    ops["u_pt0"] = ([Stage(el.Np_s, 1, [[(c, row[c]) for c in range(el.Np_s) if row[c] != 0.0]])], el.Np_s, 1)
+    return ops
+
+
+# ----------------------------------------------------------------------------
+# CUDA emission
+# ----------------------------------------------------------------------------
+
+
+def lit(v):
+    r = repr(float(v))
+    if "e" not in r and "." not in r and "inf" not in r and "nan" not in r:
+        r += ".0"
+    return r
+
+
+def fp64_ops(stage):
+    """FP64 instructions one stage issues per column (a term with coefficient
+    +-1 at the head of a row is a move, every further term one DADD/DFMA)."""
+    n = 0
+    for terms in stage.rows:
+        if not terms:
+            continue
+        n += len(terms) - 1
+        if terms[0][1] not in (1.0, -1.0):
+            n += 1
+    return n
+
+
+def emit_stage(lines, st, src, dst, indent="    "):
+    for r, terms in enumerate(st.rows):
+        d = dst(r)
+        if not terms:
+            lines.append(f"{indent}{d} = 0.0;")
+            continue
+        expr = None
+        for c, v in terms:
+            x = src(c)
+            if expr is None:
+                if v == 1.0:
+                    expr = f"{x}"
+                elif v == -1.0:
+                    expr = f"(-{x})"
+                else:
+                    expr = f"{lit(v)} * {x}"
+            else:
+                if v == 1.0:
+                    expr = f"({expr} + {x})"
+                elif v == -1.0:
+                    expr = f"({expr} - {x})"
+                else:
+                    expr = f"fma({lit(v)}, {x}, {expr})"
+        lines.append(f"{indent}{d} = {expr};")
+
+
+def emit_op(name, op):
+    stages, n_in, n_out = op
+    nops = sum(fp64_ops(s) for s in stages)
+    lines = [f"  // {name}: {n_in} -> {n_out}, {nops} FP64 instructions per column",
+             f"  template <class In, class Out>",
+             f"  static __device__ __forceinline__ void {name}(const In& in, Out out) {{"]
+    for si, st in enumerate(stages):
+        last = si == len(stages) - 1
+        if not last:
+            lines.append(f"    double t{si}[{st.n_out}];")
+        src = (lambda c: f"in({c})") if si == 0 else (lambda c, p=si - 1: f"t{p}[{c}]")
+        dst = (lambda r: f"out({r})") if last else (lambda r, s=si: f"t{s}[{r}]")
+        emit_stage(lines, st, src, dst)
+    lines.append("  }")
+    return "\n".join(lines), nops
+
+
+def add_ic_proj(el, ops):
+    """quadmat (AmrDG_ElementMatrix.tpp:154-168): spatial points -> spatial modes."""
+    D, P, N = el.D, el.P, el.N
+    ch = Chains(el)
+    pt_keys = [tuple(('q', k) for k in pt) for pt in el.pts_s]
+    tabs = {p: [[el.val[a][k] * el.weights[k] for k in range(N)] for a in range(P + 1)] for p in range(D)}
+    stages, keys = ch.project_chain(list(range(D)), pt_keys, tabs, degree_ok(P))
+    s_keys = [tuple(('m', a) for a in n) for n in el.mi_s]
+    stages.append(stage_from_map(keys, s_keys, lambda ok: [(ok, 1.0)]))
+    dense = []
+    for n in el.mi_s:
+        row = []
+        for pt in el.pts_s:
+            w = 1.0
+            for d in range(D):
+                w *= el.weights[pt[d]]
+            phi = 1.0
+            for d in range(D):
+                phi *= el.val[n[d]][pt[d]]
+            row.append(phi * w)
+        dense.append(row)
+    check_chain(stages, dense, "ic_proj")
+    ops["ic_proj"] = (stages, len(pt_keys), el.Np_s)
+
+
+def generate(D, P, out_path):
+    el = Element(D, P)
+    ops = build_ops(el)
+    add_ic_proj(el, ops)
+    N = P + 1
+    qst = N ** (D + 1)
+    qbd = N ** D
+    ns = f"gen_D{D}P{P}"
+    hdr = [
+        "// Generated by gen_element.py -- do not edit.",
+        f"// Element operators for D={D}, P={P} (ADER-DG, modal Legendre, FP64).",
+        "#pragma once",
+        f"namespace adg {{ namespace {ns} {{",
+        "__device__ __constant__ const double MDIAG_[] = {" + ", ".join(lit(v) for v in el.Mdiag) + "};",
+        "__device__ __constant__ const double MINV_[] = {" + ", ".join(lit(v) for v in el.Minv) + "};",
+        "__device__ __constant__ const double NODES_[] = {" + ", ".join(lit(v) for v in el.nodes) + "};",
+        "struct Ops {",
+        f"  static constexpr int D = {D};",
+        f"  static constexpr int P = {P};",
+        f"  static constexpr int N = {N};",
+        f"  static constexpr int Q = {D + 2};",
+        f"  static constexpr int NP_S = {el.Np_s};",
+        f"  static constexpr int NP_ST = {el.Np_st};",
+        f"  static constexpr int NQ_ST = {qst};",
+        f"  static constexpr int NQ_BD = {qbd};",
+        f"  static constexpr int NQ_S = {N ** D};",
+        f"  static constexpr int NQ_INIT = {N ** D};",
+        f"  static constexpr double CFL = {lit((1.0 / (2.0 * P + 1.0)) * (1.0 / D))};",
+        "  static __device__ __forceinline__ double mdiag(int n) { return MDIAG_[n]; }",
+        "  static __device__ __forceinline__ double minv(int n) { return MINV_[n]; }",
+        "  static __device__ __forceinline__ double node(int k) { return NODES_[k]; }",
+    ]
+    counts = {}
+    for name, op in ops.items():
+        code, nops = emit_op(name, op)
+        hdr.append(code)
+        counts[name] = nops
+    # compile-time dispatchers
+    def disp(fname, names, params):
+        lines = [f"  template <{', '.join('int ' + p for p in params)}, class In, class Out>",
+                 f"  static __device__ __forceinline__ void {fname}(const In& in, Out out) {{"]
+        first = True
+        for key, nm in names:
+            cond = " && ".join(f"{p} == {v}" for p, v in zip(params, key))
+            lines.append(f"    {'if' if first else 'else if'} constexpr ({cond}) {nm}(in, out);")
+            first = False
+        lines.append("  }")
+        return "\n".join(lines)
+    hdr.append(disp("proj", [((d,), f"proj{d}") for d in range(D)], ["d"]))
+    hdr.append(disp("proj_init", [((d,), f"proj_init{d}") for d in range(D)], ["d"]))
+    hdr.append(disp("vol_term", [((d,), f"vol_term{d}") for d in range(D)], ["d"]))
+    hdr.append(disp("face_eval", [((d, s), f"face_eval{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
+    hdr.append(disp("bd_term", [((d, s), f"bd_term{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
+    # FP64 instruction counts of the linear stages per column and step
+    sweeps = P
+    per_col = (counts["wu"] + counts["vol_eval_init"] + sum(counts[f"proj_init{d}"] for d in range(D)) + 2 * D * el.Np_st
+               + (sweeps - 1) * (counts["vol_eval"] + sum(counts[f"proj{d}"] for d in range(D)) + 2 * D * el.Np_st)
+               + counts["vol_eval"] + sum(counts[f"vol_term{d}"] for d in range(D))
+               + sum(counts[f"face_eval{d}{s}"] for d in range(D) for s in range(2))
+               + sum(counts[f"bd_term{d}{s}"] for d in range(D) for s in range(2)) + 4 * el.Np_s)
+    hdr.append(f"  static constexpr int LINEAR_FP64_PER_COLUMN = {per_col};")
+    hdr.append("};")
+    hdr.append("}}  // namespace")
+    hdr.append("")
+    with open(out_path, "w") as f:
+        f.write("\n".join(hdr))
+    return counts
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out-dir", required=True)
+    ap.add_argument("--configs", default="2:1,2:2,2:3,3:1,3:2")
+    args = ap.parse_args()
+    os.makedirs(args.out_dir, exist_ok=True)
+    for cfg in args.configs.split(","):
+        D, P = map(int, cfg.split(":"))
+        path = os.path.join(args.out_dir, f"elem_D{D}P{P}.cuh")
+        counts = generate(D, P, path)
+        print(f"D={D} P={P}: " + ", ".join(f"{k}={v}" for k, v in counts.items()), file=sys.stderr)
+
+
+if __name__ == "__main__":
+    main()

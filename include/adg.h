@@ -1,0 +1,152 @@
+/*
+ * adg.h -- C ABI of the GB300 (sm_103a) ADER-DG element path.
+ *
+ * Drop-in boundary for the hot path of AmrDG<P>::ADER
+ * (reference: Source/NumericalMethod/AmrDG/AmrDG.h:1071-1165) and the
+ * L2ProjInterp AMR transfer operators (AmrDG_Interpolater.tpp:7-448).
+ * Plain C types only: sizes, host pointers and device pointers.  Every entry
+ * point returns an int status (ADG_OK = 0); adg_last_error() gives the text.
+ *
+ * Data layout (HBM): one packed array per AMR level, element-major
+ * U_w[cell][q][n] (q = conserved variable, n = spatial Legendre mode, the
+ * reference's MultiIndex order AmrDG.h:62-122), cells ordered x-fastest over
+ * the level's valid cells.  The context owns all device memory of the
+ * hierarchy; adg_get_state/adg_set_state copy a level in or out (host or
+ * device pointers, see ADG_MEM_*).
+ */
+#ifndef ADG_H
+#define ADG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ADG_OK 0
+#define ADG_ERR_ARG 1          /* invalid argument / unsupported (D, P) */
+#define ADG_ERR_CUDA 2         /* CUDA runtime error */
+#define ADG_ERR_LAYOUT 3       /* invalid box layout (nesting, overlap) */
+#define ADG_ERR_NUMERIC 4      /* device status: NaN or non-positive density */
+#define ADG_ERR_STATE 5        /* call out of order (e.g. step before init) */
+
+#define ADG_MEM_HOST 0
+#define ADG_MEM_DEVICE 1
+
+/* Initial conditions (Source/Model/CompressibleEuler/Compressible_Euler.h:120-368). */
+#define ADG_IC_VORTEX 0     /* isentropic vortex, free stream (u_inf, v_inf) */
+#define ADG_IC_KH_NOISE 1   /* KH: sin(4 pi x) + seeded noise of amplitude noise_amp */
+#define ADG_IC_KH_REF 2     /* reference KH (Gaussian-localised v) */
+#define ADG_IC_BLAST3D 3    /* spherical blast in [0,1]^3 */
+#define ADG_IC_CONST 4      /* uniform free stream */
+
+typedef struct adg_config {
+  int D, P;                 /* spatial dimension 2|3, polynomial degree 1..3 */
+  double gamma;             /* adiabatic index (Compressible_Euler.cpp:42-47) */
+  double c_dt;              /* CFL safety factor (Solver::c_dt) */
+  int n_cell[3];            /* level-0 cells per dimension */
+  double prob_lo[3], prob_hi[3];
+  int periodic[3];          /* 1 periodic, 0 outflow (zero-gradient mode copy) */
+  int ic;                   /* ADG_IC_* */
+  double u_inf, v_inf, beta, xc, yc;
+  uint64_t seed;            /* noise seed of ADG_IC_KH_NOISE */
+  double noise_amp;
+  int max_grid;             /* max cells per box edge */
+  /* AMR (max_level = 0: single level) */
+  int max_level;
+  int blocking_factor;
+  int dtn_regrid;           /* regrid every n steps (Mesh::dtn_regrid) */
+  int tag_kind;             /* 0 normalised density gradient, 1 pressure jump */
+  double tag_threshold;
+  double grid_eff;
+  int n_error_buf;
+  int reflux_box_quirk;     /* 1: reference's per-box reflux mask (AmrDG_Interpolater.tpp:41-56) */
+  int picard_sweeps;        /* predictor sweeps; <= 0 means P (AmrDG.h:1103-1119) */
+  int elems_per_block;      /* 0: autotuned default */
+} adg_config;
+
+typedef struct adg_ctx adg_ctx;
+
+/* Context: builds the element operators for (D, P) and owns device state.
+ * Replaces AmrDG<P>::init (Source/NumericalMethod/AmrDG/AmrDG.tpp:82-246). */
+int adg_ctx_create(const adg_config* cfg, adg_ctx** out);
+int adg_ctx_destroy(adg_ctx* ctx);
+const char* adg_last_error(const adg_ctx* ctx);
+
+/* Stream all work is issued on (default: the context's own stream). */
+int adg_set_stream(adg_ctx* ctx, void* cuda_stream);
+
+/* Build the level-0 layout and project the initial condition on the device.
+ * Replaces Solver::init + AmrDG::set_initial_condition
+ * (Source/Core/Solver.h:502-597, Source/NumericalMethod/AmrDG/AmrDG.h:782-836),
+ * then computes the first Dt (AmrDG.h:1253-1357). */
+int adg_init(adg_ctx* ctx);
+
+/* Level state in/out: n_cells * Q * Np_s doubles, element-major, cells in
+ * x-fastest order over the level's valid cells. */
+int adg_num_levels(const adg_ctx* ctx, int* nlev);
+int adg_level_cells(const adg_ctx* ctx, int lev, int64_t* ncells);
+int adg_get_state(adg_ctx* ctx, int lev, double* dst, int mem);
+int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem);
+
+/* Time step size: current Dt (device-computed), set an explicit Dt, or
+ * recompute it from the state (set_Dt, AmrDG.h:1253-1357). */
+int adg_get_dt(adg_ctx* ctx, double* dt);
+int adg_set_dt(adg_ctx* ctx, double dt);
+int adg_compute_dt(adg_ctx* ctx, double* dt);
+int adg_get_time(adg_ctx* ctx, double* t);
+
+/* One ADER predictor-corrector step of every level with the current Dt
+ * (AmrDG<P>::ADER, AmrDG.h:1071-1165), without the Dt update. */
+int adg_ader(adg_ctx* ctx);
+
+/* One full step of the evolve loop body (AmrDG.h:935-1029): regrid when due,
+ * ADER, average down, ghost fill, t += Dt, new Dt. */
+int adg_step(adg_ctx* ctx);
+
+/* n steps; use_graph != 0 replays a captured CUDA graph of the step
+ * (re-captured when the layout changes). */
+int adg_advance(adg_ctx* ctx, int nsteps, int use_graph);
+
+/* Per-stage entry points (parity testing). */
+/* Predictor only for level lev: writes H_w (Q * Np_st per cell, element-major)
+ * for the valid cells to dst (device pointer). (AmrDG.tpp:495-537, 744-827) */
+int adg_predictor(adg_ctx* ctx, int lev, double* dst_dev);
+
+/* Device status word: bit 0 NaN, bit 1 non-positive density, bit 2 pressure
+ * floored (Compressible_Euler.h:586); cleared on read. */
+int adg_status(adg_ctx* ctx, uint32_t* status);
+
+/* Kernel launches issued by this context since creation (all kernels). */
+int adg_launch_count(const adg_ctx* ctx, int64_t* n);
+
+/* Select the CUDA device for contexts created afterwards by this thread. */
+int adg_set_device(int device);
+
+/* n steps like adg_advance, bracketed by CUDA events recorded on the
+ * context's stream; *ms receives the device time of the n steps. */
+int adg_advance_timed(adg_ctx* ctx, int nsteps, int use_graph, double* ms);
+
+/* n steps with CUDA events around every kernel on the context's stream;
+ * ms[k] receives the average duration of kernel kind k per step:
+ * 0 predictor (+ corrector volume term and face traces), 1 numerical flux,
+ * 2 corrector update, 3 time-step reduction, 4 AMR synchronisation. */
+int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds);
+
+/* Page-locked host buffers for host<->device state copies. */
+int adg_host_alloc(size_t bytes, void** ptr);
+int adg_host_free(void* ptr);
+
+/* Measured FP64 multiply-add throughput of this GPU (DFMA chains), GFLOP/s. */
+int adg_fp64_peak_probe(double* gflops);
+
+/* Algorithmic FP64 flops per element-step (the method's dense matvec count)
+ * and the FP64 operations the generated kernels actually issue per element. */
+int adg_flops_per_element(int D, int P, double* algorithmic, double* issued);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ADG_H */
