@@ -68,7 +68,7 @@ def build(verbose=False, extra_flags=()):
             jobs.append([nvcc, *NVCC_FLAGS, *extra_flags, "-c", os.path.join(CSRC, "adg_inst.cu"), "-o", obj,
                          f"-DADG_D={d}", f"-DADG_HDR=\"elem_D{d}P{p}.cuh\"", f"-DADG_NS=gen_D{d}P{p}",
                          f"-DADG_FACTORY=kernels_D{d}P{p}"])
-    for src in ("adg_ctx.cu", "adg_amr.cu"):
+    for src in ("adg_ctx.cu", "adg_amr.cu", "adg_noalloc.cu"):
         path = os.path.join(CSRC, src)
         if not os.path.exists(path):
             continue

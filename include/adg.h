@@ -30,6 +30,7 @@ extern "C" {
 #define ADG_ERR_LAYOUT 3       /* invalid box layout (nesting, overlap) */
 #define ADG_ERR_NUMERIC 4      /* device status: NaN or non-positive density */
 #define ADG_ERR_STATE 5        /* call out of order (e.g. step before init) */
+#define ADG_ERR_NOALLOC_CAPACITY 6 /* problem larger than the fixed scratch of adg_ader_step_noalloc */
 
 #define ADG_MEM_HOST 0
 #define ADG_MEM_DEVICE 1
@@ -140,6 +141,24 @@ int adg_host_free(void* ptr);
 
 /* Measured FP64 multiply-add throughput of this GPU (DFMA chains), GFLOP/s. */
 int adg_fp64_peak_probe(double* gflops);
+
+/* One ADER predictor-corrector step (AmrDG::ADER physics, all sweeps) of a
+ * single-level grid, periodic in every direction, that allocates nothing.
+ * No counterpart in the reference: it exists for callers that cannot
+ * allocate GPU memory when they need a step (code running inside another
+ * framework's memory arena or pool, or a loop that must not call the
+ * allocator after start-up).  The caller passes the state U_w (device
+ * pointer, element-major [cell][q][n], cells x-fastest; updated in place)
+ * and the step size; all intermediates live in one fixed device array of
+ * ADG_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * the process exits.  Problems whose intermediates do not fit return
+ * ADG_ERR_NOALLOC_CAPACITY (about 11,000 elements at D=2, P=3).  The first
+ * call on a device looks up the array's device address (make it before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU
+ * race.  Work is issued on `stream` (NULL: default stream), asynchronously. */
+#define ADG_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+int adg_ader_step_noalloc(int D, int P, const int n_cell[3], const double prob_lo[3], const double prob_hi[3],
+                          double gamma, double dt, double* U_w, void* stream);
 
 /* Algorithmic FP64 flops per element-step (the method's dense matvec count)
  * and the FP64 operations the generated kernels actually issue per element. */
