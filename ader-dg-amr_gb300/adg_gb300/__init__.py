@@ -92,6 +92,9 @@ def lib():
         "adg_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(vp)], i),
         "adg_host_free": ([vp], i),
         "adg_flops_per_element": ([i, i, dp, dp], i),
+        "adg_regrid_count": ([vp, ctypes.POINTER(i)], i),
+        "adg_get_boxes": ([vp, i, ctypes.POINTER(i), i, ctypes.POINTER(i)], i),
+        "adg_tags": ([vp, i, ctypes.POINTER(ctypes.c_uint8)], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -318,6 +321,26 @@ class AmrDG:
         out = (ctypes.c_double * 5)()
         self._check(self._L.adg_time_kernels(self.ctx, int(nsteps), out, 5), "adg_time_kernels")
         return {"predictor": out[0], "numflux": out[1], "corrector": out[2], "dt": out[3], "amr_sync": out[4]}
+
+    def regrid_count(self):
+        n = ctypes.c_int()
+        self._check(self._L.adg_regrid_count(self.ctx, ctypes.byref(n)), "adg_regrid_count")
+        return n.value
+
+    def boxes(self, lev):
+        """Boxes of level lev: array [nbox, 6] = lo0, lo1, lo2, hi0, hi1, hi2."""
+        cap = 1 << 16
+        buf = (ctypes.c_int * (6 * cap))()
+        n = ctypes.c_int()
+        self._check(self._L.adg_get_boxes(self.ctx, lev, buf, cap, ctypes.byref(n)), "adg_get_boxes")
+        return np.frombuffer(buf, dtype=np.int32, count=6 * n.value).reshape(n.value, 6).copy()
+
+    def tags(self, lev):
+        """Refinement tags of the valid cells of level lev (current state)."""
+        n = self.level_cells(lev)
+        out = np.zeros(n, dtype=np.uint8)
+        self._check(self._L.adg_tags(self.ctx, lev, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))), "adg_tags")
+        return out
 
     def set_stream(self, stream_handle):
         self._check(self._L.adg_set_stream(self.ctx, ctypes.c_void_p(stream_handle)), "adg_set_stream")

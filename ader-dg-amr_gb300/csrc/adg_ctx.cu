@@ -76,8 +76,12 @@ struct adg_ctx {
   long long launches = 0;
 
   Hierarchy hier;       // host layout (levels, boxes, element and face tables)
+  amr::GridParams gp;
   bool initialised = false;
   bool tables_dirty = true;
+  long long nstep = 0;  // completed steps (regrid schedule)
+  bool first_step = true;
+  int n_regrids = 0;
 
   // device state
   DevBuf<double> Uw, Rvol, Tr, Fnum, Hw_dbg;
@@ -86,6 +90,11 @@ struct adg_ctx {
   DevBuf<double> scal;  // [0] Dt, [1] t
   DevBuf<unsigned long long> min_bits;
   DevBuf<unsigned int> status;
+  // AMR tables
+  DevBuf<int> rf_elem, rf_off, rf_face, rf_fine, ad_all, gf_elem, gf_parent;
+  DevBuf<int8_t> rf_dside, gf_child;
+  std::vector<size_t> ad_off;  // offset (ints) of level lf's records in ad_all
+  DevBuf<uint8_t> tags;
 
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -97,6 +106,8 @@ struct adg_ctx {
     Uw.release(); Rvol.release(); Tr.release(); Fnum.release(); Hw_dbg.release();
     face_left.release(); face_right.release(); elem_face.release(); elem_cell.release();
     elem_level.release(); scal.release(); min_bits.release(); status.release();
+    rf_elem.release(); rf_off.release(); rf_face.release(); rf_fine.release(); ad_all.release();
+    gf_elem.release(); gf_parent.release(); rf_dside.release(); gf_child.release(); tags.release();
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 };
@@ -150,6 +161,28 @@ int upload_tables(adg_ctx* ctx) {
   ADG_CUDA(cudaMemcpyAsync(ctx->elem_face.p, H.elem_face.data(), H.elem_face.size() * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
   ADG_CUDA(cudaMemcpyAsync(ctx->elem_cell.p, H.elem_cell.data(), H.elem_cell.size() * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
   ADG_CUDA(cudaMemcpyAsync(ctx->elem_level.p, H.elem_level.data(), H.elem_level.size(), cudaMemcpyHostToDevice, s), "h2d");
+  // coarse-fine tables
+  auto up = [&](auto& buf, const auto& vec, const char* what) -> cudaError_t {
+    cudaError_t e = buf.ensure(vec.size());
+    if (e != cudaSuccess || vec.empty()) return e;
+    return cudaMemcpyAsync(buf.p, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice, s);
+  };
+  ADG_CUDA(up(ctx->rf_elem, H.rf_elem, "rf"), "h2d reflux");
+  ADG_CUDA(up(ctx->rf_off, H.rf_off, "rf"), "h2d reflux");
+  ADG_CUDA(up(ctx->rf_face, H.rf_face, "rf"), "h2d reflux");
+  ADG_CUDA(up(ctx->rf_dside, H.rf_dside, "rf"), "h2d reflux");
+  ADG_CUDA(up(ctx->rf_fine, H.rf_fine, "rf"), "h2d reflux");
+  std::vector<int> ad;
+  ctx->ad_off.assign(H.nlevels() + 1, 0);
+  for (int lf = 0; lf < H.nlevels(); ++lf) {
+    ctx->ad_off[lf] = ad.size();
+    ad.insert(ad.end(), H.ad_rec[lf].begin(), H.ad_rec[lf].end());
+  }
+  ctx->ad_off[H.nlevels()] = ad.size();
+  ADG_CUDA(up(ctx->ad_all, ad, "ad"), "h2d average down");
+  ADG_CUDA(up(ctx->gf_elem, H.gf_elem, "gf"), "h2d ghosts");
+  ADG_CUDA(up(ctx->gf_parent, H.gf_parent, "gf"), "h2d ghosts");
+  ADG_CUDA(up(ctx->gf_child, H.gf_child, "gf"), "h2d ghosts");
   ADG_CUDA(cudaStreamSynchronize(s), "sync tables");
   ctx->tables_dirty = false;
   if (ctx->graph_exec) {
@@ -209,6 +242,50 @@ int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
   if (e != cudaSuccess) return cuda_fail(ctx, e, "corrector launch");
   ctx->launches++;
   if (ev) cudaEventRecord(ev[3], ctx->stream);
+  if (!H.rf_elem.empty()) {  // coarse-fine flux correction (AmrDG.h:1159-1162)
+    RefluxArgs ra{};
+    ra.Uw = ctx->Uw.p;
+    ra.Fnum = ctx->Fnum.p;
+    ra.rec_elem = ctx->rf_elem.p;
+    ra.rec_off = ctx->rf_off.p;
+    ra.ent_face = ctx->rf_face.p;
+    ra.ent_dside = ctx->rf_dside.p;
+    ra.ent_fine = ctx->rf_fine.p;
+    ra.elem_level = ctx->elem_level.p;
+    ra.nrec = (int)H.rf_elem.size();
+    ra.geom = pa.geom;
+    ra.dt = ctx->scal.p;
+    e = ks->reflux(ra, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "reflux launch");
+    ctx->launches++;
+  }
+  return ADG_OK;
+}
+
+// Fine -> coarse average down (finest first) and the coarse -> fine ghost
+// fill (AmrDG.h:999-1015).
+int launch_amr_sync(adg_ctx* ctx) {
+  const Hierarchy& H = ctx->hier;
+  if (H.nlevels() <= 1) return ADG_OK;
+  const int NOV1 = (1 << ctx->cfg.D) + 1;
+  for (int lf = H.nlevels() - 1; lf >= 1; --lf) {
+    const int nrec = (int)(H.ad_rec[lf].size() / NOV1);
+    if (!nrec) continue;
+    cudaError_t e = ctx->ks->average_down(ctx->Uw.p, ctx->ad_all.p + ctx->ad_off[lf], nrec, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "average down launch");
+    ctx->launches++;
+  }
+  if (!H.gf_elem.empty()) {
+    ScatterArgs sa{};
+    sa.Uw = ctx->Uw.p;
+    sa.dst = ctx->gf_elem.p;
+    sa.parent = ctx->gf_parent.p;
+    sa.child = ctx->gf_child.p;
+    sa.n = (int)H.gf_elem.size();
+    cudaError_t e = ctx->ks->scatter(sa, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "ghost fill launch");
+    ctx->launches++;
+  }
   return ADG_OK;
 }
 
@@ -240,15 +317,168 @@ int launch_dt(adg_ctx* ctx, int advance_time) {
 int launch_step(adg_ctx* ctx, cudaEvent_t* ev = nullptr) {
   int rc = launch_ader(ctx, nullptr, ev);
   if (rc) return rc;
-  rc = launch_dt(ctx, 1);
+  rc = launch_amr_sync(ctx);
+  if (rc) return rc;
   if (ev) cudaEventRecord(ev[4], ctx->stream);
+  rc = launch_dt(ctx, 1);
+  if (ev) cudaEventRecord(ev[5], ctx->stream);
   return rc;
 }
+
+// Regrid (AmrDG.h:935-986): refinement indicator on the device, tags to the
+// host, new boxes (amr_grids.hpp), new layout, and the level-by-level remap
+// of the state (RemakeLevel / MakeNewLevelFromCoarse, AmrDG_Level.tpp:52-132).
+int regrid(adg_ctx* ctx) {
+  Hierarchy& H = ctx->hier;
+  const KernelSet* ks = ctx->ks;
+  const int F = H.nlevels() - 1;
+  const int max_crse = std::min(F, ctx->cfg.max_level - 1);
+  const size_t nt = H.level_valid_offset(max_crse) + H.level_valid_count(max_crse);
+  ADG_CUDA(ctx->tags.ensure(nt), "alloc tags");
+  for (int l = 0; l <= max_crse; ++l) {
+    TagArgs ta{};
+    ta.Uw = ctx->Uw.p;
+    ta.elem_face = ctx->elem_face.p;
+    ta.face_left = ctx->face_left.p;
+    ta.face_right = ctx->face_right.p;
+    ta.e0 = (int)H.level_valid_offset(l);
+    ta.n = (int)H.level_valid_count(l);
+    ta.kind = ctx->cfg.tag_kind;
+    ta.threshold = ctx->cfg.tag_threshold;
+    ta.gamma = ctx->cfg.gamma;
+    ta.tags = ctx->tags.p + H.level_valid_offset(l);
+    cudaError_t e = ks->tag(ta, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "tag launch");
+    ctx->launches++;
+  }
+  std::vector<uint8_t> ht(nt);
+  ADG_CUDA(cudaMemcpyAsync(ht.data(), ctx->tags.p, nt, cudaMemcpyDeviceToHost, ctx->stream), "tags d2h");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "tags sync");
+  std::vector<amr::TagField> tf(F + 1);
+  for (int l = 0; l <= F; ++l) {
+    int n[3];
+    H.dims(l, n);
+    tf[l].init(n);
+    if (l > max_crse) continue;
+    for (size_t e = H.level_valid_offset(l); e < H.level_valid_offset(l) + H.level_valid_count(l); ++e)
+      if (ht[e]) tf[l].f[tf[l].idx(H.elem_cell[3 * e], H.elem_cell[3 * e + 1], H.elem_cell[3 * e + 2])] = 1;
+  }
+  std::vector<std::vector<amr::IBox>> ng = amr::make_new_grids(ctx->gp, H.grids, tf);
+  Hierarchy NH;
+  std::string msg;
+  if (!NH.build(ctx->gp, ng, ctx->cfg.reflux_box_quirk, &msg)) return fail(ctx, ADG_ERR_LAYOUT, "regrid: " + msg);
+  // remap: level 0 is unchanged; level l from the old level l where a cell
+  // was valid there, else from the new level l-1.
+  DevBuf<double> nU;
+  const int Q = ks->Q, Ns = ks->Np_s;
+  ADG_CUDA(nU.ensure(NH.n_elem() * Q * Ns), "alloc regrid state");
+  ADG_CUDA(cudaMemcpyAsync(nU.p, ctx->Uw.p, H.level_valid_count(0) * Q * Ns * sizeof(double), cudaMemcpyDeviceToDevice,
+                           ctx->stream), "regrid copy level 0");
+  DevBuf<int> d_dst, d_par, d_src;
+  DevBuf<int8_t> d_ch;
+  for (int l = 1; l < NH.nlevels(); ++l) {
+    std::vector<int> dst, par, src;
+    std::vector<int8_t> ch;
+    for (size_t e = 0; e < NH.n_elem(); ++e) {
+      if (NH.elem_level[e] != l) continue;
+      const int* c = &NH.elem_cell[3 * e];
+      int pc[3] = {0, 0, 0}, child = 0;
+      for (int a = 0; a < NH.D; ++a) {
+        pc[a] = c[a] >> 1;
+        child += (c[a] & 1) << (NH.D - 1 - a);
+      }
+      int old = -1;
+      if (l < H.nlevels()) {
+        int oe = H.elem_at(l, c);
+        if (H.is_valid_elem(oe)) old = oe;
+      }
+      dst.push_back((int)e);
+      par.push_back(NH.cellmap[l - 1][NH.cidx(l - 1, pc)]);
+      src.push_back(old);
+      ch.push_back((int8_t)child);
+    }
+    if (dst.empty()) continue;
+    ADG_CUDA(d_dst.ensure(dst.size()), "alloc");
+    ADG_CUDA(d_par.ensure(dst.size()), "alloc");
+    ADG_CUDA(d_src.ensure(dst.size()), "alloc");
+    ADG_CUDA(d_ch.ensure(dst.size()), "alloc");
+    ADG_CUDA(cudaMemcpyAsync(d_dst.p, dst.data(), dst.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    ADG_CUDA(cudaMemcpyAsync(d_par.p, par.data(), dst.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    ADG_CUDA(cudaMemcpyAsync(d_src.p, src.data(), dst.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    ADG_CUDA(cudaMemcpyAsync(d_ch.p, ch.data(), dst.size(), cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    ScatterArgs sa{};
+    sa.Uw = nU.p;
+    sa.Uw_old = ctx->Uw.p;
+    sa.dst = d_dst.p;
+    sa.parent = d_par.p;
+    sa.child = d_ch.p;
+    sa.src_old = d_src.p;
+    sa.n = (int)dst.size();
+    cudaError_t e = ks->scatter(sa, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "regrid remap launch");
+    ctx->launches++;
+    ADG_CUDA(cudaStreamSynchronize(ctx->stream), "regrid remap sync");  // host vectors go out of scope
+  }
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "regrid sync");
+  std::swap(ctx->Uw, nU);
+  nU.release();
+  d_dst.release(); d_par.release(); d_src.release(); d_ch.release();
+  ctx->hier = std::move(NH);
+  ctx->n_regrids++;
+  return upload_tables(ctx);
+}
+
+bool regrid_due(const adg_ctx* ctx) {
+  if (ctx->cfg.max_level <= 0) return false;
+  return ctx->first_step || (ctx->cfg.dtn_regrid > 0 && ctx->nstep % ctx->cfg.dtn_regrid == 0);
+}
+
+// One evolve-loop body: regrid when due (host), then the step kernels.
+int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev = nullptr);
 
 int check_ready(adg_ctx* ctx) {
   if (!ctx) return ADG_ERR_ARG;
   if (!ctx->initialised) return fail(ctx, ADG_ERR_STATE, "adg_init has not been called");
   if (ctx->tables_dirty) return upload_tables(ctx);
+  return ADG_OK;
+}
+
+int capture_graph(adg_ctx* ctx) {
+  long long before = ctx->launches;
+  ADG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+  int rc = launch_step(ctx);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "end capture");
+  ctx->graph = g;
+  ADG_CUDA(cudaGraphInstantiate(&ctx->graph_exec, g, 0), "graph instantiate");
+  ctx->graph_kernels = (int)(ctx->launches - before);
+  ctx->launches = before;
+  return ADG_OK;
+}
+
+int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
+  if (regrid_due(ctx)) {
+    int rc = regrid(ctx);
+    if (rc) return rc;
+  }
+  ctx->first_step = false;
+  if (use_graph && !ev) {
+    if (!ctx->graph_exec) {
+      int rc = capture_graph(ctx);
+      if (rc) return rc;
+    }
+    ADG_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream), "graph launch");
+    ctx->launches += ctx->graph_kernels;
+  } else {
+    int rc = launch_step(ctx, ev);
+    if (rc) return rc;
+  }
+  ctx->nstep++;
   return ADG_OK;
 }
 
@@ -326,18 +556,36 @@ int adg_set_stream(adg_ctx* ctx, void* stream) {
 int adg_init(adg_ctx* ctx) {
   if (!ctx) return ADG_ERR_ARG;
   const adg_config& c = ctx->cfg;
-  std::string msg;
-  if (!ctx->hier.build_single_level(c, &msg)) return fail(ctx, ADG_ERR_LAYOUT, msg);
   const KernelSet* ks = ctx->ks;
-  const size_t ne = ctx->hier.n_elem();
-  ADG_CUDA(ctx->Uw.ensure(ne * ks->Q * ks->Np_s), "alloc Uw");
+  std::string msg;
+  ctx->gp = Hierarchy::params(c);
+  // Single level: one box over the domain.  AMR: level 0 chopped to
+  // max_grid, every finer level a full-domain grid to start with (the
+  // reference's initial hierarchy, Source/Core/Solver.h:571-573); the first
+  // step regrids from the refinement indicator.
+  std::vector<std::vector<amr::IBox>> g;
+  if (c.max_level <= 0) {
+    if (!ctx->hier.build_single_level(c, &msg)) return fail(ctx, ADG_ERR_LAYOUT, msg);
+  } else {
+    for (int l = 0; l <= c.max_level; ++l) {
+      amr::IBox dom;
+      for (int d = 0; d < 3; ++d) {
+        dom.lo[d] = 0;
+        dom.hi[d] = d < c.D ? (c.n_cell[d] << l) - 1 : 0;
+      }
+      g.push_back(amr::chop_max_size({dom}, c.D, ctx->gp.max_grid));
+    }
+    if (!ctx->hier.build(ctx->gp, g, c.reflux_box_quirk, &msg)) return fail(ctx, ADG_ERR_LAYOUT, msg);
+  }
+  const Hierarchy& H = ctx->hier;
+  ADG_CUDA(ctx->Uw.ensure(H.n_elem() * ks->Q * ks->Np_s), "alloc Uw");
   int rc = upload_tables(ctx);
   if (rc) return rc;
   ICArgs ia{};
   ia.Uw = ctx->Uw.p;
   ia.elem_cell = ctx->elem_cell.p;
-  ia.elem_level = nullptr;
-  ia.n_elem = (int)ne;
+  ia.elem_level = nullptr;  // level 0 elements come first
+  ia.n_elem = (int)H.level_valid_count(0);
   ia.geom = level_geom(ctx);
   for (int d = 0; d < 3; ++d) {
     ia.prob_lo[d] = c.prob_lo[d];
@@ -355,7 +603,46 @@ int adg_init(adg_ctx* ctx) {
   cudaError_t e = ks->init_ic(ia, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "init_ic launch");
   ctx->launches++;
+  // finer levels: projection from the coarser level (AMR_interpolate_initial_condition)
+  DevBuf<int> d_dst, d_par;
+  DevBuf<int8_t> d_ch;
+  for (int l = 1; l < H.nlevels(); ++l) {
+    std::vector<int> dst, par;
+    std::vector<int8_t> ch;
+    for (size_t x = H.level_valid_offset(l); x < H.level_valid_offset(l) + H.level_valid_count(l); ++x) {
+      const int* cc = &H.elem_cell[3 * x];
+      int pc[3] = {0, 0, 0}, child = 0;
+      for (int a = 0; a < H.D; ++a) {
+        pc[a] = cc[a] >> 1;
+        child += (cc[a] & 1) << (H.D - 1 - a);
+      }
+      dst.push_back((int)x);
+      par.push_back(H.cellmap[l - 1][H.cidx(l - 1, pc)]);
+      ch.push_back((int8_t)child);
+    }
+    ADG_CUDA(d_dst.ensure(dst.size()), "alloc");
+    ADG_CUDA(d_par.ensure(dst.size()), "alloc");
+    ADG_CUDA(d_ch.ensure(dst.size()), "alloc");
+    ADG_CUDA(cudaMemcpyAsync(d_dst.p, dst.data(), dst.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    ADG_CUDA(cudaMemcpyAsync(d_par.p, par.data(), dst.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    ADG_CUDA(cudaMemcpyAsync(d_ch.p, ch.data(), dst.size(), cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    ScatterArgs sa{};
+    sa.Uw = ctx->Uw.p;
+    sa.dst = d_dst.p;
+    sa.parent = d_par.p;
+    sa.child = d_ch.p;
+    sa.n = (int)dst.size();
+    e = ks->scatter(sa, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "initial projection launch");
+    ctx->launches++;
+    ADG_CUDA(cudaStreamSynchronize(ctx->stream), "init projection sync");
+  }
+  d_dst.release(); d_par.release(); d_ch.release();
   ctx->initialised = true;
+  ctx->nstep = 0;
+  ctx->first_step = true;
+  rc = launch_amr_sync(ctx);
+  if (rc) return rc;
   rc = launch_dt(ctx, 0);
   if (rc) return rc;
   ADG_CUDA(cudaStreamSynchronize(ctx->stream), "init sync");
@@ -444,7 +731,7 @@ int adg_ader(adg_ctx* ctx) {
 int adg_step(adg_ctx* ctx) {
   int rc = check_ready(ctx);
   if (rc) return rc;
-  rc = launch_step(ctx);
+  rc = host_step(ctx, false);
   if (rc) return rc;
   ADG_CUDA(cudaStreamSynchronize(ctx->stream), "step sync");
   return ADG_OK;
@@ -454,33 +741,53 @@ int adg_advance(adg_ctx* ctx, int nsteps, int use_graph) {
   int rc = check_ready(ctx);
   if (rc) return rc;
   if (nsteps < 0) return fail(ctx, ADG_ERR_ARG, "negative step count");
-  if (!use_graph) {
-    for (int s = 0; s < nsteps; ++s) {
-      rc = launch_step(ctx);
-      if (rc) return rc;
-    }
-    return ADG_OK;
-  }
-  if (!ctx->graph_exec) {
-    long long before = ctx->launches;
-    ADG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-    rc = launch_step(ctx);
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-    if (rc) {
-      if (g) cudaGraphDestroy(g);
-      return rc;
-    }
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "end capture");
-    ctx->graph = g;
-    ADG_CUDA(cudaGraphInstantiate(&ctx->graph_exec, g, 0), "graph instantiate");
-    ctx->graph_kernels = (int)(ctx->launches - before);
-    ctx->launches = before;
-  }
   for (int s = 0; s < nsteps; ++s) {
-    ADG_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream), "graph launch");
-    ctx->launches += ctx->graph_kernels;
+    rc = host_step(ctx, use_graph != 0);
+    if (rc) return rc;
   }
+  return ADG_OK;
+}
+
+int adg_regrid_count(const adg_ctx* ctx, int* n) {
+  if (!ctx || !n) return ADG_ERR_ARG;
+  *n = ctx->n_regrids;
+  return ADG_OK;
+}
+
+int adg_get_boxes(const adg_ctx* ctx, int lev, int* out, int cap, int* nbox) {
+  if (!ctx || !nbox || lev < 0 || lev >= ctx->hier.nlevels()) return ADG_ERR_ARG;
+  const auto& g = ctx->hier.grids[lev];
+  *nbox = (int)g.size();
+  for (int b = 0; b < (int)g.size() && b < cap; ++b)
+    for (int d = 0; d < 3; ++d) {
+      out[6 * b + d] = g[b].lo[d];
+      out[6 * b + 3 + d] = g[b].hi[d];
+    }
+  return ADG_OK;
+}
+
+int adg_tags(adg_ctx* ctx, int lev, uint8_t* out) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  const Hierarchy& H = ctx->hier;
+  if (!out || lev < 0 || lev >= H.nlevels()) return fail(ctx, ADG_ERR_ARG, "bad level");
+  ADG_CUDA(ctx->tags.ensure(H.n_valid()), "alloc tags");
+  TagArgs ta{};
+  ta.Uw = ctx->Uw.p;
+  ta.elem_face = ctx->elem_face.p;
+  ta.face_left = ctx->face_left.p;
+  ta.face_right = ctx->face_right.p;
+  ta.e0 = (int)H.level_valid_offset(lev);
+  ta.n = (int)H.level_valid_count(lev);
+  ta.kind = ctx->cfg.tag_kind;
+  ta.threshold = ctx->cfg.tag_threshold;
+  ta.gamma = ctx->cfg.gamma;
+  ta.tags = ctx->tags.p;
+  cudaError_t e = ctx->ks->tag(ta, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "tag launch");
+  ctx->launches++;
+  ADG_CUDA(cudaMemcpyAsync(out, ctx->tags.p, ta.n, cudaMemcpyDeviceToHost, ctx->stream), "tags d2h");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "tags sync");
   return ADG_OK;
 }
 
@@ -492,8 +799,8 @@ int adg_advance_timed(adg_ctx* ctx, int nsteps, int use_graph, double* ms) {
   int rc = check_ready(ctx);
   if (rc) return rc;
   if (!ms) return ADG_ERR_ARG;
-  if (use_graph && !ctx->graph_exec) {  // capture outside the timed region
-    rc = adg_advance(ctx, 0, 1);
+  if (use_graph && !ctx->graph_exec && !regrid_due(ctx)) {  // capture outside the timed region
+    rc = capture_graph(ctx);
     if (rc) return rc;
   }
   cudaEvent_t e0, e1;
@@ -517,17 +824,18 @@ int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds) {
   int rc = check_ready(ctx);
   if (rc) return rc;
   if (!ms || nkinds < 1 || nsteps < 1) return ADG_ERR_ARG;
-  const int NEV = 5;
+  const int NEV = 6;
   std::vector<cudaEvent_t> ev((size_t)NEV * nsteps);
   for (auto& x : ev) ADG_CUDA(cudaEventCreate(&x), "event");
-  for (int s = 0; s < nsteps && rc == ADG_OK; ++s) rc = launch_step(ctx, &ev[(size_t)s * NEV]);
+  for (int s = 0; s < nsteps && rc == ADG_OK; ++s) rc = host_step(ctx, false, &ev[(size_t)s * NEV]);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   double acc[5] = {0, 0, 0, 0, 0};
   if (rc == ADG_OK && e == cudaSuccess) {
+    const int from[5] = {0, 1, 2, 4, 3}, to[5] = {1, 2, 3, 5, 4};
     for (int s = 0; s < nsteps; ++s)
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < 5; ++k) {
         float f = 0.f;
-        cudaEventElapsedTime(&f, ev[(size_t)s * NEV + k], ev[(size_t)s * NEV + k + 1]);
+        cudaEventElapsedTime(&f, ev[(size_t)s * NEV + from[k]], ev[(size_t)s * NEV + to[k]]);
         acc[k] += f;
       }
   }

@@ -79,6 +79,29 @@ struct Impl final : KernelSet {
     k_dt_reduce<O><<<(a.n_valid + bs - 1) / bs, bs, 0, s>>>(a);
     return cudaGetLastError();
   }
+  cudaError_t reflux(const RefluxArgs& a, cudaStream_t s) const override {
+    const long long n = (long long)a.nrec * O::Q;
+    if (n == 0) return cudaSuccess;
+    k_reflux<O><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  cudaError_t average_down(double* Uw, const int* rec, int nrec, cudaStream_t s) const override {
+    const long long n = (long long)nrec * O::Q;
+    if (n == 0) return cudaSuccess;
+    k_average_down<O><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(Uw, rec, nrec);
+    return cudaGetLastError();
+  }
+  cudaError_t scatter(const ScatterArgs& a, cudaStream_t s) const override {
+    const long long n = (long long)a.n * O::Q;
+    if (n == 0) return cudaSuccess;
+    k_scatter<O><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  cudaError_t tag(const TagArgs& a, cudaStream_t s) const override {
+    if (a.n == 0) return cudaSuccess;
+    k_tag<O><<<(a.n + 127) / 128, 128, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const override {
     const int bs = 64;
     k_init_ic<O><<<(a.n_elem + bs - 1) / bs, bs, 0, s>>>(a);

@@ -389,4 +389,228 @@ __global__ void k_init_ic(ICArgs a) {
   }
 }
 
+
+// ===========================================================================
+// AMR transfer kernels (L2ProjInterp, Source/NumericalMethod/AmrDG/AmrDG_Interpolater.tpp)
+// One thread per (element, variable) column; runtime child / face indices are
+// dispatched to the compile-time generated operators.
+// ===========================================================================
+template <class O, class In, class Out>
+__device__ __forceinline__ void pcf_rt(int l, const In& in, Out out) {
+  switch (l) {
+    case 0: O::template pcf<0>(in, out); break;
+    case 1: O::template pcf<1>(in, out); break;
+    case 2: O::template pcf<2>(in, out); break;
+    case 3: O::template pcf<3>(in, out); break;
+    default:
+      if constexpr (O::D == 3) {
+        switch (l) {
+          case 4: O::template pcf<4>(in, out); break;
+          case 5: O::template pcf<5>(in, out); break;
+          case 6: O::template pcf<6>(in, out); break;
+          default: O::template pcf<7>(in, out); break;
+        }
+      }
+  }
+}
+
+template <class O, int DD, int S, class In, class Out>
+__device__ __forceinline__ void pflux_k(int k, const In& in, Out out) {
+  if constexpr (O::D == 2) {
+    if (k == 0) O::template pflux<DD, S, 0>(in, out);
+    else O::template pflux<DD, S, 1>(in, out);
+  } else {
+    switch (k) {
+      case 0: O::template pflux<DD, S, 0>(in, out); break;
+      case 1: O::template pflux<DD, S, 1>(in, out); break;
+      case 2: O::template pflux<DD, S, 2>(in, out); break;
+      default: O::template pflux<DD, S, 3>(in, out); break;
+    }
+  }
+}
+
+// Coarse-fine flux correction (FluxRegister CrseAdd/FineAdd/Reflux +
+// L2ProjInterp::reflux, AmrDG.h:1138-1161, AmrDG_Interpolater.tpp:7-72):
+//   corr = sum_faces sgn * (J_c Mkbd Fnum_c - sum_k J_f P_flux[k] Fnum_f[k]),
+//   U_c += (2^D / vol_c) Minv corr,  sgn = +1 on the coarse cell's high face.
+struct RefluxArgs {
+  double* Uw;
+  const double* Fnum;
+  const int* rec_elem;
+  const int* rec_off;
+  const int* ent_face;
+  const int8_t* ent_dside;
+  const int* ent_fine;
+  const int8_t* elem_level;
+  int nrec;
+  LevelGeom geom;
+  const double* dt;
+};
+
+template <class O>
+__global__ void k_reflux(RefluxArgs a) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NB = O::NQ_BD, NFC = 1 << (D - 1);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)a.nrec * Q) return;
+  const int r = (int)(t / Q), q = (int)(t % Q);
+  const int e = a.rec_elem[r];
+  const int lc = a.elem_level[e];
+  const double dt = *a.dt;
+  double corr[NP_S];
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) corr[n] = 0.0;
+  for (int x = a.rec_off[r]; x < a.rec_off[r + 1]; ++x) {
+    const int ds = a.ent_dside[x];
+    const int d = ds >> 1, side = ds & 1;
+    double area_c = 1.0, area_f = 1.0;
+    for (int k = 0; k < D; ++k)
+      if (k != d) {
+        area_c *= a.geom.dx[lc][k];
+        area_f *= a.geom.dx[lc + 1][k];
+      }
+    const double Jc = (dt / 2.0) * (area_c / (double)NFC);
+    const double Jf = (dt / 2.0) * (area_f / (double)NFC);
+    double fc[NP_S], ff[NP_S], tmp[NP_S];
+    const double* fnc = a.Fnum + ((size_t)a.ent_face[x] * Q + q) * NB;
+#define ADG_FC(DD, SS) O::template bd_term<DD, SS>(RegIn{fnc}, RegOut{fc})
+    if (d == 0) { if (side) ADG_FC(0, 1); else ADG_FC(0, 0); }
+    else if (d == 1) { if (side) ADG_FC(1, 1); else ADG_FC(1, 0); }
+    else if constexpr (D == 3) { if (side) ADG_FC(2, 1); else ADG_FC(2, 0); }
+#undef ADG_FC
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) ff[n] = 0.0;
+    for (int k = 0; k < NFC; ++k) {
+      const double* fnf = a.Fnum + ((size_t)a.ent_fine[(size_t)x * NFC + k] * Q + q) * NB;
+#define ADG_FF(DD, SS) pflux_k<O, DD, SS>(k, RegIn{fnf}, RegOut{tmp})
+      if (d == 0) { if (side) ADG_FF(0, 1); else ADG_FF(0, 0); }
+      else if (d == 1) { if (side) ADG_FF(1, 1); else ADG_FF(1, 0); }
+      else if constexpr (D == 3) { if (side) ADG_FF(2, 1); else ADG_FF(2, 0); }
+#undef ADG_FF
+#pragma unroll
+      for (int n = 0; n < NP_S; ++n) ff[n] += tmp[n];
+    }
+    const double sgn = side ? 1.0 : -1.0;
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) corr[n] += sgn * (Jc * fc[n] - Jf * ff[n]);
+  }
+  double vol = 1.0;
+  for (int k = 0; k < D; ++k) vol *= a.geom.dx[lc][k];
+  const double inv_jac = (double)(1 << D) / vol;
+  double* u = a.Uw + ((size_t)e * Q + q) * NP_S;
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) u[n] += inv_jac * (O::minv(n) * corr[n]);
+}
+
+// average_down / amr_gather (AmrDG_Interpolater.tpp:283-342, 366-398):
+// u_c = 2^-D Minv sum_l P_fc[l] u_f[l].  rec: coarse, fine_0 .. fine_{2^D-1}.
+template <class O>
+__global__ void k_average_down(double* Uw, const int* rec, int nrec) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NOV = 1 << D;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nrec * Q) return;
+  const int r = (int)(t / Q), q = (int)(t % Q);
+  const int* rr = rec + (size_t)r * (NOV + 1);
+  double sum[NP_S], tmp[NP_S];
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) sum[n] = 0.0;
+#define ADG_G(L)                                                                      \
+  {                                                                                   \
+    O::template pfc<L>(RegIn{Uw + ((size_t)rr[1 + L] * Q + q) * NP_S}, RegOut{tmp});  \
+    _Pragma("unroll") for (int n = 0; n < NP_S; ++n) sum[n] += tmp[n];                \
+  }
+  ADG_G(0) ADG_G(1) ADG_G(2) ADG_G(3)
+  if constexpr (D == 3) { ADG_G(4) ADG_G(5) ADG_G(6) ADG_G(7) }
+#undef ADG_G
+  double* uc = Uw + ((size_t)rr[0] * Q + q) * NP_S;
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) uc[n] = (1.0 / NOV) * (O::minv(n) * sum[n]);
+}
+
+// Coarse -> fine projection (amr_scatter, AmrDG_Interpolater.tpp:344-364)
+// into ghost elements (FillPatchTwoLevels) or, with src_old, the regrid
+// remap of a level (valid data of the old layout where it existed).
+struct ScatterArgs {
+  double* Uw;            // destination array (and coarse source)
+  const double* Uw_old;  // optional: old layout's state
+  const int* dst;        // [n] destination element
+  const int* parent;     // [n] coarse parent element in Uw
+  const int8_t* child;   // [n] child index
+  const int* src_old;    // optional [n]: element in Uw_old, -1 = project
+  int n;
+};
+
+template <class O>
+__global__ void k_scatter(ScatterArgs a) {
+  constexpr int Q = O::Q, NP_S = O::NP_S;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)a.n * Q) return;
+  const int i = (int)(t / Q), q = (int)(t % Q);
+  double* dst = a.Uw + ((size_t)a.dst[i] * Q + q) * NP_S;
+  if (a.src_old && a.src_old[i] >= 0) {
+    const double* s = a.Uw_old + ((size_t)a.src_old[i] * Q + q) * NP_S;
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) dst[n] = s[n];
+    return;
+  }
+  double v[NP_S];
+  pcf_rt<O>(a.child[i], RegIn{a.Uw + ((size_t)a.parent[i] * Q + q) * NP_S}, RegOut{v});
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) dst[n] = v[n];
+}
+
+// Refinement indicator on cell means (mode 0), tag when above threshold:
+// kind 0 normalised density gradient max_d |rho(i+e_d)-rho(i-e_d)|/(2 rho(i)),
+// kind 1 the same on pressure.  IEEE operations in a fixed order (no FMA
+// contraction) so the indicator is the one the CPU oracle evaluates.
+struct TagArgs {
+  const double* Uw;
+  const int* elem_face;
+  const int* face_left;
+  const int* face_right;
+  int e0, n;
+  int kind;
+  double threshold, gamma;
+  uint8_t* tags;
+};
+
+template <class O>
+__device__ __forceinline__ double cell_pressure(const double* Uw, int e, double gamma) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S;
+  const double rho = Uw[((size_t)e * Q + 0) * NP_S];
+  double ke = 0.0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double m = Uw[((size_t)e * Q + d + 1) * NP_S];
+    ke = __dadd_rn(ke, __ddiv_rn(__dmul_rn(m, m), rho));
+  }
+  const double E = Uw[((size_t)e * Q + D + 1) * NP_S];
+  return __dmul_rn(gamma - 1.0, __dsub_rn(E, __dmul_rn(0.5, ke)));
+}
+
+template <class O>
+__global__ void k_tag(TagArgs a) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int e = a.e0 + i;
+  double ind = 0.0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const int hi = a.face_right[a.elem_face[(size_t)e * 2 * D + 2 * d + 1]];
+    const int lo = a.face_left[a.elem_face[(size_t)e * 2 * D + 2 * d]];
+    double v;
+    if (a.kind == 0) {
+      const double rp = a.Uw[((size_t)hi * Q) * NP_S], rm = a.Uw[((size_t)lo * Q) * NP_S];
+      const double rc = a.Uw[((size_t)e * Q) * NP_S];
+      v = __ddiv_rn(fabs(__dsub_rn(rp, rm)), __dmul_rn(2.0, rc));
+    } else {
+      const double pp = cell_pressure<O>(a.Uw, hi, a.gamma), pm = cell_pressure<O>(a.Uw, lo, a.gamma);
+      const double pc = cell_pressure<O>(a.Uw, e, a.gamma);
+      v = __ddiv_rn(fabs(__dsub_rn(pp, pm)), __dmul_rn(2.0, pc));
+    }
+    ind = fmax(ind, v);
+  }
+  a.tags[i] = ind > a.threshold ? 1 : 0;
+}
+
 }  // namespace adg

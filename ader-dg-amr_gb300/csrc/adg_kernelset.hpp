@@ -21,6 +21,10 @@ struct KernelSet {
   virtual cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t dt_reduce(const DtArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t reflux(const RefluxArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t average_down(double* Uw, const int* rec, int nrec, cudaStream_t s) const = 0;
+  virtual cudaError_t scatter(const ScatterArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t tag(const TagArgs& a, cudaStream_t s) const = 0;
 };
 
 const KernelSet* kernels_D2P1();

@@ -640,10 +640,84 @@ def add_ic_proj(el, ops):
     ops["ic_proj"] = (stages, len(pt_keys), el.Np_s)
 
 
+def add_amr_ops(el, ops):
+    """L2ProjInterp operators (AmrDG_Interpolater.tpp:85-231), each an exact
+    sum of products of the double-valued tables, rounded once:
+      pcf{l}      = Minv P_cf[l]              coarse -> fine child l (amr_scatter)
+      pfc{l}      = P_fc[l]                   fine child l -> coarse (amr_gather)
+      pflux{d}{s}{k} = P_flux_fc_{low,high}[d][k]  fine face points -> coarse face modes
+    Child l of P_cf / P_fc: bit (D-1-d) of l is the upper half in direction d.
+    Face child k of P_flux: bit i of k is the upper half in the i-th direction != d."""
+    D, P, N = el.D, el.P, el.N
+    ms = el.mi_s
+    quad = [[Fraction(0)] * len(el.pts_s) for _ in ms]  # quadmat (exact products of doubles)
+    for j, n in enumerate(ms):
+        for qi, pt in enumerate(el.pts_s):
+            w = Fraction(1)
+            ph = Fraction(1)
+            for d in range(D):
+                w *= Fraction(el.weights[pt[d]])
+                ph *= Fraction(el.val[n[d]][pt[d]])
+            quad[j][qi] = ph * w
+    minv = [Fraction(1) / el.ms(n) for n in ms]
+    for l in range(1 << D):
+        up = [(l >> (D - 1 - d)) & 1 for d in range(D)]
+
+        def phi_child(n, pt):
+            v = Fraction(1)
+            for d in range(D):
+                tbl = el.shi if up[d] else el.slo
+                v *= Fraction(tbl[n[d]][pt[d]])
+            return v
+
+        Pcf = [[sum(quad[j][qi] * phi_child(ms[m], pt) for qi, pt in enumerate(el.pts_s)) for m in range(len(ms))]
+               for j in range(len(ms))]
+        Pfc = [[sum(quad[m][qi] * phi_child(ms[j], pt) for qi, pt in enumerate(el.pts_s)) for m in range(len(ms))]
+               for j in range(len(ms))]
+        cf = [[float(minv[j] * Pcf[j][m]) for m in range(len(ms))] for j in range(len(ms))]
+        fc = [[float(Pfc[j][m]) for m in range(len(ms))] for j in range(len(ms))]
+        ops[f"pcf{l}"] = ([Stage(len(ms), len(ms), [[(c, r[c]) for c in range(len(ms)) if r[c] != 0.0] for r in cf])],
+                          len(ms), len(ms))
+        ops[f"pfc{l}"] = ([Stage(len(ms), len(ms), [[(c, r[c]) for c in range(len(ms)) if r[c] != 0.0] for r in fc])],
+                          len(ms), len(ms))
+    nfc = 1 << (D - 1)
+    for d in range(D):
+        free = [a for a in range(D) if a != d] + [D]
+        for k in range(nfc):
+            upper = {}
+            bit = 0
+            for a in range(D):
+                if a == d:
+                    continue
+                upper[a] = (k >> bit) & 1
+                bit += 1
+            for side in range(2):
+                rows = []
+                for n in ms:
+                    row = []
+                    for pt in el.pts_bd:
+                        c = {a: pt[i] for i, a in enumerate(free)}
+                        w = Fraction(1)
+                        for a in free:
+                            w *= Fraction(el.weights[c[a]])
+                        ph = Fraction(el.bd[n[d]][side])
+                        for a in range(D):
+                            if a == d:
+                                continue
+                            tbl = el.shi if upper[a] else el.slo
+                            ph *= Fraction(tbl[n[a]][c[a]])
+                        row.append(float(ph * w))
+                    rows.append(row)
+                ops[f"pflux{d}{side}{k}"] = ([Stage(len(el.pts_bd), len(ms),
+                                                    [[(c, r[c]) for c in range(len(el.pts_bd)) if r[c] != 0.0]
+                                                     for r in rows])], len(el.pts_bd), len(ms))
+
+
 def generate(D, P, out_path):
     el = Element(D, P)
     ops = build_ops(el)
     add_ic_proj(el, ops)
+    add_amr_ops(el, ops)
     N = P + 1
     qst = N ** (D + 1)
     qbd = N ** D
@@ -693,6 +767,10 @@ def generate(D, P, out_path):
     hdr.append(disp("vol_term", [((d,), f"vol_term{d}") for d in range(D)], ["d"]))
     hdr.append(disp("face_eval", [((d, s), f"face_eval{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("bd_term", [((d, s), f"bd_term{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
+    hdr.append(disp("pcf", [((l,), f"pcf{l}") for l in range(1 << D)], ["l"]))
+    hdr.append(disp("pfc", [((l,), f"pfc{l}") for l in range(1 << D)], ["l"]))
+    hdr.append(disp("pflux", [((d, s, k), f"pflux{d}{s}{k}") for d in range(D) for s in range(2)
+                              for k in range(1 << (D - 1))], ["d", "s", "k"]))
     # FP64 instruction counts of the linear stages per column and step
     sweeps = P
     per_col = (counts["wu"] + counts["vol_eval_init"] + sum(counts[f"proj_init{d}"] for d in range(D)) + 2 * D * el.Np_st

@@ -110,6 +110,14 @@ int adg_step(adg_ctx* ctx);
  * (re-captured when the layout changes). */
 int adg_advance(adg_ctx* ctx, int nsteps, int use_graph);
 
+/* AMR layout: number of regrids so far; boxes of a level
+ * (out[6*b + {lo0,lo1,lo2,hi0,hi1,hi2}], up to cap boxes); refinement tags
+ * of the valid cells of a level from the current state (1 byte per cell, the
+ * level's cell order).  (AmrDG_TagCellRef.tpp:4-52, Mesh::regrid) */
+int adg_regrid_count(const adg_ctx* ctx, int* n);
+int adg_get_boxes(const adg_ctx* ctx, int lev, int* out, int cap, int* nbox);
+int adg_tags(adg_ctx* ctx, int lev, uint8_t* out);
+
 /* Per-stage entry points (parity testing). */
 /* Predictor only for level lev: writes H_w (Q * Np_st per cell, element-major)
  * for the valid cells to dst (device pointer). (AmrDG.tpp:495-537, 744-827) */

@@ -1,12 +1,29 @@
 // CPU oracle (test infrastructure only; never linked into the product).
 //
-// Time loop of the reference (AmrDG::evolve, Source/NumericalMethod/AmrDG/AmrDG.h:853-1055)
-// around the single-level ADER stages of oracle_solver.hpp.
+// Multi-level time loop of the reference around the single-level stages of
+// oracle_solver.hpp:
+//   evolve loop body             Source/NumericalMethod/AmrDG/AmrDG.h:935-1029
+//   ADER + flux registers        Source/NumericalMethod/AmrDG/AmrDG.h:1071-1165
+//   C-F flux projections         Source/NumericalMethod/AmrDG/AmrDG.tpp:554-647
+//   C-F face masks (ownership)   Source/NumericalMethod/AmrDG/AmrDG_Level.tpp:240-414
+//   AMR_flux_correction          Source/NumericalMethod/AmrDG/AmrDG_Level.tpp:416-446
+//   L2ProjInterp::reflux         Source/NumericalMethod/AmrDG/AmrDG_Interpolater.tpp:7-72
+//   amr_scatter / amr_gather     Source/NumericalMethod/AmrDG/AmrDG_Interpolater.tpp:344-398
+//   FillPatch / FillFromCoarse   Source/NumericalMethod/AmrDG/AmrDG_Level.tpp:137-224
+//   RemakeLevel / new level      Source/NumericalMethod/AmrDG/AmrDG_Level.tpp:52-132
+// Third-party semantics the reference takes from AMReX (absent from the
+// reference tree) are restated from AMReX's documented behaviour:
+// FluxRegister CrseAdd/FineAdd/Reflux (face-summed fine fluxes, mult, and the
+// -/+ orientation signs of Reflux), FillPatchTwoLevels (fine data first,
+// coarse interpolation for the rest), and AmrCore regrid (shared with the
+// product in ader-dg-amr_gb300/csrc/amr_grids.hpp).
 #pragma once
 
 #include <algorithm>
+#include <map>
 #include <vector>
 
+#include "amr_grids.hpp"
 #include "oracle_solver.hpp"
 
 namespace oracle {
@@ -23,28 +40,611 @@ struct AmrConfig {
   int reflux_box_quirk = 1;
 };
 
+namespace A = adg::amr;
+
 class AmrSim {
  public:
   Sim sim;
   AmrConfig amr;
+  A::GridParams gp;
+  std::vector<std::vector<A::IBox>> grids;
+  bool first_step = true;
+  int n_regrids = 0;
 
-  AmrSim(const SimConfig& s, const AmrConfig& a) : sim(s), amr(a) {}
+  AmrSim(const SimConfig& s, const AmrConfig& a) : sim(s), amr(a) {
+    gp.D = s.D;
+    for (int d = 0; d < 3; ++d) {
+      gp.n_cell0[d] = d < s.D ? s.n_cell[d] : 1;
+      gp.periodic[d] = d < s.D ? s.periodic[d] : 1;
+    }
+    gp.max_level = a.max_level;
+    gp.blocking_factor = a.blocking_factor;
+    gp.max_grid = a.max_grid;
+    gp.grid_eff = a.grid_eff;
+    gp.n_error_buf = a.n_error_buf;
+  }
 
+  int D() const { return sim.D; }
+  int finest() const { return (int)sim.lev.size() - 1; }
+
+  static std::vector<Box> to_boxes(const std::vector<A::IBox>& v) {
+    std::vector<Box> b(v.size());
+    for (size_t i = 0; i < v.size(); ++i)
+      for (int d = 0; d < 3; ++d) {
+        b[i].lo[d] = v[i].lo[d];
+        b[i].hi[d] = v[i].hi[d];
+      }
+    return b;
+  }
+
+  // ---------------------------------------------------------------- init
   double init() {
-    sim.define_single_level(amr.max_grid);
-    sim.set_initial_condition(0);
+    if (amr.max_level == 0) {
+      grids = {A::chop_max_size({full_domain(0)}, D(), amr.max_grid)};
+      sim.lev.clear();
+      sim.define_level(0, to_boxes(grids[0]));
+      sim.set_initial_condition(0);
+    } else {
+      // Every level starts as a full-domain grid (Source/Core/Solver.h:571-573);
+      // finer levels are filled by projection from the coarser one
+      // (AMR_interpolate_initial_condition, AmrDG_Level.tpp:134-137) and all
+      // ghost cells are synchronised (AMR_sync_initial_condition).
+      grids.clear();
+      sim.lev.clear();
+      for (int l = 0; l <= amr.max_level; ++l) {
+        grids.push_back(A::chop_max_size({full_domain(l)}, D(), amr.max_grid));
+        sim.define_level(l, to_boxes(grids[l]));
+      }
+      sim.set_initial_condition(0);
+      for (int l = 1; l <= amr.max_level; ++l) fill_from_coarse(l, nullptr);
+      for (int l = 0; l <= amr.max_level; ++l) fill_patch(l);
+    }
     sim.t = 0.0;
     sim.nstep = 0;
+    first_step = true;
     sim.Dt = sim.compute_Dt();
     return sim.Dt;
   }
 
-  void ader() {
-    for (int l = (int)sim.lev.size() - 1; l >= 0; --l) sim.ader_level(l);
+  A::IBox full_domain(int l) const {
+    A::IBox b;
+    for (int d = 0; d < 3; ++d) {
+      b.lo[d] = 0;
+      b.hi[d] = d < D() ? (sim.cfg.n_cell[d] << l) - 1 : 0;
+    }
+    return b;
   }
 
+  // ----------------------------------------------------------- cell utils
+  // Periodic wrap; false if outside a non-periodic domain.
+  bool wrap(const Level& L, int* c) const {
+    for (int d = 0; d < D(); ++d) {
+      if (c[d] >= 0 && c[d] < L.n[d]) continue;
+      if (!sim.cfg.periodic[d]) return false;
+      c[d] = ((c[d] % L.n[d]) + L.n[d]) % L.n[d];
+    }
+    return true;
+  }
+
+  bool valid_at(int l, const int* cin) const {
+    const Level& L = sim.lev[l];
+    int c[3] = {cin[0], cin[1], cin[2]};
+    if (!wrap(L, c)) return false;
+    return L.status[L.cell(c[0], c[1], c[2])] == ST_VALID;
+  }
+
+  bool covered(int l, const int* c) const {
+    if (l + 1 > finest()) return false;
+    int f[3] = {0, 0, 0};
+    for (int d = 0; d < D(); ++d) f[d] = 2 * c[d];
+    return valid_at(l + 1, f);
+  }
+
+  // amr_scatter (AmrDG_Interpolater.tpp:344-364): fine cell c of level l
+  // from its coarse parent on level l-1 (periodically wrapped).
+  bool scatter_into(int l, const int* c, double* out /*Q*Np_s element-major*/) const {
+    const Level& C = sim.lev[l - 1];
+    int cc[3] = {0, 0, 0}, idx = 0;
+    int f[3] = {c[0], c[1], c[2]};
+    const Level& F = sim.lev[l];
+    if (!wrap(F, f)) return false;
+    for (int d = 0; d < D(); ++d) {
+      cc[d] = f[d] >> 1;
+      idx += (f[d] - 2 * cc[d]) * (1 << (D() - 1 - d));
+    }
+    long src = C.cell(cc[0], cc[1], cc[2]);
+    const int Ns = sim.Np_s;
+    const Elem& el = sim.el;
+    for (int q = 0; q < sim.Q; ++q)
+      for (int n = 0; n < Ns; ++n) {
+        double s = 0.0;
+        for (int m = 0; m < Ns; ++m) {
+          double mp = el.Minv(n, n) * el.P_cf[idx](n, m);  // (Minv * P_cf)(n, m)
+          s += mp * C.Uw[((size_t)q * Ns + m) * C.ncell + src];
+        }
+        out[q * Ns + n] = s;
+      }
+    return true;
+  }
+
+  void put(Level& L, long c, const double* v) {
+    const int nc = sim.Q * sim.Np_s;
+    for (int k = 0; k < nc; ++k) L.Uw[(size_t)k * L.ncell + c] = v[k];
+  }
+
+  // InterpFromCoarseLevel with the L2 projection (AMR_FillFromCoarsePatch,
+  // AmrDG_Level.tpp:137-166): every active cell of level l from level l-1.
+  // old_valid: if given, cells that were valid on the old level l take the
+  // old data (FillPatchTwoLevels used by RemakeLevel).
+  void fill_from_coarse(int l, const Level* old) {
+    Level& L = sim.lev[l];
+    const int nc = sim.Q * sim.Np_s;
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < L.ncell; ++c) {
+      if (L.status[c] == ST_NONE) continue;
+      int ijk[3];
+      L.coords(c, ijk[0], ijk[1], ijk[2]);
+      if (old) {
+        int w[3] = {ijk[0], ijk[1], ijk[2]};
+        if (wrap(*old, w)) {
+          long oc = old->cell(w[0], w[1], w[2]);
+          if (old->status[oc] == ST_VALID) {
+            for (int k = 0; k < nc; ++k) L.Uw[(size_t)k * L.ncell + c] = old->Uw[(size_t)k * old->ncell + oc];
+            continue;
+          }
+        }
+      }
+      std::vector<double> v(nc);
+      if (scatter_into(l, ijk, v.data()))
+        for (int k = 0; k < nc; ++k) L.Uw[(size_t)k * L.ncell + c] = v[k];
+      else
+        for (int k = 0; k < nc; ++k) L.Uw[(size_t)k * L.ncell + c] = 0.0;
+    }
+  }
+
+  // AMR_FillPatch (AmrDG_Level.tpp:172-224) on a zeroed copy: valid cells,
+  // same-level periodic copies, coarse interpolation elsewhere in the
+  // domain; outside a non-periodic domain the cells stay zero (the physical
+  // BC is applied by FillBoundaryCells at the next ADER).
+  void fill_patch(int l) {
+    Level& L = sim.lev[l];
+    const int nc = sim.Q * sim.Np_s;
+    std::vector<double> out((size_t)nc * L.ncell, 0.0);
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < L.ncell; ++c) {
+      if (L.status[c] == ST_NONE) continue;
+      int ijk[3];
+      L.coords(c, ijk[0], ijk[1], ijk[2]);
+      int w[3] = {ijk[0], ijk[1], ijk[2]};
+      if (!wrap(L, w)) continue;
+      long src = L.cell(w[0], w[1], w[2]);
+      if (L.status[src] == ST_VALID) {
+        for (int k = 0; k < nc; ++k) out[(size_t)k * L.ncell + c] = L.Uw[(size_t)k * L.ncell + src];
+      } else if (l > 0) {
+        std::vector<double> v(nc);
+        if (scatter_into(l, ijk, v.data()))
+          for (int k = 0; k < nc; ++k) out[(size_t)k * L.ncell + c] = v[k];
+      }
+    }
+    L.Uw.swap(out);
+  }
+
+  // average_down / amr_gather (AmrDG_Interpolater.tpp:283-342, 366-398).
+  void average_down(int lf) {
+    Level& C = sim.lev[lf - 1];
+    const Level& F = sim.lev[lf];
+    const int Ns = sim.Np_s, nov = 1 << D();
+    const Elem& el = sim.el;
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < C.ncell; ++c) {
+      if (C.status[c] != ST_VALID) continue;
+      int ijk[3];
+      C.coords(c, ijk[0], ijk[1], ijk[2]);
+      if (!covered(lf - 1, ijk)) continue;
+      for (int q = 0; q < sim.Q; ++q) {
+        std::vector<double> sum(Ns, 0.0);
+        for (int l = 0; l < nov; ++l) {
+          int f[3] = {0, 0, 0};
+          for (int d = 0; d < D(); ++d) f[d] = 2 * ijk[d] + ((l >> (D() - 1 - d)) & 1);
+          long fc = F.cell(f[0], f[1], f[2]);
+          for (int n = 0; n < Ns; ++n) {
+            double s = 0.0;
+            for (int m = 0; m < Ns; ++m) s += el.P_fc[l](n, m) * F.Uw[((size_t)q * Ns + m) * F.ncell + fc];
+            sum[n] += s;
+          }
+        }
+        for (int n = 0; n < Ns; ++n)
+          C.Uw[((size_t)q * Ns + n) * C.ncell + c] = (1.0 / nov) * (el.Minv(n, n) * sum[n]);
+      }
+    }
+  }
+
+  // ------------------------------------------------------------ C-F masks
+  // cf_mask of level l (AmrDG_Level.tpp:290-298): 1 on valid cells covered by
+  // level l+1 (periodic images included), copied from the adjacent valid
+  // cell outside a non-periodic domain, 0 elsewhere.
+  int cf_mask(int l, const int* cin) const {
+    const Level& L = sim.lev[l];
+    int c[3] = {cin[0], cin[1], cin[2]};
+    for (int d = 0; d < D(); ++d)
+      if (!sim.cfg.periodic[d]) c[d] = std::min(std::max(c[d], 0), L.n[d] - 1);
+    if (!wrap(L, c)) return 0;
+    if (L.status[L.cell(c[0], c[1], c[2])] != ST_VALID) return 0;
+    return covered(l, c) ? 1 : 0;
+  }
+
+  // cf_face_b_coarse of box b of level l at the low face of cell f along d
+  // (AmrDG_Level.tpp:300-331), with the reference's ownership rule: the low
+  // face of the box is never flagged in the box's own face array.
+  int b_coarse(int l, const Box& b, int d, const int* f) const {
+    if (f[d] == b.lo[d]) return 0;
+    int left[3] = {f[0], f[1], f[2]};
+    left[d] -= 1;
+    int ml = cf_mask(l, left), mr = cf_mask(l, f);
+    if (ml == mr) return 0;
+    return (ml == 0) ? 1 : -1;
+  }
+
+  int vmask(int l, const int* cin) const {
+    const Level& L = sim.lev[l];
+    int c[3] = {cin[0], cin[1], cin[2]};
+    for (int d = 0; d < D(); ++d)
+      if (!sim.cfg.periodic[d] && (c[d] < 0 || c[d] >= L.n[d])) return 1;
+    return valid_at(l, c) ? 1 : 0;
+  }
+
+  // cf_face_b_fine and cf_face_child_idx (AmrDG_Level.tpp:342-396).
+  int b_fine(int l, int d, const int* f, int* child) const {
+    int left[3] = {f[0], f[1], f[2]};
+    left[d] -= 1;
+    int vl = vmask(l, left), vr = vmask(l, f);
+    if (vl == vr) return 0;
+    int ci = 0, bit = 0;
+    for (int dir = 0; dir < D(); ++dir) {
+      if (dir == d) continue;
+      if (f[dir] % 2 != 0) ci |= (1 << bit);
+      bit++;
+    }
+    *child = ci;
+    return (vl == 0) ? 1 : -1;
+  }
+
+  double face_jacobian(int l, int d) const {
+    const Level& L = sim.lev[l];
+    double dvol = 1.0;
+    for (int a = 0; a < D(); ++a)
+      if (a != d) dvol *= L.dx[a];
+    return (sim.Dt / 2.0) * (dvol / std::pow(2.0, D() - 1));
+  }
+
+  // J * mat * fnum at face (lo face of cell f) of level l, into out[q*Ns+n].
+  void face_project(int l, int d, const int* f, const Mat& mat, bool mat_first, double* out) const {
+    const Level& L = sim.lev[l];
+    const long c = L.cell(f[0], f[1], f[2]);
+    const double J = face_jacobian(l, d);
+    const int Ns = sim.Np_s, qbd = sim.qbd;
+    for (int q = 0; q < sim.Q; ++q) {
+      const double* fn = &L.Fnum[(((size_t)d * sim.Q + q) * qbd) * L.ncell];
+      for (int n = 0; n < Ns; ++n) {
+        double s = 0.0;
+        for (int m = 0; m < qbd; ++m) {
+          double fv = fn[(size_t)m * L.ncell + c];
+          s += mat_first ? mat(n, m) * fv : fv * mat(n, m);
+        }
+        out[q * Ns + n] = s * J;
+      }
+    }
+  }
+
+  // ------------------------------------------------------ flux registers
+  // Register of fine level lf: per fine box, per orientation (d, side),
+  // values on the coarse faces of the coarsened box boundary.
+  struct Reg {
+    int box, d, side;
+    A::IBox cb;                  // coarsened fine box
+    std::vector<double> v;       // [tangential face][q*Ns+n]
+  };
+
+  static long tang_index(const A::IBox& cb, int D, int d, const int* f) {
+    long idx = 0, mul = 1;
+    for (int a = 0; a < D; ++a) {
+      if (a == d) continue;
+      idx += (f[a] - cb.lo[a]) * mul;
+      mul *= (cb.hi[a] - cb.lo[a] + 1);
+    }
+    return idx;
+  }
+
+  std::vector<Reg> make_regs(int lf) const {
+    std::vector<Reg> regs;
+    const int nc = sim.Q * sim.Np_s;
+    // orientation order of the reference's Reflux loop: low faces of every
+    // direction, then high faces
+    for (int side = 0; side < 2; ++side)
+      for (int d = 0; d < D(); ++d)
+        for (size_t b = 0; b < grids[lf].size(); ++b) {
+          Reg r;
+          r.box = (int)b;
+          r.d = d;
+          r.side = side;
+          r.cb = A::coarsen(grids[lf][b], D(), 2);
+          long nt = 1;
+          for (int a = 0; a < D(); ++a)
+            if (a != d) nt *= (r.cb.hi[a] - r.cb.lo[a] + 1);
+          r.v.assign((size_t)nt * nc, 0.0);
+          regs.push_back(r);
+        }
+    return regs;
+  }
+
+  // FineAdd (+1): fine C-F face fluxes summed over the coarse face.
+  void fine_add(int lf, int d, std::vector<Reg>& regs) const {
+    const int Ns = sim.Np_s, nc = sim.Q * Ns;
+    const Elem& el = sim.el;
+    for (Reg& r : regs) {
+      if (r.d != d) continue;
+      const Box b = to_boxes({grids[lf][r.box]})[0];
+      const int fface = r.side == 0 ? b.lo[d] : b.hi[d] + 1;
+      // loop over fine faces on this side
+      int lo[3] = {b.lo[0], b.lo[1], b.lo[2]}, hi[3] = {b.hi[0], b.hi[1], b.hi[2]};
+      lo[d] = hi[d] = fface;
+      for (int k = lo[2]; k <= hi[2]; ++k)
+        for (int j = lo[1]; j <= hi[1]; ++j)
+          for (int i = lo[0]; i <= hi[0]; ++i) {
+            int f[3] = {i, j, k}, child = 0;
+            int bf = b_fine(lf, d, f, &child);
+            if (bf == 0) continue;
+            const Mat& P = (bf == 1) ? el.P_flux_high[d][child] : el.P_flux_low[d][child];
+            std::vector<double> v(nc);
+            face_project(lf, d, f, P, true, v.data());
+            int cf[3] = {0, 0, 0};
+            for (int a = 0; a < D(); ++a) cf[a] = (a == d) ? fface / 2 : (f[a] >> 1);
+            long t = tang_index(r.cb, D(), d, cf);
+            for (int x = 0; x < nc; ++x) r.v[(size_t)t * nc + x] += 1.0 * v[x];
+          }
+    }
+  }
+
+  // CrseAdd (-1): coarse C-F face fluxes of every coarse box whose face array
+  // holds the face (periodic images included).
+  void crse_add(int lc, int d, std::vector<Reg>& regs) const {
+    const Level& C = sim.lev[lc];
+    const int nc = sim.Q * sim.Np_s;
+    const Elem& el = sim.el;
+    const std::vector<Box> cboxes = to_boxes(grids[lc]);
+    for (Reg& r : regs) {
+      if (r.d != d) continue;
+      const int cface = r.side == 0 ? r.cb.lo[d] : r.cb.hi[d] + 1;
+      int lo[3] = {r.cb.lo[0], r.cb.lo[1], r.cb.lo[2]}, hi[3] = {r.cb.hi[0], r.cb.hi[1], r.cb.hi[2]};
+      lo[d] = hi[d] = cface;
+      for (int k = lo[2]; k <= hi[2]; ++k)
+        for (int j = lo[1]; j <= hi[1]; ++j)
+          for (int i = lo[0]; i <= hi[0]; ++i) {
+            int f[3] = {i, j, k};
+            long t = tang_index(r.cb, D(), d, f);
+            // the face and its periodic images
+            std::vector<std::array<int, 3>> imgs = {{f[0], f[1], f[2]}};
+            if (sim.cfg.periodic[d]) {
+              if (f[d] == 0) imgs.push_back({d == 0 ? C.n[0] : f[0], d == 1 ? C.n[1] : f[1], d == 2 ? C.n[2] : f[2]});
+              if (f[d] == C.n[d]) imgs.push_back({d == 0 ? 0 : f[0], d == 1 ? 0 : f[1], d == 2 ? 0 : f[2]});
+            }
+            for (const auto& im : imgs)
+              for (const Box& cb : cboxes) {
+                bool in = true;
+                for (int a = 0; a < D(); ++a) {
+                  int lo_a = cb.lo[a], hi_a = cb.hi[a] + (a == d ? 1 : 0);
+                  if (im[a] < lo_a || im[a] > hi_a) in = false;
+                }
+                if (!in) continue;
+                int bc = b_coarse(lc, cb, d, im.data());
+                if (bc == 0) continue;
+                const Mat& M = (bc == 1) ? el.Mkbdp[d] : el.Mkbdm[d];
+                std::vector<double> v(nc);
+                face_project(lc, d, im.data(), M, false, v.data());
+                for (int x = 0; x < nc; ++x) r.v[(size_t)t * nc + x] += -1.0 * v[x];
+              }
+          }
+    }
+  }
+
+  // AMR_flux_correction: FluxRegister::Reflux into a zeroed correction
+  // array, then L2ProjInterp::reflux applies it to coarse cells flagged at
+  // a C-F face in their own box's face arrays.
+  void reflux(int lf, const std::vector<Reg>& regs) {
+    const int lc = lf - 1;
+    Level& C = sim.lev[lc];
+    const int Ns = sim.Np_s, nc = sim.Q * Ns;
+    std::map<long, std::vector<double>> corr;
+    for (const Reg& r : regs) {
+      const int d = r.d;
+      const int cface = r.side == 0 ? r.cb.lo[d] : r.cb.hi[d] + 1;
+      int lo[3] = {r.cb.lo[0], r.cb.lo[1], r.cb.lo[2]}, hi[3] = {r.cb.hi[0], r.cb.hi[1], r.cb.hi[2]};
+      lo[d] = hi[d] = cface;
+      for (int k = lo[2]; k <= hi[2]; ++k)
+        for (int j = lo[1]; j <= hi[1]; ++j)
+          for (int i = lo[0]; i <= hi[0]; ++i) {
+            int f[3] = {i, j, k};
+            long t = tang_index(r.cb, D(), d, f);
+            int cell[3] = {i, j, k};
+            if (r.side == 0) cell[d] -= 1;
+            if (!wrap(C, cell)) continue;
+            long c = C.cell(cell[0], cell[1], cell[2]);
+            if (C.status[c] != ST_VALID) continue;
+            auto& v = corr[c];
+            if (v.empty()) v.assign(nc, 0.0);
+            const double sgn = r.side == 0 ? -1.0 : 1.0;
+            for (int x = 0; x < nc; ++x) v[x] += sgn * r.v[(size_t)t * nc + x] / 1.0;
+          }
+    }
+    double vol = 1.0;
+    for (int a = 0; a < D(); ++a) vol *= C.dx[a];
+    const double inv_jac = std::pow(2.0, D()) / vol;
+    const std::vector<Box> cboxes = to_boxes(grids[lc]);
+    for (auto& kv : corr) {
+      const long c = kv.first;
+      int ijk[3];
+      C.coords(c, ijk[0], ijk[1], ijk[2]);
+      bool at_interface = false;
+      if (amr.reflux_box_quirk) {
+        for (const Box& b : cboxes) {
+          bool in = true;
+          for (int a = 0; a < D(); ++a)
+            if (ijk[a] < b.lo[a] || ijk[a] > b.hi[a]) in = false;
+          if (!in) continue;
+          for (int d = 0; d < D() && !at_interface; ++d) {
+            int lof[3] = {ijk[0], ijk[1], ijk[2]}, hif[3] = {ijk[0], ijk[1], ijk[2]};
+            hif[d] += 1;
+            if (b_coarse(lc, b, d, lof) != 0 || b_coarse(lc, b, d, hif) != 0) at_interface = true;
+          }
+          break;
+        }
+      } else {
+        at_interface = true;
+      }
+      if (!at_interface) continue;
+      for (int q = 0; q < sim.Q; ++q)
+        for (int n = 0; n < Ns; ++n) {
+          double delta = inv_jac * (sim.el.Minv(n, n) * kv.second[q * Ns + n]);
+          C.Uw[((size_t)q * Ns + n) * C.ncell + c] += delta;
+        }
+    }
+  }
+
+  // ----------------------------------------------------------------- ADER
+  void ader() {
+    const int F = finest();
+    std::vector<std::vector<Reg>> regs(F + 1);
+    for (int l = 1; l <= F; ++l) regs[l] = make_regs(l);
+    for (int l = F; l >= 0; --l) {
+      Sim& s = sim;
+      s.fill_boundary(l);
+      s.set_predictor(l);
+      for (int it = 0; it < s.P; ++it) {
+        s.get_H_from_H_w(l);
+        for (int d = 0; d < D(); ++d) s.flux_vol(l, d);
+        s.update_H_w(l);
+      }
+      s.get_H_from_H_w(l);
+      for (int d = 0; d < D(); ++d) {
+        s.flux_vol(l, d);
+        s.get_H_from_H_w_bd(l, d, 0, s.lev[l].Hm);
+        s.flux_bd(l, d, s.lev[l].Hm, s.lev[l].Fm, s.lev[l].DFm);
+        s.get_H_from_H_w_bd(l, d, 1, s.lev[l].Hp);
+        s.flux_bd(l, d, s.lev[l].Hp, s.lev[l].Fp, s.lev[l].DFp);
+        s.numflux(l, d);
+        if (F > 0) {
+          if (l < F) crse_add(l, d, regs[l + 1]);
+          if (l > 0) fine_add(l, d, regs[l]);
+        }
+      }
+      s.update_U_w(l);
+    }
+    for (int l = F; l > 0; --l) reflux(l, regs[l]);
+  }
+
+  // ---------------------------------------------------------------- tags
+  double tag_indicator(const Level& L, long c, const int* ijk) const {
+    const int Ns = sim.Np_s, Dd = D();
+    auto mean = [&](long cc, int q) { return L.Uw[((size_t)q * Ns + 0) * L.ncell + cc]; };
+    auto pres = [&](long cc) {
+      double ke = 0.0;
+      for (int d = 0; d < Dd; ++d) ke = ke + (mean(cc, d + 1) * mean(cc, d + 1)) / mean(cc, 0);
+      return (sim.cfg.gamma - 1.0) * (mean(cc, Dd + 1) - 0.5 * ke);
+    };
+    double ind = 0.0;
+    for (int d = 0; d < Dd; ++d) {
+      int a[3] = {ijk[0], ijk[1], ijk[2]}, b[3] = {ijk[0], ijk[1], ijk[2]};
+      a[d] += 1;
+      b[d] -= 1;
+      long ca = L.cell(a[0], a[1], a[2]), cb = L.cell(b[0], b[1], b[2]);
+      double v;
+      if (amr.tag_kind == 0)
+        v = std::abs(mean(ca, 0) - mean(cb, 0)) / (2.0 * mean(c, 0));
+      else
+        v = std::abs(pres(ca) - pres(cb)) / (2.0 * pres(c));
+      ind = std::max(ind, v);
+    }
+    return ind;
+  }
+
+  A::TagField compute_tags(int l) {
+    sim.fill_boundary(l);
+    const Level& L = sim.lev[l];
+    A::TagField t;
+    t.init(L.n);
+    for (long c = 0; c < L.ncell; ++c) {
+      if (L.status[c] != ST_VALID) continue;
+      int ijk[3];
+      L.coords(c, ijk[0], ijk[1], ijk[2]);
+      if (tag_indicator(L, c, ijk) > amr.tag_threshold) t.f[t.idx(ijk[0], ijk[1], ijk[2])] = 1;
+    }
+    return t;
+  }
+
+  long tags_valid(int l, int8_t* out) {
+    A::TagField t = compute_tags(l);
+    const Level& L = sim.lev[l];
+    long w = 0;
+    for (int k = 0; k < L.n[2]; ++k)
+      for (int j = 0; j < L.n[1]; ++j)
+        for (int i = 0; i < L.n[0]; ++i) {
+          if (L.status[L.cell(i, j, k)] != ST_VALID) continue;
+          out[w++] = (int8_t)t.f[t.idx(i, j, k)];
+        }
+    return w;
+  }
+
+  // --------------------------------------------------------------- regrid
+  void regrid() {
+    const int F = finest();
+    const int max_crse = std::min(F, amr.max_level - 1);
+    std::vector<A::TagField> tags(F + 1);
+    for (int l = 0; l <= max_crse; ++l) tags[l] = compute_tags(l);
+    for (int l = max_crse + 1; l <= F; ++l) tags[l].init(sim.lev[l].n);
+    std::vector<std::vector<A::IBox>> ng = A::make_new_grids(gp, grids, tags);
+    const int new_finest = (int)ng.size() - 1;
+    bool coarse_changed = false;
+    for (int l = 1; l <= new_finest; ++l) {
+      bool changed = l > F || !same_boxes(ng[l], grids[l]);
+      if (l <= F) {
+        if (changed || coarse_changed) {
+          Level old = sim.lev[l];
+          sim.define_level(l, to_boxes(ng[l]));
+          grids[l] = ng[l];
+          fill_from_coarse(l, &old);
+        }
+      } else {
+        grids.resize(l + 1);
+        grids[l] = ng[l];
+        sim.define_level(l, to_boxes(ng[l]));
+        fill_from_coarse(l, nullptr);
+      }
+      coarse_changed = changed;
+    }
+    sim.lev.resize(new_finest + 1);
+    grids.resize(new_finest + 1);
+    n_regrids++;
+  }
+
+  static bool same_boxes(const std::vector<A::IBox>& a, const std::vector<A::IBox>& b) {
+    if (a.size() != b.size()) return false;
+    for (size_t i = 0; i < a.size(); ++i)
+      for (int d = 0; d < 3; ++d)
+        if (a[i].lo[d] != b[i].lo[d] || a[i].hi[d] != b[i].hi[d]) return false;
+    return true;
+  }
+
+  // ----------------------------------------------------------------- step
   double step() {
+    if (amr.max_level > 0) {
+      bool due = first_step || (amr.dtn_regrid > 0 && sim.nstep % amr.dtn_regrid == 0);
+      if (due) regrid();
+      first_step = false;
+    }
     ader();
+    for (int l = finest(); l > 0; --l) average_down(l);
+    if (amr.max_level > 0)
+      for (int l = 0; l <= finest(); ++l) fill_patch(l);
     sim.nstep += 1;
     sim.t += sim.Dt;
     sim.Dt = sim.compute_Dt();
@@ -93,7 +693,6 @@ class AmrSim {
     return w;
   }
 
-  // Whole grown array (x fastest), element-major. which: 0 U_w, 1 H_w.
   long get_grown(int l, int which, double* out) const {
     const Level& L = sim.lev[l];
     int nc = sim.Q * (which == 0 ? sim.Np_s : sim.Np_st);
@@ -103,13 +702,12 @@ class AmrSim {
     return L.ncell;
   }
 
-  long tags_valid(int, int8_t*) const { return 0; }
-
   // ------------------------------------------------------------------ norms
-  // LpNorm_DG_AMR (AmrDG.h:1399-1655). other == nullptr: error against the
-  // analytic initial condition; otherwise against the other DG solution.
+  // LpNorm_DG_AMR (AmrDG.h:1399-1655) over leaf cells.  other == nullptr:
+  // error against the analytic initial condition; otherwise against the
+  // other solution (same layout).
   double norm(const AmrSim* other, int p, int q) const {
-    const int D = sim.D;
+    const int Dd = D();
     int N1;
     std::vector<double> pts1;
     if (p == 1) {
@@ -120,34 +718,31 @@ class AmrSim {
       pts1 = sim.l2_points_1d();
     }
     int M = 1;
-    for (int d = 0; d < D; ++d) M *= N1;
+    for (int d = 0; d < Dd; ++d) M *= N1;
     std::vector<std::array<double, 3>> qp(M);
     for (int m = 0; m < M; ++m) {
-      int rem = m;
-      int idx[3] = {0, 0, 0};
-      for (int d = D - 1; d >= 0; --d) {
+      int rem = m, idx[3] = {0, 0, 0};
+      for (int d = Dd - 1; d >= 0; --d) {
         idx[d] = rem % N1;
         rem /= N1;
       }
-      for (int d = 0; d < 3; ++d) qp[m][d] = (d < D) ? pts1[idx[d]] : 0.0;
+      for (int d = 0; d < 3; ++d) qp[m][d] = (d < Dd) ? pts1[idx[d]] : 0.0;
     }
     std::vector<double> wq(M, 1.0);
     for (int m = 0; m < M; ++m) {
       double w = 1.0;
-      for (int d = 0; d < D; ++d) w *= 2.0 / std::pow(std::assoc_legendre(N1, 1, qp[m][d]), 2);
+      for (int d = 0; d < Dd; ++d) w *= 2.0 / std::pow(std::assoc_legendre(N1, 1, qp[m][d]), 2);
       wq[m] = w;
     }
-    // basis at the points
     std::vector<double> phi((size_t)sim.Np_s * M);
     for (int n = 0; n < sim.Np_s; ++n)
       for (int m = 0; m < M; ++m) phi[(size_t)n * M + m] = sim.phi_s_at(n, qp[m].data());
-
     double total = 0.0, V_amr = 0.0;
-    for (size_t l = 0; l < sim.lev.size(); ++l) {
+    for (int l = 0; l <= finest(); ++l) {
       const Level& L = sim.lev[l];
       double vol = 1.0;
-      for (int d = 0; d < D; ++d) vol *= L.dx[d];
-      double coeff = vol / std::pow(2.0, D);
+      for (int d = 0; d < Dd; ++d) vol *= L.dx[d];
+      double coeff = vol / std::pow(2.0, Dd);
       double lev_sum = 0.0;
       long nleaf = 0;
 #pragma omp parallel for reduction(+ : lev_sum, nleaf) schedule(static)
@@ -164,19 +759,17 @@ class AmrSim {
           double u;
           if (other == nullptr) {
             double x[3] = {0, 0, 0};
-            for (int d = 0; d < D; ++d) {
+            for (int d = 0; d < Dd; ++d) {
               double xc = sim.cfg.prob_lo[d] + (ijk[d] + 0.5) * L.dx[d];
               x[d] = (L.dx[d] / 2.0) * qp[m][d] + xc;
             }
-            uint64_t cl0 = 0;
-            u = pde_IC(q, x, D, sim.cfg.gamma, sim.cfg.icp, cl0, 0);
+            u = pde_IC(q, x, Dd, sim.cfg.gamma, sim.cfg.icp, 0, 0);
           } else {
             const Level& O = other->sim.lev[l];
             u = 0.0;
             for (int n = 0; n < sim.Np_s; ++n) u += O.Uw[((size_t)q * sim.Np_s + n) * O.ncell + c] * phi[(size_t)n * M + m];
           }
-          double f = std::pow(std::abs(u - u_h), (double)p);
-          cell += f * wq[m];
+          cell += std::pow(std::abs(u - u_h), (double)p) * wq[m];
         }
         lev_sum += cell * coeff;
       }
@@ -184,15 +777,6 @@ class AmrSim {
       V_amr += vol * (double)nleaf;
     }
     return std::pow(total / V_amr, 1.0 / (double)p);
-  }
-
-  // True if cell ijk of level l is covered by a valid cell of level l+1.
-  bool covered(size_t l, const int* ijk) const {
-    if (l + 1 >= sim.lev.size()) return false;
-    const Level& F = sim.lev[l + 1];
-    int f[3];
-    for (int d = 0; d < 3; ++d) f[d] = (d < sim.D) ? 2 * ijk[d] : 0;
-    return F.status[F.cell(f[0], f[1], f[2])] == ST_VALID;
   }
 };
 

@@ -164,6 +164,13 @@ class OracleSim:
         arr = np.ascontiguousarray(arr, dtype=np.float64)
         self.L.oracle_set_uw(self.h, lev, arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
 
+    def tags(self, lev):
+        n = self.ncells_level(lev)
+        out = np.zeros(n, dtype=np.int8)
+        w = self.L.oracle_tags(self.h, lev, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)))
+        assert w == n
+        return out
+
     def norm(self, p=2, q=0, other=None):
         return self.L.oracle_norm(self.h, other.h if other is not None else None, p, q)
 
