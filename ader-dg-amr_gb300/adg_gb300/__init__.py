@@ -93,6 +93,19 @@ def lib():
         "adg_host_free": ([vp], i),
         "adg_flops_per_element": ([i, i, dp, dp], i),
         "adg_regrid_count": ([vp, ctypes.POINTER(i)], i),
+        "adg_dof_updates": ([vp, ctypes.POINTER(ctypes.c_int64), dp], i),
+        "adg_seed_create": ([i, i, i, ctypes.c_uint64, ctypes.POINTER(vp)], i),
+        "adg_seed_destroy": ([vp], i),
+        "adg_seed_collect": ([vp, vp, i], i),
+        "adg_seed_num_samples": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_seed_train": ([vp, i, i, ctypes.c_double, dp], i),
+        "adg_seed_forward": ([vp, vp, i, vp], i),
+        "adg_seed_gradients": ([vp, vp, vp, i, vp, dp], i),
+        "adg_seed_num_params": ([vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_seed_get_params": ([vp, vp], i),
+        "adg_seed_set_params": ([vp, vp], i),
+        "adg_seed_attach": ([vp, vp, i, i, ctypes.c_double], i),
+        "adg_seed_stats": ([vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)], i),
         "adg_get_boxes": ([vp, i, ctypes.POINTER(i), i, ctypes.POINTER(i)], i),
         "adg_tags": ([vp, i, ctypes.POINTER(ctypes.c_uint8)], i),
     }
@@ -322,6 +335,12 @@ class AmrDG:
         self._check(self._L.adg_time_kernels(self.ctx, int(nsteps), out, 5), "adg_time_kernels")
         return {"predictor": out[0], "numflux": out[1], "corrector": out[2], "dt": out[3], "amr_sync": out[4]}
 
+    def dof_updates(self):
+        """(total DOF updates so far, ms of host time spent in regrids)."""
+        n, ms = ctypes.c_int64(), ctypes.c_double()
+        self._check(self._L.adg_dof_updates(self.ctx, ctypes.byref(n), ctypes.byref(ms)), "adg_dof_updates")
+        return n.value, ms.value
+
     def regrid_count(self):
         n = ctypes.c_int()
         self._check(self._L.adg_regrid_count(self.ctx, ctypes.byref(n)), "adg_regrid_count")
@@ -344,6 +363,112 @@ class AmrDG:
 
     def set_stream(self, stream_handle):
         self._check(self._L.adg_set_stream(self.ctx, ctypes.c_void_p(stream_handle)), "adg_set_stream")
+
+
+class PredictorSeed:
+    """Learned predictor seed (MLP, FP32, trained on the GPU).
+
+    Inputs: the element's Q*Np_s modal coefficients and Dt/dx (standardised);
+    three hidden layers of `hidden` units with GELU; outputs the Q*Np_st
+    space-time predictor coefficients (as H_w - W U_w, standardised)."""
+
+    def __init__(self, D, P, hidden=128, rng_seed=1234):
+        self.D, self.P, self.hidden = D, P, hidden
+        self._L = lib()
+        h = ctypes.c_void_p()
+        rc = self._L.adg_seed_create(D, P, hidden, rng_seed, ctypes.byref(h))
+        if rc != ADG_OK:
+            raise AdgError(f"adg_seed_create failed ({rc})")
+        self.h = h
+        self.Q = D + 2
+        self.n_in = self.Q * comb(P + D, D) + 1
+        self.n_out = self.Q * comb(P + D + 1, D + 1)
+
+    def close(self):
+        if self.h:
+            self._L.adg_seed_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc, what):
+        if rc != ADG_OK:
+            raise AdgError(f"{what} failed ({rc})")
+
+    def collect(self, sim, target_sweeps=8):
+        self._ok(self._L.adg_seed_collect(sim.ctx, self.h, int(target_sweeps)), "adg_seed_collect")
+
+    def num_samples(self):
+        n = ctypes.c_int64()
+        self._ok(self._L.adg_seed_num_samples(self.h, ctypes.byref(n)), "adg_seed_num_samples")
+        return n.value
+
+    def train(self, epochs, batch=4096, lr=1e-3):
+        v = ctypes.c_double()
+        self._ok(self._L.adg_seed_train(self.h, int(epochs), int(batch), float(lr), ctypes.byref(v)), "adg_seed_train")
+        return v.value
+
+    def forward(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], self.n_out), dtype=np.float32)
+        self._ok(self._L.adg_seed_forward(self.h, X.ctypes.data, X.shape[0], Y.ctypes.data), "adg_seed_forward")
+        return Y
+
+    def gradients(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        nw, _ = self.num_params()
+        g = np.zeros(nw, dtype=np.float32)
+        loss = ctypes.c_double()
+        self._ok(self._L.adg_seed_gradients(self.h, X.ctypes.data, T.ctypes.data, X.shape[0], g.ctypes.data,
+                                            ctypes.byref(loss)), "adg_seed_gradients")
+        return g, loss.value
+
+    def num_params(self):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._ok(self._L.adg_seed_num_params(self.h, ctypes.byref(a), ctypes.byref(b)), "adg_seed_num_params")
+        return a.value, b.value
+
+    def get_params(self):
+        _, n = self.num_params()
+        out = np.zeros(n, dtype=np.float32)
+        self._ok(self._L.adg_seed_get_params(self.h, out.ctypes.data), "adg_seed_get_params")
+        return out
+
+    def set_params(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float32)
+        self._ok(self._L.adg_seed_set_params(self.h, v.ctypes.data), "adg_seed_set_params")
+
+    def weights(self):
+        """List of (W, b) per layer from the flat parameter vector."""
+        p = self.get_params()
+        sizes = [(self.n_in, self.hidden), (self.hidden, self.hidden), (self.hidden, self.hidden),
+                 (self.hidden, self.n_out)]
+        out, o = [], 0
+        for (a, b) in sizes:
+            W = p[o:o + a * b].reshape(a, b)
+            o += a * b
+            bias = p[o:o + b]
+            o += b
+            out.append((W, bias))
+        return out
+
+    def attach(self, sim, mode=1, sweeps=1, tol=1e-3):
+        """mode 1: seeded sweeps in FP64, 2: in FP32, 0: detach."""
+        self._ok(self._L.adg_seed_attach(sim.ctx, self.h if mode else None, int(mode), int(sweeps), float(tol)),
+                 "adg_seed_attach")
+
+
+def seed_stats(sim):
+    a, b = ctypes.c_int64(), ctypes.c_int64()
+    rc = lib().adg_seed_stats(sim.ctx, ctypes.byref(a), ctypes.byref(b))
+    if rc != ADG_OK:
+        raise AdgError("adg_seed_stats failed")
+    return a.value, b.value
 
 
 def set_device(dev):

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -13,6 +14,8 @@
 #include "adg.h"
 #include "adg_kernelset.hpp"
 #include "adg_layout.hpp"
+#include "adg_mlp.cuh"
+#include <random>
 
 namespace adg {
 
@@ -65,6 +68,34 @@ __global__ void k_fp64_probe(double* out, int iters) {
 
 using namespace adg;
 
+struct adg_seed {
+  int D = 2, P = 1, Q = 4, n_in = 0, n_out = 0, h = 128;
+  const KernelSet* ks = nullptr;
+  cudaStream_t stream = nullptr;
+  size_t off[8] = {}, sz[8] = {};
+  size_t nparam = 0;
+  DevBuf<float> params, grads, am, av;
+  DevBuf<float> x_mean, x_istd, y_mean, y_std;
+  bool normalised = false;
+  DevBuf<float> X, T;  // data set
+  long long nsamp = 0;
+  DevBuf<float> Z1, A1, Z2, A2, Z3, A3, Y, dY, dA, dZ, Xb, Tb;
+  long long work_rows = 0;
+  DevBuf<int> idx;
+  DevBuf<double> loss;
+  std::mt19937_64 rng;
+  long long adam_t = 0;
+  std::string err;
+  ~adg_seed() {
+    DevBuf<float>* bufs[] = {&params, &grads, &am, &av, &x_mean, &x_istd, &y_mean, &y_std, &X, &T,
+                             &Z1, &A1, &Z2, &A2, &Z3, &A3, &Y, &dY, &dA, &dZ, &Xb, &Tb};
+    for (auto* b : bufs) b->release();
+    idx.release();
+    loss.release();
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
 struct adg_ctx {
   adg_config cfg{};
   const KernelSet* ks = nullptr;
@@ -80,6 +111,8 @@ struct adg_ctx {
   bool initialised = false;
   bool tables_dirty = true;
   long long nstep = 0;  // completed steps (regrid schedule)
+  long long dof_updates = 0;  // sum over steps of valid elements * Q * Np_s
+  double regrid_ms = 0.0;     // host wall time spent in regrids
   bool first_step = true;
   int n_regrids = 0;
 
@@ -95,6 +128,15 @@ struct adg_ctx {
   DevBuf<int8_t> rf_dside, gf_child;
   std::vector<size_t> ad_off;  // offset (ints) of level lf's records in ad_all
   DevBuf<uint8_t> tags;
+  // learned seed
+  adg_seed* seed = nullptr;
+  int seed_mode = 0, seed_sweeps = 1;
+  double seed_tol = 1e-3;
+  DevBuf<float> sx, sy0, sy1, syo;     // features, ping-pong activations, outputs
+  DevBuf<double> hseed;
+  DevBuf<int> fb_list, fb_count;
+  DevBuf<unsigned long long> fb_total;
+  long long seed_predicted = 0;
 
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -108,6 +150,8 @@ struct adg_ctx {
     elem_level.release(); scal.release(); min_bits.release(); status.release();
     rf_elem.release(); rf_off.release(); rf_face.release(); rf_fine.release(); ad_all.release();
     gf_elem.release(); gf_parent.release(); rf_dside.release(); gf_child.release(); tags.release();
+    sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); fb_list.release(); fb_count.release();
+    fb_total.release();
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 };
@@ -155,6 +199,15 @@ int upload_tables(adg_ctx* ctx) {
   ADG_CUDA(ctx->elem_face.ensure(ne * 2 * D), "alloc elem faces");
   ADG_CUDA(ctx->elem_cell.ensure(ne * 3), "alloc elem cells");
   ADG_CUDA(ctx->elem_level.ensure(ne), "alloc elem levels");
+  if (ctx->seed) {
+    const adg_seed* sd = ctx->seed;
+    ADG_CUDA(ctx->sx.ensure(ne * sd->n_in), "alloc seed features");
+    ADG_CUDA(ctx->sy0.ensure(ne * sd->h), "alloc seed activations");
+    ADG_CUDA(ctx->sy1.ensure(ne * sd->h), "alloc seed activations");
+    ADG_CUDA(ctx->syo.ensure(ne * sd->n_out), "alloc seed outputs");
+    ADG_CUDA(ctx->hseed.ensure(ne * (size_t)ks->Q * ks->Np_st), "alloc seed H_w");
+    ADG_CUDA(ctx->fb_list.ensure(ne), "alloc fallback list");
+  }
   cudaStream_t s = ctx->stream;
   ADG_CUDA(cudaMemcpyAsync(ctx->face_left.p, H.face_left.data(), nf * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
   ADG_CUDA(cudaMemcpyAsync(ctx->face_right.p, H.face_right.data(), nf * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
@@ -196,6 +249,10 @@ int upload_tables(adg_ctx* ctx) {
   return ADG_OK;
 }
 
+}  // namespace
+int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base);
+namespace {
+
 // ADER of every level with the current device Dt (AmrDG.h:1071-1165).
 int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
   const Hierarchy& H = ctx->hier;
@@ -213,10 +270,16 @@ int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
   pa.Tr = ctx->Tr.p;
   pa.Hw_out = hw_out;
   if (ev) cudaEventRecord(ev[0], ctx->stream);
-  cudaError_t e = ks->predictor(pa, ctx->E, ctx->stream);
+  cudaError_t e = cudaSuccess;
+  if (ctx->seed_mode && ctx->seed) {
+    int rc = launch_seeded_predictor(ctx, pa);
+    if (rc) return rc;
+  } else {
+    e = ks->predictor(pa, ctx->E, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "predictor launch");
+    ctx->launches++;
+  }
   if (ev) cudaEventRecord(ev[1], ctx->stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "predictor launch");
-  ctx->launches++;
 
   FaceArgs fa{};
   fa.Tr = ctx->Tr.p;
@@ -463,9 +526,12 @@ int capture_graph(adg_ctx* ctx) {
 
 int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
   if (regrid_due(ctx)) {
+    auto t0 = std::chrono::steady_clock::now();
     int rc = regrid(ctx);
     if (rc) return rc;
+    ctx->regrid_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
+  ctx->dof_updates += (long long)ctx->hier.n_valid() * ctx->ks->Q * ctx->ks->Np_s;
   ctx->first_step = false;
   if (use_graph && !ev) {
     if (!ctx->graph_exec) {
@@ -748,6 +814,13 @@ int adg_advance(adg_ctx* ctx, int nsteps, int use_graph) {
   return ADG_OK;
 }
 
+int adg_dof_updates(const adg_ctx* ctx, int64_t* total, double* regrid_ms) {
+  if (!ctx || !total) return ADG_ERR_ARG;
+  *total = ctx->dof_updates;
+  if (regrid_ms) *regrid_ms = ctx->regrid_ms;
+  return ADG_OK;
+}
+
 int adg_regrid_count(const adg_ctx* ctx, int* n) {
   if (!ctx || !n) return ADG_ERR_ARG;
   *n = ctx->n_regrids;
@@ -936,6 +1009,455 @@ int adg_flops_per_element(int D, int P, double* algorithmic, double* issued) {
   const double Fc = 2 * Q * qst * Npst + 2 * D * 2 * Q * qbd * Npst + 2 * Q * (D * Nps * qst + 2 * D * Nps * qbd) + 2 * Q * Nps;
   if (algorithmic) *algorithmic = Fp + Fc;
   if (issued) *issued = Q * (double)ks->linear_fp64_per_column;
+  return ADG_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Learned predictor seed: network, training, inference inside the step.
+// ===========================================================================
+namespace {
+
+void sgemm(int TA, int TB, int M, int N, int K, const float* A, const float* B, float* C, const float* bias,
+           float* aux, int epi, cudaStream_t st) {
+  dim3 grid((N + 63) / 64, (M + 63) / 64);
+  if (!TA && !TB) mlp::k_sgemm<0, 0><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
+  else if (TA && !TB) mlp::k_sgemm<1, 0><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
+  else if (!TA && TB) mlp::k_sgemm<0, 1><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
+  else mlp::k_sgemm<1, 1><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
+}
+
+float* P(adg_seed* s, int k) { return s->params.p + s->off[k]; }
+float* G(adg_seed* s, int k) { return s->grads.p + s->off[k]; }
+
+cudaError_t seed_work(adg_seed* s, long long rows) {
+  if (rows <= s->work_rows) return cudaSuccess;
+  const size_t h = s->h;
+  DevBuf<float>* hb[] = {&s->Z1, &s->A1, &s->Z2, &s->A2, &s->Z3, &s->A3, &s->dA, &s->dZ};
+  for (auto* b : hb) {
+    cudaError_t e = b->ensure((size_t)rows * h);
+    if (e != cudaSuccess) return e;
+  }
+  cudaError_t e = s->Y.ensure((size_t)rows * s->n_out);
+  if (e == cudaSuccess) e = s->dY.ensure((size_t)rows * s->n_out);
+  if (e == cudaSuccess) e = s->Xb.ensure((size_t)rows * s->n_in);
+  if (e == cudaSuccess) e = s->Tb.ensure((size_t)rows * s->n_out);
+  if (e == cudaSuccess) s->work_rows = rows;
+  return e;
+}
+
+// Forward with stored pre-activations (training).
+void seed_forward_train(adg_seed* s, const float* X, int B, cudaStream_t st) {
+  using namespace mlp;
+  sgemm(0, 0, B, s->h, s->n_in, X, P(s, 0), s->A1.p, P(s, 1), s->Z1.p, EPI_BIAS_GELU, st);
+  sgemm(0, 0, B, s->h, s->h, s->A1.p, P(s, 2), s->A2.p, P(s, 3), s->Z2.p, EPI_BIAS_GELU, st);
+  sgemm(0, 0, B, s->h, s->h, s->A2.p, P(s, 4), s->A3.p, P(s, 5), s->Z3.p, EPI_BIAS_GELU, st);
+  sgemm(0, 0, B, s->n_out, s->h, s->A3.p, P(s, 6), s->Y.p, P(s, 7), nullptr, EPI_BIAS, st);
+}
+
+// Backward from dY (in s->dY) into s->grads.
+void seed_backward(adg_seed* s, const float* X, int B, cudaStream_t st) {
+  using namespace mlp;
+  const int h = s->h;
+  sgemm(1, 0, h, s->n_out, B, s->A3.p, s->dY.p, G(s, 6), nullptr, nullptr, EPI_STORE, st);
+  k_colsum<<<(s->n_out + 127) / 128, 128, 0, st>>>(B, s->n_out, s->dY.p, G(s, 7));
+  sgemm(0, 1, B, h, s->n_out, s->dY.p, P(s, 6), s->dZ.p, nullptr, s->Z3.p, EPI_GELU_BWD, st);  // dZ3
+  sgemm(1, 0, h, h, B, s->A2.p, s->dZ.p, G(s, 4), nullptr, nullptr, EPI_STORE, st);
+  k_colsum<<<(h + 127) / 128, 128, 0, st>>>(B, h, s->dZ.p, G(s, 5));
+  sgemm(0, 1, B, h, h, s->dZ.p, P(s, 4), s->dA.p, nullptr, s->Z2.p, EPI_GELU_BWD, st);  // dZ2
+  sgemm(1, 0, h, h, B, s->A1.p, s->dA.p, G(s, 2), nullptr, nullptr, EPI_STORE, st);
+  k_colsum<<<(h + 127) / 128, 128, 0, st>>>(B, h, s->dA.p, G(s, 3));
+  sgemm(0, 1, B, h, h, s->dA.p, P(s, 2), s->dZ.p, nullptr, s->Z1.p, EPI_GELU_BWD, st);  // dZ1
+  sgemm(1, 0, s->n_in, h, B, X, s->dZ.p, G(s, 0), nullptr, nullptr, EPI_STORE, st);
+  k_colsum<<<(h + 127) / 128, 128, 0, st>>>(B, h, s->dZ.p, G(s, 1));
+}
+
+// Inference with ping-pong activations a0, a1 (rows x h each).
+void seed_forward_infer(adg_seed* s, const float* X, int B, float* a0, float* a1, float* Y, cudaStream_t st) {
+  using namespace mlp;
+  sgemm(0, 0, B, s->h, s->n_in, X, P(s, 0), a0, P(s, 1), nullptr, EPI_BIAS_GELU, st);
+  sgemm(0, 0, B, s->h, s->h, a0, P(s, 2), a1, P(s, 3), nullptr, EPI_BIAS_GELU, st);
+  sgemm(0, 0, B, s->h, s->h, a1, P(s, 4), a0, P(s, 5), nullptr, EPI_BIAS_GELU, st);
+  sgemm(0, 0, B, s->n_out, s->h, a0, P(s, 6), Y, P(s, 7), nullptr, EPI_BIAS, st);
+}
+
+cudaError_t grow_rows(DevBuf<float>& b, size_t keep, size_t need) {
+  if (need <= b.n) return cudaSuccess;
+  DevBuf<float> nb;
+  cudaError_t e = nb.ensure(std::max(need, b.n * 2));
+  if (e != cudaSuccess) return e;
+  if (keep) e = cudaMemcpy(nb.p, b.p, keep * sizeof(float), cudaMemcpyDeviceToDevice);
+  b.release();
+  b = nb;
+  nb.p = nullptr;
+  nb.n = 0;
+  return e;
+}
+
+__global__ void k_accumulate_count(const int* c, unsigned long long* total) {
+  if (threadIdx.x == 0) *total += (unsigned long long)*c;
+}
+
+}  // namespace
+
+// Seeded predictor: network inference, seeded sweeps with residual test,
+// fallback of rejected elements to the full Picard predictor.
+int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base) {
+  adg_seed* sd = ctx->seed;
+  const Hierarchy& H = ctx->hier;
+  const KernelSet* ks = ctx->ks;
+  const int n = (int)H.n_elem();
+  cudaStream_t st = ctx->stream;
+  SeedFeatArgs fa{};
+  fa.Uw = ctx->Uw.p;
+  fa.e0 = 0;
+  fa.n = n;
+  fa.elem_level = H.nlevels() > 1 ? ctx->elem_level.p : nullptr;
+  fa.geom = base.geom;
+  fa.dt = ctx->scal.p;
+  fa.x_mean = sd->x_mean.p;
+  fa.x_istd = sd->x_istd.p;
+  fa.X = ctx->sx.p;
+  cudaError_t e = ks->seed_features(fa, st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "seed features");
+  seed_forward_infer(sd, ctx->sx.p, n, ctx->sy0.p, ctx->sy1.p, ctx->syo.p, st);
+  e = ks->seed_assemble(ctx->Uw.p, ctx->syo.p, sd->y_mean.p, sd->y_std.p, n, fa.elem_level, base.geom, ctx->scal.p,
+                       ctx->hseed.p, st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "seed assemble");
+  ADG_CUDA(cudaMemsetAsync(ctx->fb_count.p, 0, sizeof(int), st), "fallback reset");
+  PredictorArgs pa = base;
+  pa.Hseed = ctx->hseed.p;
+  pa.seed_tol = ctx->seed_tol;
+  pa.fb_list = ctx->fb_list.p;
+  pa.fb_count = ctx->fb_count.p;
+  pa.sweeps = ctx->seed_sweeps;
+  e = ks->predictor(pa, ctx->E, st, ctx->seed_mode);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "seeded predictor");
+  PredictorArgs fb = base;  // full FP64 Picard for the rejected elements
+  fb.elem_list = ctx->fb_list.p;
+  fb.list_count = ctx->fb_count.p;
+  e = ks->predictor(fb, ctx->E, st, 0);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "fallback predictor");
+  k_accumulate_count<<<1, 32, 0, st>>>(ctx->fb_count.p, ctx->fb_total.p);
+  ctx->launches += 4 + 4 + 1;  // features, 4 GEMMs, assemble, 2 predictors, count
+  ctx->seed_predicted += n;
+  return ADG_OK;
+}
+
+extern "C" {
+
+int adg_seed_create(int D, int P, int hidden, uint64_t rng_seed, adg_seed** out) {
+  if (!out) return ADG_ERR_ARG;
+  *out = nullptr;
+  const KernelSet* ks = kernel_set(D, P);
+  if (!ks || hidden <= 0 || hidden > 4096) return ADG_ERR_ARG;
+  adg_seed* s = new adg_seed();
+  s->D = D;
+  s->P = P;
+  s->Q = ks->Q;
+  s->ks = ks;
+  s->h = hidden;
+  s->n_in = ks->Q * ks->Np_s + 1;
+  s->n_out = ks->Q * ks->Np_st;
+  const size_t h = hidden;
+  const size_t sizes[8] = {(size_t)s->n_in * h, h, h * h, h, h * h, h, h * s->n_out, (size_t)s->n_out};
+  size_t o = 0;
+  for (int k = 0; k < 8; ++k) {
+    s->off[k] = o;
+    s->sz[k] = sizes[k];
+    o += sizes[k];
+  }
+  s->nparam = o;
+  s->rng.seed(rng_seed);
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      s->params.ensure(o) != cudaSuccess || s->grads.ensure(o) != cudaSuccess || s->am.ensure(o) != cudaSuccess ||
+      s->av.ensure(o) != cudaSuccess || s->x_mean.ensure(s->n_in) != cudaSuccess ||
+      s->x_istd.ensure(s->n_in) != cudaSuccess || s->y_mean.ensure(s->n_out) != cudaSuccess ||
+      s->y_std.ensure(s->n_out) != cudaSuccess || s->loss.ensure(1) != cudaSuccess) {
+    delete s;
+    return ADG_ERR_CUDA;
+  }
+  // Glorot-uniform weights, zero biases, identity standardisation
+  std::vector<float> hp(o, 0.0f);
+  const int fin[4] = {s->n_in, hidden, hidden, hidden}, fout[4] = {hidden, hidden, hidden, s->n_out};
+  for (int L = 0; L < 4; ++L) {
+    const double a = std::sqrt(6.0 / (fin[L] + fout[L]));
+    std::uniform_real_distribution<double> U(-a, a);
+    for (size_t i = 0; i < sizes[2 * L]; ++i) hp[s->off[2 * L] + i] = (float)U(s->rng);
+  }
+  std::vector<float> zin(s->n_in, 0.f), oin(s->n_in, 1.f), zout(s->n_out, 0.f), oout(s->n_out, 1.f);
+  cudaMemcpy(s->params.p, hp.data(), o * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemset(s->am.p, 0, o * sizeof(float));
+  cudaMemset(s->av.p, 0, o * sizeof(float));
+  cudaMemcpy(s->x_mean.p, zin.data(), zin.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->x_istd.p, oin.data(), oin.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->y_mean.p, zout.data(), zout.size() * 4, cudaMemcpyHostToDevice);
+  if (cudaMemcpy(s->y_std.p, oout.data(), oout.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+    delete s;
+    return ADG_ERR_CUDA;
+  }
+  *out = s;
+  return ADG_OK;
+}
+
+int adg_seed_destroy(adg_seed* s) {
+  if (!s) return ADG_ERR_ARG;
+  cudaDeviceSynchronize();
+  delete s;
+  return ADG_OK;
+}
+
+int adg_seed_num_samples(const adg_seed* s, int64_t* n) {
+  if (!s || !n) return ADG_ERR_ARG;
+  *n = s->nsamp;
+  return ADG_OK;
+}
+
+int adg_seed_collect(adg_ctx* ctx, adg_seed* s, int target_sweeps) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!s || s->D != ctx->cfg.D || s->P != ctx->cfg.P || target_sweeps < 1) return fail(ctx, ADG_ERR_ARG, "bad seed");
+  if (s->normalised) return fail(ctx, ADG_ERR_STATE, "data set already standardised by training");
+  const Hierarchy& H = ctx->hier;
+  const KernelSet* ks = ctx->ks;
+  const size_t nv = H.n_valid();
+  ADG_CUDA(ctx->Hw_dbg.ensure(H.n_elem() * (size_t)ks->Q * ks->Np_st), "alloc Hw");
+  DevBuf<double> save;
+  ADG_CUDA(save.ensure(ctx->Uw.n), "alloc save");
+  ADG_CUDA(cudaMemcpyAsync(save.p, ctx->Uw.p, ctx->Uw.n * 8, cudaMemcpyDeviceToDevice, ctx->stream), "save");
+  const int sw = ctx->sweeps, mode = ctx->seed_mode;
+  ctx->sweeps = target_sweeps;
+  ctx->seed_mode = 0;
+  rc = launch_ader(ctx, ctx->Hw_dbg.p);
+  ctx->sweeps = sw;
+  ctx->seed_mode = mode;
+  if (rc) {
+    save.release();
+    return rc;
+  }
+  ADG_CUDA(cudaMemcpyAsync(ctx->Uw.p, save.p, ctx->Uw.n * 8, cudaMemcpyDeviceToDevice, ctx->stream), "restore");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "collect sync");
+  save.release();
+  ADG_CUDA(grow_rows(s->X, (size_t)s->nsamp * s->n_in, (s->nsamp + nv) * (size_t)s->n_in), "grow X");
+  ADG_CUDA(grow_rows(s->T, (size_t)s->nsamp * s->n_out, (s->nsamp + nv) * (size_t)s->n_out), "grow T");
+  SeedFeatArgs fa{};
+  fa.Uw = ctx->Uw.p;
+  fa.Hw = ctx->Hw_dbg.p;
+  fa.e0 = 0;
+  fa.n = (int)nv;
+  fa.elem_level = H.nlevels() > 1 ? ctx->elem_level.p : nullptr;
+  fa.geom = level_geom(ctx);
+  fa.dt = ctx->scal.p;
+  fa.X = s->X.p + (size_t)s->nsamp * s->n_in;
+  fa.T = s->T.p + (size_t)s->nsamp * s->n_out;
+  cudaError_t e = ks->seed_features(fa, ctx->stream);
+  if (e == cudaSuccess) e = ks->seed_targets(fa, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "collect kernels");
+  ctx->launches += 2;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "collect sync");
+  s->nsamp += (long long)nv;
+  return ADG_OK;
+}
+
+static int seed_normalise(adg_seed* s) {
+  const long long M = s->nsamp;
+  auto moments = [&](DevBuf<float>& X, int F, std::vector<double>& mean, std::vector<double>& sd) -> cudaError_t {
+    DevBuf<double> acc;
+    cudaError_t e = acc.ensure(2 * (size_t)F);
+    if (e != cudaSuccess) return e;
+    cudaMemsetAsync(acc.p, 0, 2 * F * sizeof(double), s->stream);
+    dim3 grid(64, F);
+    mlp::k_col_moments<<<grid, 256, 0, s->stream>>>(M, F, X.p, acc.p, acc.p + F);
+    std::vector<double> h(2 * F);
+    e = cudaMemcpyAsync(h.data(), acc.p, 2 * F * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    acc.release();
+    mean.resize(F);
+    sd.resize(F);
+    for (int f = 0; f < F; ++f) {
+      mean[f] = h[f] / M;
+      const double var = std::max(0.0, h[F + f] / M - mean[f] * mean[f]);
+      sd[f] = std::sqrt(var);
+    }
+    return e;
+  };
+  std::vector<double> xm, xs, ym, ys;
+  if (moments(s->X, s->n_in, xm, xs) != cudaSuccess || moments(s->T, s->n_out, ym, ys) != cudaSuccess) return ADG_ERR_CUDA;
+  std::vector<float> fxm(s->n_in), fxi(s->n_in), fym(s->n_out), fys(s->n_out), fyi(s->n_out);
+  // Feature scale: the spread in the data, floored at 10 % of the feature's
+  // mean magnitude so a nearly constant feature (Dt/dx within one run, a
+  // mode that is almost zero) does not turn small changes into large inputs.
+  double xmax = 0.0;
+  for (int f = 0; f < s->n_in; ++f) xmax = std::max(xmax, std::abs(xm[f]) + xs[f]);
+  for (int f = 0; f < s->n_in; ++f) {
+    fxm[f] = (float)xm[f];
+    const double sc = std::max({xs[f], 0.1 * std::abs(xm[f]), 1e-6 * xmax, 1e-30});
+    fxi[f] = (float)(1.0 / sc);
+  }
+  for (int f = 0; f < s->n_out; ++f) {
+    fym[f] = (float)ym[f];
+    const double sd = ys[f] > 1e-30 ? ys[f] : 1.0;
+    fys[f] = (float)sd;
+    fyi[f] = (float)(1.0 / sd);
+  }
+  DevBuf<float> yi;
+  if (yi.ensure(s->n_out) != cudaSuccess) return ADG_ERR_CUDA;
+  cudaMemcpy(s->x_mean.p, fxm.data(), s->n_in * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->x_istd.p, fxi.data(), s->n_in * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->y_mean.p, fym.data(), s->n_out * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->y_std.p, fys.data(), s->n_out * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(yi.p, fyi.data(), s->n_out * 4, cudaMemcpyHostToDevice);
+  mlp::k_standardise<<<(unsigned)((M * s->n_in + 255) / 256), 256, 0, s->stream>>>(M, s->n_in, s->X.p, s->x_mean.p,
+                                                                                     s->x_istd.p);
+  mlp::k_standardise<<<(unsigned)((M * s->n_out + 255) / 256), 256, 0, s->stream>>>(M, s->n_out, s->T.p, s->y_mean.p,
+                                                                                      yi.p);
+  cudaError_t e = cudaStreamSynchronize(s->stream);
+  yi.release();
+  if (e != cudaSuccess) return ADG_ERR_CUDA;
+  s->normalised = true;
+  return ADG_OK;
+}
+
+int adg_seed_train(adg_seed* s, int epochs, int batch, double lr, double* last_loss) {
+  if (!s || epochs < 0 || batch <= 0 || !(lr > 0)) return ADG_ERR_ARG;
+  if (s->nsamp <= 0) return ADG_ERR_STATE;
+  if (!s->normalised) {
+    int rc = seed_normalise(s);
+    if (rc) return rc;
+  }
+  if (seed_work(s, batch) != cudaSuccess || s->idx.ensure(s->nsamp) != cudaSuccess) return ADG_ERR_CUDA;
+  std::vector<int> perm(s->nsamp);
+  for (long long i = 0; i < s->nsamp; ++i) perm[i] = (int)i;
+  double epoch_loss = 0.0;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  for (int ep = 0; ep < epochs; ++ep) {
+    std::shuffle(perm.begin(), perm.end(), s->rng);
+    cudaMemcpyAsync(s->idx.p, perm.data(), perm.size() * 4, cudaMemcpyHostToDevice, s->stream);
+    cudaMemsetAsync(s->loss.p, 0, sizeof(double), s->stream);
+    for (long long b0 = 0; b0 < s->nsamp; b0 += batch) {
+      const int B = (int)std::min<long long>(batch, s->nsamp - b0);
+      mlp::k_gather_rows<<<(unsigned)(((long long)B * s->n_in + 255) / 256), 256, 0, s->stream>>>(
+          B, s->n_in, s->idx.p + b0, s->X.p, s->Xb.p);
+      mlp::k_gather_rows<<<(unsigned)(((long long)B * s->n_out + 255) / 256), 256, 0, s->stream>>>(
+          B, s->n_out, s->idx.p + b0, s->T.p, s->Tb.p);
+      seed_forward_train(s, s->Xb.p, B, s->stream);
+      mlp::k_mse_grad<<<(unsigned)(((long long)B * s->n_out + 255) / 256), 256, 0, s->stream>>>(
+          B, s->n_out, s->Y.p, s->Tb.p, s->dY.p, s->loss.p);
+      seed_backward(s, s->Xb.p, B, s->stream);
+      s->adam_t++;
+      const float bc1 = 1.f - (float)std::pow(b1, (double)s->adam_t), bc2 = 1.f - (float)std::pow(b2, (double)s->adam_t);
+      mlp::k_adam<<<(unsigned)((s->nparam + 255) / 256), 256, 0, s->stream>>>((int)s->nparam, s->params.p, s->grads.p,
+                                                                              s->am.p, s->av.p, (float)lr, b1, b2, eps,
+                                                                              bc1, bc2);
+    }
+    double l = 0.0;
+    cudaMemcpyAsync(&l, s->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return ADG_ERR_CUDA;
+    epoch_loss = l / ((double)s->nsamp * s->n_out);
+  }
+  if (last_loss) *last_loss = epoch_loss;
+  return ADG_OK;
+}
+
+int adg_seed_forward(adg_seed* s, const float* X, int n, float* Y) {
+  if (!s || !X || !Y || n <= 0) return ADG_ERR_ARG;
+  DevBuf<float> dx, a0, a1, dy;
+  if (dx.ensure((size_t)n * s->n_in) != cudaSuccess || a0.ensure((size_t)n * s->h) != cudaSuccess ||
+      a1.ensure((size_t)n * s->h) != cudaSuccess || dy.ensure((size_t)n * s->n_out) != cudaSuccess)
+    return ADG_ERR_CUDA;
+  cudaMemcpyAsync(dx.p, X, (size_t)n * s->n_in * 4, cudaMemcpyHostToDevice, s->stream);
+  seed_forward_infer(s, dx.p, n, a0.p, a1.p, dy.p, s->stream);
+  cudaMemcpyAsync(Y, dy.p, (size_t)n * s->n_out * 4, cudaMemcpyDeviceToHost, s->stream);
+  cudaError_t e = cudaStreamSynchronize(s->stream);
+  dx.release(); a0.release(); a1.release(); dy.release();
+  return e == cudaSuccess ? ADG_OK : ADG_ERR_CUDA;
+}
+
+int adg_seed_gradients(adg_seed* s, const float* X, const float* T, int n, float* grads, double* loss) {
+  if (!s || !X || !T || !grads || n <= 0) return ADG_ERR_ARG;
+  if (seed_work(s, n) != cudaSuccess) return ADG_ERR_CUDA;
+  cudaMemcpyAsync(s->Xb.p, X, (size_t)n * s->n_in * 4, cudaMemcpyHostToDevice, s->stream);
+  cudaMemcpyAsync(s->Tb.p, T, (size_t)n * s->n_out * 4, cudaMemcpyHostToDevice, s->stream);
+  cudaMemsetAsync(s->loss.p, 0, sizeof(double), s->stream);
+  seed_forward_train(s, s->Xb.p, n, s->stream);
+  mlp::k_mse_grad<<<(unsigned)(((long long)n * s->n_out + 255) / 256), 256, 0, s->stream>>>(n, s->n_out, s->Y.p,
+                                                                                          s->Tb.p, s->dY.p, s->loss.p);
+  seed_backward(s, s->Xb.p, n, s->stream);
+  double l = 0.0;
+  cudaMemcpyAsync(&l, s->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+  cudaMemcpyAsync(grads, s->grads.p, s->nparam * 4, cudaMemcpyDeviceToHost, s->stream);
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return ADG_ERR_CUDA;
+  if (loss) *loss = l / ((double)n * s->n_out);
+  return ADG_OK;
+}
+
+int adg_seed_num_params(const adg_seed* s, int64_t* n_weights, int64_t* n_total) {
+  if (!s) return ADG_ERR_ARG;
+  if (n_weights) *n_weights = (int64_t)s->nparam;
+  if (n_total) *n_total = (int64_t)(s->nparam + 2 * s->n_in + 2 * s->n_out);
+  return ADG_OK;
+}
+
+int adg_seed_get_params(adg_seed* s, float* out) {
+  if (!s || !out) return ADG_ERR_ARG;
+  size_t o = 0;
+  cudaMemcpy(out, s->params.p, s->nparam * 4, cudaMemcpyDeviceToHost);
+  o += s->nparam;
+  cudaMemcpy(out + o, s->x_mean.p, s->n_in * 4, cudaMemcpyDeviceToHost);
+  o += s->n_in;
+  cudaMemcpy(out + o, s->x_istd.p, s->n_in * 4, cudaMemcpyDeviceToHost);
+  o += s->n_in;
+  cudaMemcpy(out + o, s->y_mean.p, s->n_out * 4, cudaMemcpyDeviceToHost);
+  o += s->n_out;
+  return cudaMemcpy(out + o, s->y_std.p, s->n_out * 4, cudaMemcpyDeviceToHost) == cudaSuccess ? ADG_OK : ADG_ERR_CUDA;
+}
+
+int adg_seed_set_params(adg_seed* s, const float* in) {
+  if (!s || !in) return ADG_ERR_ARG;
+  size_t o = 0;
+  cudaMemcpy(s->params.p, in, s->nparam * 4, cudaMemcpyHostToDevice);
+  o += s->nparam;
+  cudaMemcpy(s->x_mean.p, in + o, s->n_in * 4, cudaMemcpyHostToDevice);
+  o += s->n_in;
+  cudaMemcpy(s->x_istd.p, in + o, s->n_in * 4, cudaMemcpyHostToDevice);
+  o += s->n_in;
+  cudaMemcpy(s->y_mean.p, in + o, s->n_out * 4, cudaMemcpyHostToDevice);
+  o += s->n_out;
+  s->normalised = true;
+  return cudaMemcpy(s->y_std.p, in + o, s->n_out * 4, cudaMemcpyHostToDevice) == cudaSuccess ? ADG_OK : ADG_ERR_CUDA;
+}
+
+int adg_seed_attach(adg_ctx* ctx, adg_seed* s, int mode, int sweeps, double tol) {
+  if (!ctx) return ADG_ERR_ARG;
+  if (mode == 0 || !s) {
+    ctx->seed = nullptr;
+    ctx->seed_mode = 0;
+  } else {
+    if (s->D != ctx->cfg.D || s->P != ctx->cfg.P || mode < 1 || mode > 2 || sweeps < 0 || !(tol > 0))
+      return fail(ctx, ADG_ERR_ARG, "bad seed attach arguments");
+    ctx->seed = s;
+    ctx->seed_mode = mode;
+    ctx->seed_sweeps = sweeps;
+    ctx->seed_tol = tol;
+    ADG_CUDA(ctx->fb_count.ensure(1), "alloc");
+    ADG_CUDA(ctx->fb_total.ensure(1), "alloc");
+    ADG_CUDA(cudaMemset(ctx->fb_total.p, 0, sizeof(unsigned long long)), "reset");
+    ctx->seed_predicted = 0;
+  }
+  ctx->tables_dirty = true;  // resizes the inference buffers, drops the graph
+  return ADG_OK;
+}
+
+int adg_seed_stats(adg_ctx* ctx, int64_t* fallbacks, int64_t* predicted) {
+  if (!ctx) return ADG_ERR_ARG;
+  unsigned long long t = 0;
+  if (ctx->fb_total.p) {
+    ADG_CUDA(cudaMemcpyAsync(&t, ctx->fb_total.p, sizeof(t), cudaMemcpyDeviceToHost, ctx->stream), "stats");
+    ADG_CUDA(cudaStreamSynchronize(ctx->stream), "stats sync");
+  }
+  if (fallbacks) *fallbacks = (int64_t)t;
+  if (predicted) *predicted = (int64_t)ctx->seed_predicted;
   return ADG_OK;
 }
 

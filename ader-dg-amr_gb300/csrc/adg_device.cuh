@@ -10,24 +10,32 @@ namespace adg {
 // Operand accessors: the generated operators are written against these, so
 // the same code reads registers (stride 1, compile-time indices) or a shared
 // memory column (runtime stride).
-struct RegIn {
-  const double* p;
-  __device__ __forceinline__ double operator()(int i) const { return p[i]; }
+template <class T>
+struct RegInT {
+  const T* p;
+  __device__ __forceinline__ T operator()(int i) const { return p[i]; }
 };
-struct RegOut {
-  double* p;
-  __device__ __forceinline__ double& operator()(int i) const { return p[i]; }
+template <class T>
+struct RegOutT {
+  T* p;
+  __device__ __forceinline__ T& operator()(int i) const { return p[i]; }
 };
-struct ColIn {
-  const double* p;
+template <class T>
+struct ColInT {
+  const T* p;
   int s;
-  __device__ __forceinline__ double operator()(int i) const { return p[i * s]; }
+  __device__ __forceinline__ T operator()(int i) const { return p[i * s]; }
 };
-struct ColOut {
-  double* p;
+template <class T>
+struct ColOutT {
+  T* p;
   int s;
-  __device__ __forceinline__ double& operator()(int i) const { return p[i * s]; }
+  __device__ __forceinline__ T& operator()(int i) const { return p[i * s]; }
 };
+using RegIn = RegInT<double>;
+using RegOut = RegOutT<double>;
+using ColIn = ColInT<double>;
+using ColOut = ColOutT<double>;
 
 // Pressure floor of the reference model: 10 * machine epsilon
 // (Source/Model/CompressibleEuler/Compressible_Euler.cpp:50-55).
@@ -44,18 +52,19 @@ __device__ __forceinline__ double floor_limit(double p) { return (p < kPdeLimit)
 // Physical flux of the compressible Euler equations in every direction at one
 // point (Compressible_Euler.h:370-487; pressure Compressible_Euler.h:562-589).
 // u: Q = D+2 conserved variables; F[d*Q + q].
-template <int D>
-__device__ __forceinline__ void euler_flux_all(const double* u, double gm1, double* F) {
+template <int D, class T = double>
+__device__ __forceinline__ void euler_flux_all(const T* u, T gm1, T* F) {
   constexpr int Q = D + 2;
-  const double r = 1.0 / u[0];
-  double v[D];
+  const T r = T(1) / u[0];
+  T v[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) v[d] = u[d + 1] * r;
-  double ke = u[1] * v[0];
+  T ke = u[1] * v[0];
 #pragma unroll
   for (int d = 1; d < D; ++d) ke = fma(u[d + 1], v[d], ke);
-  const double p = floor_limit(gm1 * fma(-0.5, ke, u[D + 1]));
-  const double ep = u[D + 1] + p;
+  T p = gm1 * fma(T(-0.5), ke, u[D + 1]);
+  p = (p < T(kPdeLimit)) ? T(kPdeLimit) : p;
+  const T ep = u[D + 1] + p;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     F[d * Q + 0] = u[d + 1];

@@ -15,18 +15,25 @@ constexpr size_t smem_bytes() {
   return (size_t)(a > b ? a : b) * (E * O::Q + 1) * sizeof(double);
 }
 
-template <int E>
-cudaError_t launch_predictor(const PredictorArgs& a, cudaStream_t s) {
+template <int E, int MODE>
+cudaError_t launch_predictor_mode(const PredictorArgs& a, cudaStream_t s) {
   constexpr size_t smem = smem_bytes<E>();
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_predictor<O, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_predictor<O, E, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr = true;
   }
   const int grid = (a.n_elem + E - 1) / E;
-  k_predictor<O, E><<<grid, E * O::Q, smem, s>>>(a);
+  k_predictor<O, E, MODE><<<grid, E * O::Q, smem, s>>>(a);
   return cudaGetLastError();
+}
+
+template <int E>
+cudaError_t launch_predictor(const PredictorArgs& a, cudaStream_t s, int mode) {
+  if (mode == 1) return launch_predictor_mode<E, 1>(a, s);
+  if (mode == 2) return launch_predictor_mode<E, 2>(a, s);
+  return launch_predictor_mode<E, 0>(a, s);
 }
 
 struct Impl final : KernelSet {
@@ -46,20 +53,20 @@ struct Impl final : KernelSet {
   size_t predictor_smem(int E) const override {
     return E == 8 ? smem_bytes<8>() : E == 16 ? smem_bytes<16>() : smem_bytes<32>();
   }
-  cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s) const override {
-    if (E == 8) return launch_predictor<8>(a, s);
-    if (E == 16) return launch_predictor<16>(a, s);
-    return launch_predictor<32>(a, s);
+  cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s, int mode) const override {
+    if (E == 8) return launch_predictor<8>(a, s, mode);
+    if (E == 16) return launch_predictor<16>(a, s, mode);
+    return launch_predictor<32>(a, s, mode);
   }
 #else
   std::vector<int> elems_per_block_choices() const override { return {4, 8, 16}; }
   size_t predictor_smem(int E) const override {
     return E == 4 ? smem_bytes<4>() : E == 8 ? smem_bytes<8>() : smem_bytes<16>();
   }
-  cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s) const override {
-    if (E == 4) return launch_predictor<4>(a, s);
-    if (E == 8) return launch_predictor<8>(a, s);
-    return launch_predictor<16>(a, s);
+  cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s, int mode) const override {
+    if (E == 4) return launch_predictor<4>(a, s, mode);
+    if (E == 8) return launch_predictor<8>(a, s, mode);
+    return launch_predictor<16>(a, s, mode);
   }
 #endif
   cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s) const override {
@@ -100,6 +107,27 @@ struct Impl final : KernelSet {
   cudaError_t tag(const TagArgs& a, cudaStream_t s) const override {
     if (a.n == 0) return cudaSuccess;
     k_tag<O><<<(a.n + 127) / 128, 128, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  cudaError_t seed_features(const SeedFeatArgs& a, cudaStream_t s) const override {
+    const long long n = (long long)a.n * (O::Q * O::NP_S + 1);
+    if (n == 0) return cudaSuccess;
+    k_seed_features<O><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  cudaError_t seed_targets(const SeedFeatArgs& a, cudaStream_t s) const override {
+    const long long n = (long long)a.n * O::Q;
+    if (n == 0) return cudaSuccess;
+    k_seed_targets<O><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  cudaError_t seed_assemble(const double* Uw, const float* Y, const float* y_mean, const float* y_std, int n,
+                            const int8_t* elem_level, const LevelGeom& geom, const double* dt, double* Hseed,
+                            cudaStream_t s) const override {
+    const long long t = (long long)n * O::Q;
+    if (t == 0) return cudaSuccess;
+    k_seed_assemble<O><<<(unsigned)((t + 127) / 128), 128, 0, s>>>(Uw, Y, y_mean, y_std, n, elem_level, geom, dt,
+                                                                    Hseed);
     return cudaGetLastError();
   }
   cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const override {

@@ -34,23 +34,32 @@ struct PredictorArgs {
   double* Rvol;
   double* Tr;
   double* Hw_out;             // optional: final H_w per element [elem][q][Np_st]
+  // learned seed (modes 1, 2): initial H_w per element, residual tolerance,
+  // fallback list of elements whose seed residual exceeds it
+  const double* Hseed;
+  double seed_tol;
+  int* fb_list;
+  int* fb_count;
+  // optional element list (fallback pass): element = elem_list[i], i < *list_count
+  const int* elem_list;
+  const int* list_count;
 };
 
 // Point-wise flux stage: H at NQ points of E elements (shared, [point][col])
 // -> F_d for every direction d, written over H (d = 0) and into the next
 // NQ x ld slabs (d >= 1).
-template <class O, int E, int NQ>
-__device__ __forceinline__ void flux_stage(double* sm, int ld, double gm1) {
+template <class O, int E, int NQ, class T = double>
+__device__ __forceinline__ void flux_stage(T* sm, int ld, T gm1) {
   constexpr int Q = O::Q, D = O::D;
   for (int it = threadIdx.x; it < E * NQ; it += blockDim.x) {
     const int m = it % NQ;
     const int e = it / NQ;
-    double* base = sm + m * ld + e * Q;
-    double u[Q];
+    T* base = sm + m * ld + e * Q;
+    T u[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) u[q] = base[q];
-    double F[D * Q];
-    euler_flux_all<D>(u, gm1, F);
+    T F[D * Q];
+    euler_flux_all<D, T>(u, gm1, F);
 #pragma unroll
     for (int d = 0; d < D; ++d)
 #pragma unroll
@@ -58,7 +67,39 @@ __device__ __forceinline__ void flux_stage(double* sm, int ld, double gm1) {
   }
 }
 
-template <class O, int E>
+// One Picard sweep (AmrDG.tpp:744-827, folded): H = V H_w at the space-time
+// points, F_d = f_d(H), H_w' = W U - sum_d c_d A_d F_d.  T: arithmetic of
+// the sweep (double on the plain path; float allowed on the seeded path).
+template <class O, int E, class T>
+__device__ __forceinline__ void picard_sweep(const double* hw, const double* wu, const double* c, T* sm, int col,
+                                             double gm1, double* out) {
+  constexpr int D = O::D, NP_ST = O::NP_ST, NQ = O::NQ_ST;
+  constexpr int LD = E * O::Q + 1;
+  O::template vol_eval<T>(RegIn{hw}, ColOutT<T>{sm + col, LD});
+  __syncthreads();
+  flux_stage<O, E, NQ, T>(sm, LD, (T)gm1);
+  __syncthreads();
+#pragma unroll
+  for (int n = 0; n < NP_ST; ++n) out[n] = wu[n];
+  T y[NP_ST];
+  O::template proj<0, T>(ColInT<T>{sm + col, LD}, RegOutT<T>{y});
+#pragma unroll
+  for (int n = 0; n < NP_ST; ++n) out[n] = fma(-c[0], (double)y[n], out[n]);
+  O::template proj<1, T>(ColInT<T>{sm + NQ * LD + col, LD}, RegOutT<T>{y});
+#pragma unroll
+  for (int n = 0; n < NP_ST; ++n) out[n] = fma(-c[1], (double)y[n], out[n]);
+  if constexpr (D == 3) {
+    O::template proj<2, T>(ColInT<T>{sm + 2 * NQ * LD + col, LD}, RegOutT<T>{y});
+#pragma unroll
+    for (int n = 0; n < NP_ST; ++n) out[n] = fma(-c[2], (double)y[n], out[n]);
+  }
+  __syncthreads();
+}
+
+// MODE 0: plain FP64 Picard (the reference's initial guess, P sweeps);
+// MODE 1 / 2: seeded, `sweeps` sweeps from the learned seed in FP64 / FP32,
+// the first one judging the seed by its residual.
+template <class O, int E, int MODE = 0>
 __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NP_ST = O::NP_ST;
   constexpr int NQ = O::NQ_ST, NB = O::NQ_BD, NI = O::NQ_INIT;
@@ -69,9 +110,15 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   const int col = threadIdx.x;
   const int el = col / Q;
   const int q = col % Q;
-  const int e_raw = blockIdx.x * E + el;
-  const bool live = e_raw < a.n_elem;
-  const int e = live ? e_raw : (a.n_elem - 1);
+  int e_raw = blockIdx.x * E + el;
+  bool live = e_raw < a.n_elem;
+  if (a.elem_list) {
+    const int cnt = *a.list_count;
+    if ((int)(blockIdx.x * E) >= cnt) return;  // whole block idle
+    live = e_raw < cnt;
+    e_raw = live ? a.elem_list[e_raw] : a.elem_list[cnt - 1];
+  }
+  const int e = live ? e_raw : (a.elem_list ? e_raw : (a.n_elem - 1));
   const int lev = a.elem_level ? a.elem_level[e] : 0;
   const double dt = *a.dt;
   double c[D];
@@ -88,49 +135,88 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   O::wu(RegIn{u}, RegOut{wu});
   double hw[NP_ST];
 
-  // ---- sweep 1: the reference's initial guess H_w = [U_w, 0, ...]
-  // (AmrDG.tpp:520-533) does not depend on x_0; evaluate on the (x_1.., t) grid.
-  O::vol_eval_init(RegIn{u}, ColOut{sm + col, LD});
-  __syncthreads();
-  flux_stage<O, E, NI>(sm, LD, gm1);
-  __syncthreads();
-#pragma unroll
-  for (int n = 0; n < NP_ST; ++n) hw[n] = wu[n];
-  {
-    double y[NP_ST];
-    O::template proj_init<0>(ColIn{sm + col, LD}, RegOut{y});
-#pragma unroll
-    for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[0], y[n], hw[n]);
-    O::template proj_init<1>(ColIn{sm + NI * LD + col, LD}, RegOut{y});
-#pragma unroll
-    for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[1], y[n], hw[n]);
-    if constexpr (D == 3) {
-      O::template proj_init<2>(ColIn{sm + 2 * NI * LD + col, LD}, RegOut{y});
-#pragma unroll
-      for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[2], y[n], hw[n]);
-    }
-  }
-  __syncthreads();
-
-  // ---- remaining Picard sweeps (AmrDG.h:1103-1119)
-  for (int s = 1; s < a.sweeps; ++s) {
-    O::vol_eval(RegIn{hw}, ColOut{sm + col, LD});
+  if constexpr (MODE == 0) {
+    // ---- sweep 1: the reference's initial guess H_w = [U_w, 0, ...]
+    // (AmrDG.tpp:520-533) does not depend on x_0; evaluate on the (x_1.., t) grid.
+    O::vol_eval_init(RegIn{u}, ColOut{sm + col, LD});
     __syncthreads();
-    flux_stage<O, E, NQ>(sm, LD, gm1);
+    flux_stage<O, E, NI>(sm, LD, gm1);
     __syncthreads();
-#pragma unroll
+  #pragma unroll
     for (int n = 0; n < NP_ST; ++n) hw[n] = wu[n];
-    double y[NP_ST];
-    O::template proj<0>(ColIn{sm + col, LD}, RegOut{y});
+    {
+      double y[NP_ST];
+      O::template proj_init<0>(ColIn{sm + col, LD}, RegOut{y});
+  #pragma unroll
+      for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[0], y[n], hw[n]);
+      O::template proj_init<1>(ColIn{sm + NI * LD + col, LD}, RegOut{y});
+  #pragma unroll
+      for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[1], y[n], hw[n]);
+      if constexpr (D == 3) {
+        O::template proj_init<2>(ColIn{sm + 2 * NI * LD + col, LD}, RegOut{y});
+  #pragma unroll
+        for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[2], y[n], hw[n]);
+      }
+    }
+    __syncthreads();
+
+    // ---- remaining Picard sweeps (AmrDG.h:1103-1119)
+    for (int s = 1; s < a.sweeps; ++s) {
+      O::vol_eval(RegIn{hw}, ColOut{sm + col, LD});
+      __syncthreads();
+      flux_stage<O, E, NQ>(sm, LD, gm1);
+      __syncthreads();
+  #pragma unroll
+      for (int n = 0; n < NP_ST; ++n) hw[n] = wu[n];
+      double y[NP_ST];
+      O::template proj<0>(ColIn{sm + col, LD}, RegOut{y});
+  #pragma unroll
+      for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[0], y[n], hw[n]);
+      O::template proj<1>(ColIn{sm + NQ * LD + col, LD}, RegOut{y});
+  #pragma unroll
+      for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[1], y[n], hw[n]);
+      if constexpr (D == 3) {
+        O::template proj<2>(ColIn{sm + 2 * NQ * LD + col, LD}, RegOut{y});
+  #pragma unroll
+        for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[2], y[n], hw[n]);
+      }
+      __syncthreads();
+    }
+  } else {
+    // ---- learned seed: H_w from the network, then `sweeps` sweeps; the
+    // first sweep's change judges the seed (residual relative to the
+    // element's largest cell mean), failures go to the fallback list.
+    const double* hs = a.Hseed + ((size_t)e * Q + q) * NP_ST;
 #pragma unroll
-    for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[0], y[n], hw[n]);
-    O::template proj<1>(ColIn{sm + NQ * LD + col, LD}, RegOut{y});
+    for (int n = 0; n < NP_ST; ++n) hw[n] = hs[n];
+    double res = 0.0;
+    for (int s = 0; s < a.sweeps; ++s) {
+      double nw[NP_ST];
+      if constexpr (MODE == 1)
+        picard_sweep<O, E, double>(hw, wu, c, sm, col, gm1, nw);
+      else
+        picard_sweep<O, E, float>(hw, wu, c, reinterpret_cast<float*>(sm), col, gm1, nw);
+      if (s == 0)
 #pragma unroll
-    for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[1], y[n], hw[n]);
-    if constexpr (D == 3) {
-      O::template proj<2>(ColIn{sm + 2 * NQ * LD + col, LD}, RegOut{y});
+        for (int n = 0; n < NP_ST; ++n) res = fmax(res, fabs(nw[n] - hw[n]));
 #pragma unroll
-      for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[2], y[n], hw[n]);
+      for (int n = 0; n < NP_ST; ++n) hw[n] = nw[n];
+    }
+    // per-element reduction over its Q columns through shared memory
+    double* red = sm;
+    red[col] = res;
+    red[NCOL + col] = fabs(u[0]);
+    __syncthreads();
+    if (q == 0 && live) {
+      double r = 0.0, scale = 0.0;
+      for (int k = 0; k < Q; ++k) {
+        r = fmax(r, red[el * Q + k]);
+        scale = fmax(scale, red[NCOL + el * Q + k]);
+      }
+      if (!(r <= a.seed_tol * scale)) {  // NaN fails too
+        const int slot = atomicAdd(a.fb_count, 1);
+        a.fb_list[slot] = e;
+      }
     }
     __syncthreads();
   }
@@ -182,17 +268,19 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   constexpr int NF = 2 * D;
   constexpr int NFIELD = 2 * Q + 1;
   const int e0 = blockIdx.x * E;
+  const int limit = a.elem_list ? *a.list_count : a.n_elem;
   for (int it = threadIdx.x; it < E * NF * NB; it += blockDim.x) {
     const int m = it % NB;
     const int f = (it / NB) % NF;
     const int ee = it / (NB * NF);
-    if (e0 + ee >= a.n_elem) continue;
+    if (e0 + ee >= limit) continue;
+    const int elem = a.elem_list ? a.elem_list[e0 + ee] : e0 + ee;
     const double* h = sm + (f * NB + m) * LD + ee * Q;
     double uu[Q], F[Q];
 #pragma unroll
     for (int k = 0; k < Q; ++k) uu[k] = h[k];
     const double df = euler_flux_normal<D>(f >> 1, uu, a.gamma, F);
-    double* t = a.Tr + (((size_t)(e0 + ee) * NF + f) * NFIELD) * NB + m;
+    double* t = a.Tr + (((size_t)elem * NF + f) * NFIELD) * NB + m;
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
       t[k * NB] = uu[k];
@@ -611,6 +699,85 @@ __global__ void k_tag(TagArgs a) {
     ind = fmax(ind, v);
   }
   a.tags[i] = ind > a.threshold ? 1 : 0;
+}
+
+// ===========================================================================
+// Learned predictor seed: features, training targets, seed assembly.
+// Features of element e: U_w (Q * Np_s modal coefficients) and Dt/dx_0 of
+// its level, standardised; targets: H_w - W U_w (the part of the predictor
+// the time evolution adds), standardised.
+// ===========================================================================
+struct SeedFeatArgs {
+  const double* Uw;
+  const double* Hw;      // targets only
+  int e0, n;             // elements e0 .. e0+n-1
+  const int8_t* elem_level;
+  LevelGeom geom;
+  const double* dt;
+  const float* x_mean;   // optional standardisation
+  const float* x_istd;
+  float* X;              // n x (Q*Np_s + 1)
+  float* T;              // n x (Q*Np_st)
+};
+
+template <class O>
+__global__ void k_seed_features(SeedFeatArgs a) {
+  constexpr int Q = O::Q, NP_S = O::NP_S, NIN = Q * NP_S + 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)a.n * NIN) return;
+  const int i = (int)(t / NIN), f = (int)(t % NIN);
+  const int e = a.e0 + i;
+  double v;
+  if (f < Q * NP_S) {
+    // the Euler flux is homogeneous of degree one in U: scale by the cell
+    // mean density so the network sees density-free states
+    v = a.Uw[(size_t)e * Q * NP_S + f] / a.Uw[(size_t)e * Q * NP_S];
+  } else {
+    const int lev = a.elem_level ? a.elem_level[e] : 0;
+    v = *a.dt / a.geom.dx[lev][0];
+  }
+  float x = (float)v;
+  if (a.x_mean) x = (x - a.x_mean[f]) * a.x_istd[f];
+  a.X[t] = x;
+}
+
+template <class O>
+__global__ void k_seed_targets(SeedFeatArgs a) {
+  constexpr int Q = O::Q, NP_S = O::NP_S, NP_ST = O::NP_ST;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)a.n * Q) return;
+  const int i = (int)(t / Q), q = (int)(t % Q);
+  const int e = a.e0 + i;
+  double wu[NP_ST];
+  O::wu(RegIn{a.Uw + ((size_t)e * Q + q) * NP_S}, RegOut{wu});
+  const double* h = a.Hw + ((size_t)e * Q + q) * NP_ST;
+  float* out = a.T + (size_t)i * Q * NP_ST + q * NP_ST;
+  // the predictor's change over the step, per unit density and Dt/dx
+  const int lev = a.elem_level ? a.elem_level[e] : 0;
+  const double scale = a.Uw[(size_t)e * Q * NP_S] * (*a.dt / a.geom.dx[lev][0]);
+#pragma unroll
+  for (int n = 0; n < NP_ST; ++n) out[n] = (float)((h[n] - wu[n]) / scale);
+}
+
+// H_seed = W U + rho_mean * (Dt/dx) * (Y * y_std + y_mean)
+template <class O>
+__global__ void k_seed_assemble(const double* Uw, const float* Y, const float* y_mean, const float* y_std, int n,
+                                const int8_t* elem_level, LevelGeom geom, const double* dt, double* Hseed) {
+  constexpr int Q = O::Q, NP_S = O::NP_S, NP_ST = O::NP_ST;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * Q) return;
+  const int e = (int)(t / Q), q = (int)(t % Q);
+  double wu[NP_ST];
+  O::wu(RegIn{Uw + ((size_t)e * Q + q) * NP_S}, RegOut{wu});
+  const int lev = elem_level ? elem_level[e] : 0;
+  const double scale = Uw[(size_t)e * Q * NP_S] * (*dt / geom.dx[lev][0]);
+  const float* y = Y + (size_t)e * Q * NP_ST + q * NP_ST;
+  double* h = Hseed + ((size_t)e * Q + q) * NP_ST;
+#pragma unroll
+  for (int k = 0; k < NP_ST; ++k) {
+    const int f = q * NP_ST + k;
+    h[k] = wu[k] + scale * (double)(y[k] * y_std[f] + y_mean[f]);
+  }
 }
 
 }  // namespace adg

@@ -16,7 +16,7 @@ struct KernelSet {
   virtual ~KernelSet() = default;
   virtual std::vector<int> elems_per_block_choices() const = 0;
   virtual size_t predictor_smem(int E) const = 0;
-  virtual cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s) const = 0;
+  virtual cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s, int mode = 0) const = 0;
   virtual cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s) const = 0;
   virtual cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t dt_reduce(const DtArgs& a, cudaStream_t s) const = 0;
@@ -25,6 +25,11 @@ struct KernelSet {
   virtual cudaError_t average_down(double* Uw, const int* rec, int nrec, cudaStream_t s) const = 0;
   virtual cudaError_t scatter(const ScatterArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t tag(const TagArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t seed_features(const SeedFeatArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t seed_targets(const SeedFeatArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t seed_assemble(const double* Uw, const float* Y, const float* y_mean, const float* y_std, int n,
+                                    const int8_t* elem_level, const LevelGeom& geom, const double* dt, double* Hseed,
+                                    cudaStream_t s) const = 0;
 };
 
 const KernelSet* kernels_D2P1();

@@ -576,7 +576,7 @@ def emit_stage(lines, st, src, dst, indent="    "):
     for r, terms in enumerate(st.rows):
         d = dst(r)
         if not terms:
-            lines.append(f"{indent}{d} = 0.0;")
+            lines.append(f"{indent}{d} = T(0);")
             continue
         expr = None
         for c, v in terms:
@@ -587,14 +587,14 @@ def emit_stage(lines, st, src, dst, indent="    "):
                 elif v == -1.0:
                     expr = f"(-{x})"
                 else:
-                    expr = f"{lit(v)} * {x}"
+                    expr = f"T({lit(v)}) * {x}"
             else:
                 if v == 1.0:
                     expr = f"({expr} + {x})"
                 elif v == -1.0:
                     expr = f"({expr} - {x})"
                 else:
-                    expr = f"fma({lit(v)}, {x}, {expr})"
+                    expr = f"fma(T({lit(v)}), {x}, {expr})"
         lines.append(f"{indent}{d} = {expr};")
 
 
@@ -602,13 +602,13 @@ def emit_op(name, op):
     stages, n_in, n_out = op
     nops = sum(fp64_ops(s) for s in stages)
     lines = [f"  // {name}: {n_in} -> {n_out}, {nops} FP64 instructions per column",
-             f"  template <class In, class Out>",
+             f"  template <class T = double, class In, class Out>",
              f"  static __device__ __forceinline__ void {name}(const In& in, Out out) {{"]
     for si, st in enumerate(stages):
         last = si == len(stages) - 1
         if not last:
-            lines.append(f"    double t{si}[{st.n_out}];")
-        src = (lambda c: f"in({c})") if si == 0 else (lambda c, p=si - 1: f"t{p}[{c}]")
+            lines.append(f"    T t{si}[{st.n_out}];")
+        src = (lambda c: f"T(in({c}))") if si == 0 else (lambda c, p=si - 1: f"t{p}[{c}]")
         dst = (lambda r: f"out({r})") if last else (lambda r, s=si: f"t{s}[{r}]")
         emit_stage(lines, st, src, dst)
     lines.append("  }")
@@ -753,12 +753,12 @@ def generate(D, P, out_path):
         counts[name] = nops
     # compile-time dispatchers
     def disp(fname, names, params):
-        lines = [f"  template <{', '.join('int ' + p for p in params)}, class In, class Out>",
+        lines = [f"  template <{', '.join('int ' + p for p in params)}, class T = double, class In, class Out>",
                  f"  static __device__ __forceinline__ void {fname}(const In& in, Out out) {{"]
         first = True
         for key, nm in names:
             cond = " && ".join(f"{p} == {v}" for p, v in zip(params, key))
-            lines.append(f"    {'if' if first else 'else if'} constexpr ({cond}) {nm}(in, out);")
+            lines.append(f"    {'if' if first else 'else if'} constexpr ({cond}) {nm}<T>(in, out);")
             first = False
         lines.append("  }")
         return "\n".join(lines)

@@ -115,6 +115,9 @@ int adg_advance(adg_ctx* ctx, int nsteps, int use_graph);
  * of the valid cells of a level from the current state (1 byte per cell, the
  * level's cell order).  (AmrDG_TagCellRef.tpp:4-52, Mesh::regrid) */
 int adg_regrid_count(const adg_ctx* ctx, int* n);
+/* DOF updates done so far (sum over steps of valid elements of every level
+ * times Q * Np_s) and the host wall time spent in regrids. */
+int adg_dof_updates(const adg_ctx* ctx, int64_t* total, double* regrid_ms);
 int adg_get_boxes(const adg_ctx* ctx, int lev, int* out, int cap, int* nbox);
 int adg_tags(adg_ctx* ctx, int lev, uint8_t* out);
 
@@ -146,6 +149,41 @@ int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds);
 /* Page-locked host buffers for host<->device state copies. */
 int adg_host_alloc(size_t bytes, void** ptr);
 int adg_host_free(void* ptr);
+
+/* ---------------------------------------------------------------------------
+ * Learned predictor seed.  A multilayer perceptron (Q*Np_s + 1 inputs: the
+ * element's modal state and Dt/dx; three hidden layers with GELU; Q*Np_st
+ * outputs: the space-time predictor H_w) trained on the GPU with FP32
+ * kernels on pairs the Picard predictor itself generates.  Attached to a
+ * context it supplies the predictor's initial guess: `sweeps` Picard sweeps
+ * from the seed replace the P sweeps of AmrDG<P>::ADER (AmrDG.h:1099-1119);
+ * the first sweep's change judges every element and elements whose residual
+ * exceeds `tol` (relative to the element's largest cell mean) rerun the full
+ * FP64 Picard predictor.  The corrector is always FP64.
+ * ------------------------------------------------------------------------- */
+typedef struct adg_seed adg_seed;
+int adg_seed_create(int D, int P, int hidden, uint64_t rng_seed, adg_seed** out);
+int adg_seed_destroy(adg_seed* s);
+/* Append (features, targets) of the current state of ctx's valid elements,
+ * targets from a Picard predictor of target_sweeps sweeps. */
+int adg_seed_collect(adg_ctx* ctx, adg_seed* s, int target_sweeps);
+int adg_seed_num_samples(const adg_seed* s, int64_t* n);
+/* Standardise the data set (first call) and train epochs of Adam. */
+int adg_seed_train(adg_seed* s, int epochs, int batch, double lr, double* last_epoch_loss);
+/* Network on standardised inputs X (n x n_in, host) -> Y (n x n_out, host). */
+int adg_seed_forward(adg_seed* s, const float* X, int n, float* Y);
+/* Loss and parameter gradients of the MSE on (X, T) (host, standardised). */
+int adg_seed_gradients(adg_seed* s, const float* X, const float* T, int n, float* grads, double* loss);
+/* Parameters: W1 b1 W2 b2 W3 b3 W4 b4 (row-major, in x out), then
+ * x_mean, x_istd, y_mean, y_std. */
+int adg_seed_num_params(const adg_seed* s, int64_t* n_weights, int64_t* n_total);
+int adg_seed_get_params(adg_seed* s, float* out);
+int adg_seed_set_params(adg_seed* s, const float* in);
+/* mode 0 detaches; 1: sweeps in FP64; 2: sweeps in FP32. */
+int adg_seed_attach(adg_ctx* ctx, adg_seed* s, int mode, int sweeps, double tol);
+/* Elements whose seed was rejected (fallback to the full Picard), and
+ * elements predicted, since attach. */
+int adg_seed_stats(adg_ctx* ctx, int64_t* fallbacks, int64_t* predicted);
 
 /* Measured FP64 multiply-add throughput of this GPU (DFMA chains), GFLOP/s. */
 int adg_fp64_peak_probe(double* gflops);

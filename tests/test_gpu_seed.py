@@ -1,0 +1,154 @@
+"""Learned predictor seed: the GPU FP32 training kernels against a float64
+restatement (forward, gradients, finite differences), training on Picard
+data, the residual fallback, and what the trained network buys over the
+method without it (same single sweep from the reference's initial guess)."""
+import numpy as np
+import pytest
+
+import mlp_ref
+from parity import G, make_gpu, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _layers64(seed):
+    return [(W.astype(np.float64), b.astype(np.float64)) for W, b in seed.weights()]
+
+
+def test_forward_matches_float64_restatement():
+    s = G.PredictorSeed(2, 3, hidden=64, rng_seed=7)
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((300, s.n_in)).astype(np.float32)
+    Y = s.forward(X)
+    Yr, _, _ = mlp_ref.forward(_layers64(s), X.astype(np.float64))
+    assert np.max(np.abs(Y - Yr)) < 1e-4 * max(1.0, np.max(np.abs(Yr)))
+
+
+def test_gradients_match_float64_restatement_and_finite_differences():
+    s = G.PredictorSeed(2, 1, hidden=32, rng_seed=11)
+    rng = np.random.default_rng(1)
+    X = rng.standard_normal((257, s.n_in)).astype(np.float32)
+    T = rng.standard_normal((257, s.n_out)).astype(np.float32)
+    g, loss = s.gradients(X, T)
+    layers = _layers64(s)
+    lr, gr = mlp_ref.loss_and_grads(layers, X.astype(np.float64), T.astype(np.float64))
+    gref = mlp_ref.flatten(gr)
+    assert abs(loss - lr) < 1e-5 * lr
+    assert np.max(np.abs(g - gref)) < 1e-4 * np.max(np.abs(gref))
+    # the float64 restatement itself against central differences
+    for (li, which, idx) in [(0, 0, (3, 5)), (1, 1, (7,)), (3, 0, (10, 2)), (2, 0, (0, 31))]:
+        W, b = layers[li]
+        arr = W if which == 0 else b
+        h = 1e-6
+        old = arr[idx]
+        arr[idx] = old + h
+        lp, _ = mlp_ref.loss_and_grads(layers, X.astype(np.float64), T.astype(np.float64))
+        arr[idx] = old - h
+        lm, _ = mlp_ref.loss_and_grads(layers, X.astype(np.float64), T.astype(np.float64))
+        arr[idx] = old
+        fd = (lp - lm) / (2 * h)
+        an = gr[li][which][idx]
+        assert abs(fd - an) < 1e-6 * max(1.0, abs(an)) + 1e-9
+
+
+def _kh(n=64, seed=12345, amp=1e-3, **kw):
+    s = G.AmrDG(P=3, D=2)
+    s.setGeometrySettings(prob_lo=(0, 0), prob_hi=(1, 1), n_cell=(n, n))
+    s.settings(c_dt=0.5, **kw)
+    s.init(G.Compressible_Euler().settings("kh_noise", seed=seed, noise_amp=amp))
+    return s
+
+
+_SEED = {}
+
+
+def _trained_seed():
+    """Seed trained on Picard pairs (converged predictor, 8 sweeps) of KH runs
+    with perturbed initial conditions; cached for the module."""
+    if "s" not in _SEED:
+        seed = G.PredictorSeed(2, 3, hidden=128, rng_seed=5)
+        for ic_seed in (1, 2, 3, 4):
+            s = _kh(seed=ic_seed, amp=1e-3 * ic_seed)
+            for k in range(24):
+                if k % 2 == 0:
+                    seed.collect(s, target_sweeps=8)
+                s.time_integration()
+        l0 = seed.train(1, batch=4096, lr=1e-3)
+        l1 = seed.train(60, batch=4096, lr=1e-3)
+        _SEED["s"] = (seed, l0, l1)
+    return _SEED["s"]
+
+
+def _predictor(sim):
+    torch = pytest.importorskip("torch")
+    n = sim.level_cells(0)
+    buf = torch.zeros(n * sim.Q * sim.Np_st, dtype=torch.float64, device="cuda")
+    sim.predictor(0, buf.data_ptr())
+    torch.cuda.synchronize()
+    return buf.cpu().numpy().reshape(n, sim.Q, sim.Np_st)
+
+
+def _state_after(steps, seed=42):
+    s = _kh(seed=seed)
+    for _ in range(steps):
+        s.time_integration()
+    return s.get_U_w(), s.Dt
+
+
+def _err(H, Hc, U):
+    scale = np.max(np.abs(U[:, :, 0]), axis=0)
+    return max(float(np.max(np.abs(H[:, q] - Hc[:, q])) / scale[q]) for q in (0, 1, 3))
+
+
+def test_training_reduces_loss_and_seed_beats_unseeded_single_sweep():
+    seed, l0, l1 = _trained_seed()
+    assert l1 < 0.1 * l0
+    U, dt = _state_after(15)
+
+    def run(**kw):
+        s = _kh(**kw)
+        s.set_U_w(U)
+        s.Dt = dt
+        return s
+
+    Hc = _predictor(run(picard_sweeps=10))  # converged Picard
+    e_plain = _err(_predictor(run()), Hc, U)
+    e_one = _err(_predictor(run(picard_sweeps=1)), Hc, U)
+    sd = run()
+    seed.attach(sd, mode=1, sweeps=1, tol=1e9)
+    e_seed1 = _err(_predictor(sd), Hc, U)
+    sd2 = run()
+    seed.attach(sd2, mode=2, sweeps=2, tol=1e9)
+    e_seed2_f32 = _err(_predictor(sd2), Hc, U)
+    # what the network buys: one sweep from the seed against one sweep from
+    # the reference's initial guess, and two FP32 sweeps from the seed
+    # against the reference's three FP64 sweeps
+    assert e_seed1 < 0.1 * e_one, (e_seed1, e_one)
+    assert e_seed2_f32 < 10 * e_plain, (e_seed2_f32, e_plain)
+
+
+def test_zero_tolerance_falls_back_everywhere_to_the_plain_path():
+    seed, _, _ = _trained_seed()
+    a = _kh(n=32, seed=9)
+    b = _kh(n=32, seed=9)
+    seed.attach(b, mode=1, sweeps=1, tol=1e-300)
+    for _ in range(3):
+        a.time_integration()
+        b.time_integration()
+    assert np.array_equal(a.get_U_w(), b.get_U_w())
+    fb, n = G.seed_stats(b)
+    assert fb == n == 3 * 32 * 32
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_seeded_run_stays_close_to_plain_run(mode):
+    seed, _, _ = _trained_seed()
+    a = _kh(seed=77)
+    b = _kh(seed=77)
+    seed.attach(b, mode=mode, sweeps=2, tol=1e-3)
+    for _ in range(10):
+        a.time_integration()
+        b.time_integration()
+    err = rel_err(b.get_U_w(), a.get_U_w())
+    assert err < 1e-5, err
+    assert b.status() == 0
