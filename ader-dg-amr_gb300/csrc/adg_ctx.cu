@@ -128,6 +128,9 @@ struct adg_ctx {
   DevBuf<int8_t> rf_dside, gf_child;
   std::vector<size_t> ad_off;  // offset (ints) of level lf's records in ad_all
   DevBuf<uint8_t> tags;
+  DevBuf<double> Uw_alt;   // regrid target state (swapped with Uw)
+  DevBuf<int> remap_i;     // regrid remap entries: dst | parent | src_old
+  DevBuf<int8_t> remap_c;  // regrid remap child indices
   // learned seed
   adg_seed* seed = nullptr;
   int seed_mode = 0, seed_sweeps = 1;
@@ -141,6 +144,7 @@ struct adg_ctx {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_kernels = 0;
+  bool graph_stale = false;
 
   ~adg_ctx() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
@@ -151,7 +155,7 @@ struct adg_ctx {
     rf_elem.release(); rf_off.release(); rf_face.release(); rf_fine.release(); ad_all.release();
     gf_elem.release(); gf_parent.release(); rf_dside.release(); gf_child.release(); tags.release();
     sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); fb_list.release(); fb_count.release();
-    fb_total.release();
+    fb_total.release(); Uw_alt.release(); remap_i.release(); remap_c.release();
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 };
@@ -238,14 +242,7 @@ int upload_tables(adg_ctx* ctx) {
   ADG_CUDA(up(ctx->gf_child, H.gf_child, "gf"), "h2d ghosts");
   ADG_CUDA(cudaStreamSynchronize(s), "sync tables");
   ctx->tables_dirty = false;
-  if (ctx->graph_exec) {
-    cudaGraphExecDestroy(ctx->graph_exec);
-    ctx->graph_exec = nullptr;
-  }
-  if (ctx->graph) {
-    cudaGraphDestroy(ctx->graph);
-    ctx->graph = nullptr;
-  }
+  ctx->graph_stale = true;  // re-captured before the next replay
   return ADG_OK;
 }
 
@@ -431,17 +428,17 @@ int regrid(adg_ctx* ctx) {
   std::string msg;
   if (!NH.build(ctx->gp, ng, ctx->cfg.reflux_box_quirk, &msg)) return fail(ctx, ADG_ERR_LAYOUT, "regrid: " + msg);
   // remap: level 0 is unchanged; level l from the old level l where a cell
-  // was valid there, else from the new level l-1.
-  DevBuf<double> nU;
+  // was valid there, else from the new level l-1 (levels in order on the stream).
   const int Q = ks->Q, Ns = ks->Np_s;
-  ADG_CUDA(nU.ensure(NH.n_elem() * Q * Ns), "alloc regrid state");
-  ADG_CUDA(cudaMemcpyAsync(nU.p, ctx->Uw.p, H.level_valid_count(0) * Q * Ns * sizeof(double), cudaMemcpyDeviceToDevice,
+  ADG_CUDA(ctx->Uw_alt.ensure(NH.n_elem() * Q * Ns), "alloc regrid state");
+  double* nU = ctx->Uw_alt.p;
+  ADG_CUDA(cudaMemcpyAsync(nU, ctx->Uw.p, H.level_valid_count(0) * Q * Ns * sizeof(double), cudaMemcpyDeviceToDevice,
                            ctx->stream), "regrid copy level 0");
-  DevBuf<int> d_dst, d_par, d_src;
-  DevBuf<int8_t> d_ch;
+  std::vector<int> dst, par, src;
+  std::vector<int8_t> ch;
+  std::vector<size_t> lo(NH.nlevels() + 1, 0);
   for (int l = 1; l < NH.nlevels(); ++l) {
-    std::vector<int> dst, par, src;
-    std::vector<int8_t> ch;
+    lo[l] = dst.size();
     for (size_t e = 0; e < NH.n_elem(); ++e) {
       if (NH.elem_level[e] != l) continue;
       const int* c = &NH.elem_cell[3 * e];
@@ -460,32 +457,36 @@ int regrid(adg_ctx* ctx) {
       src.push_back(old);
       ch.push_back((int8_t)child);
     }
-    if (dst.empty()) continue;
-    ADG_CUDA(d_dst.ensure(dst.size()), "alloc");
-    ADG_CUDA(d_par.ensure(dst.size()), "alloc");
-    ADG_CUDA(d_src.ensure(dst.size()), "alloc");
-    ADG_CUDA(d_ch.ensure(dst.size()), "alloc");
-    ADG_CUDA(cudaMemcpyAsync(d_dst.p, dst.data(), dst.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "h2d");
-    ADG_CUDA(cudaMemcpyAsync(d_par.p, par.data(), dst.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "h2d");
-    ADG_CUDA(cudaMemcpyAsync(d_src.p, src.data(), dst.size() * 4, cudaMemcpyHostToDevice, ctx->stream), "h2d");
-    ADG_CUDA(cudaMemcpyAsync(d_ch.p, ch.data(), dst.size(), cudaMemcpyHostToDevice, ctx->stream), "h2d");
-    ScatterArgs sa{};
-    sa.Uw = nU.p;
-    sa.Uw_old = ctx->Uw.p;
-    sa.dst = d_dst.p;
-    sa.parent = d_par.p;
-    sa.child = d_ch.p;
-    sa.src_old = d_src.p;
-    sa.n = (int)dst.size();
-    cudaError_t e = ks->scatter(sa, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "regrid remap launch");
-    ctx->launches++;
-    ADG_CUDA(cudaStreamSynchronize(ctx->stream), "regrid remap sync");  // host vectors go out of scope
   }
-  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "regrid sync");
-  std::swap(ctx->Uw, nU);
-  nU.release();
-  d_dst.release(); d_par.release(); d_src.release(); d_ch.release();
+  lo[NH.nlevels()] = dst.size();
+  const size_t nr = dst.size();
+  if (nr) {
+    std::vector<int> packed(3 * nr);
+    std::copy(dst.begin(), dst.end(), packed.begin());
+    std::copy(par.begin(), par.end(), packed.begin() + nr);
+    std::copy(src.begin(), src.end(), packed.begin() + 2 * nr);
+    ADG_CUDA(ctx->remap_i.ensure(3 * nr), "alloc remap");
+    ADG_CUDA(ctx->remap_c.ensure(nr), "alloc remap");
+    ADG_CUDA(cudaMemcpyAsync(ctx->remap_i.p, packed.data(), 3 * nr * 4, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    ADG_CUDA(cudaMemcpyAsync(ctx->remap_c.p, ch.data(), nr, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    for (int l = 1; l < NH.nlevels(); ++l) {
+      const size_t o = lo[l], n = lo[l + 1] - lo[l];
+      if (!n) continue;
+      ScatterArgs sa{};
+      sa.Uw = nU;
+      sa.Uw_old = ctx->Uw.p;
+      sa.dst = ctx->remap_i.p + o;
+      sa.parent = ctx->remap_i.p + nr + o;
+      sa.src_old = ctx->remap_i.p + 2 * nr + o;
+      sa.child = ctx->remap_c.p + o;
+      sa.n = (int)n;
+      cudaError_t e = ks->scatter(sa, ctx->stream);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "regrid remap launch");
+      ctx->launches++;
+    }
+  }
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "regrid sync");  // pageable sources above
+  std::swap(ctx->Uw, ctx->Uw_alt);
   ctx->hier = std::move(NH);
   ctx->n_regrids++;
   return upload_tables(ctx);
@@ -506,6 +507,8 @@ int check_ready(adg_ctx* ctx) {
   return ADG_OK;
 }
 
+// Capture the step; an existing executable graph of the same topology is
+// updated in place (cheaper than instantiating after every regrid).
 int capture_graph(adg_ctx* ctx) {
   long long before = ctx->launches;
   ADG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
@@ -517,10 +520,23 @@ int capture_graph(adg_ctx* ctx) {
     return rc;
   }
   if (e != cudaSuccess) return cuda_fail(ctx, e, "end capture");
+  bool updated = false;
+  if (ctx->graph_exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(ctx->graph_exec, g, &info) == cudaSuccess) {
+      updated = true;
+    } else {
+      cudaGetLastError();  // clear the update error
+      cudaGraphExecDestroy(ctx->graph_exec);
+      ctx->graph_exec = nullptr;
+    }
+  }
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
   ctx->graph = g;
-  ADG_CUDA(cudaGraphInstantiate(&ctx->graph_exec, g, 0), "graph instantiate");
+  if (!updated) ADG_CUDA(cudaGraphInstantiate(&ctx->graph_exec, g, 0), "graph instantiate");
   ctx->graph_kernels = (int)(ctx->launches - before);
   ctx->launches = before;
+  ctx->graph_stale = false;
   return ADG_OK;
 }
 
@@ -534,7 +550,7 @@ int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
   ctx->dof_updates += (long long)ctx->hier.n_valid() * ctx->ks->Q * ctx->ks->Np_s;
   ctx->first_step = false;
   if (use_graph && !ev) {
-    if (!ctx->graph_exec) {
+    if (!ctx->graph_exec || ctx->graph_stale) {
       int rc = capture_graph(ctx);
       if (rc) return rc;
     }
@@ -872,7 +888,7 @@ int adg_advance_timed(adg_ctx* ctx, int nsteps, int use_graph, double* ms) {
   int rc = check_ready(ctx);
   if (rc) return rc;
   if (!ms) return ADG_ERR_ARG;
-  if (use_graph && !ctx->graph_exec && !regrid_due(ctx)) {  // capture outside the timed region
+  if (use_graph && (!ctx->graph_exec || ctx->graph_stale) && !regrid_due(ctx)) {  // capture outside the timed region
     rc = capture_graph(ctx);
     if (rc) return rc;
   }
@@ -1021,7 +1037,12 @@ namespace {
 
 void sgemm(int TA, int TB, int M, int N, int K, const float* A, const float* B, float* C, const float* bias,
            float* aux, int epi, cudaStream_t st) {
-  dim3 grid((N + 63) / 64, (M + 63) / 64);
+  dim3 grid((N + 63) / 64, (M + 63) / 64, 1);
+  const int tiles = grid.x * grid.y;
+  if (epi == mlp::EPI_STORE && tiles < 64 && K >= 512) {  // few output tiles, long K: split K
+    grid.z = std::min(64, std::max(1, K / 256));
+    cudaMemsetAsync(C, 0, (size_t)M * N * sizeof(float), st);
+  }
   if (!TA && !TB) mlp::k_sgemm<0, 0><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
   else if (TA && !TB) mlp::k_sgemm<1, 0><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
   else if (!TA && TB) mlp::k_sgemm<0, 1><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
@@ -1057,20 +1078,26 @@ void seed_forward_train(adg_seed* s, const float* X, int B, cudaStream_t st) {
 }
 
 // Backward from dY (in s->dY) into s->grads.
+void colsum(int M, int N, const float* X, float* out, cudaStream_t st) {
+  cudaMemsetAsync(out, 0, (size_t)N * sizeof(float), st);
+  dim3 grid((N + 127) / 128, std::max(1, std::min(128, M / 64)));
+  mlp::k_colsum<<<grid, 128, 0, st>>>(M, N, X, out);
+}
+
 void seed_backward(adg_seed* s, const float* X, int B, cudaStream_t st) {
   using namespace mlp;
   const int h = s->h;
   sgemm(1, 0, h, s->n_out, B, s->A3.p, s->dY.p, G(s, 6), nullptr, nullptr, EPI_STORE, st);
-  k_colsum<<<(s->n_out + 127) / 128, 128, 0, st>>>(B, s->n_out, s->dY.p, G(s, 7));
+  colsum(B, s->n_out, s->dY.p, G(s, 7), st);
   sgemm(0, 1, B, h, s->n_out, s->dY.p, P(s, 6), s->dZ.p, nullptr, s->Z3.p, EPI_GELU_BWD, st);  // dZ3
   sgemm(1, 0, h, h, B, s->A2.p, s->dZ.p, G(s, 4), nullptr, nullptr, EPI_STORE, st);
-  k_colsum<<<(h + 127) / 128, 128, 0, st>>>(B, h, s->dZ.p, G(s, 5));
+  colsum(B, h, s->dZ.p, G(s, 5), st);
   sgemm(0, 1, B, h, h, s->dZ.p, P(s, 4), s->dA.p, nullptr, s->Z2.p, EPI_GELU_BWD, st);  // dZ2
   sgemm(1, 0, h, h, B, s->A1.p, s->dA.p, G(s, 2), nullptr, nullptr, EPI_STORE, st);
-  k_colsum<<<(h + 127) / 128, 128, 0, st>>>(B, h, s->dA.p, G(s, 3));
+  colsum(B, h, s->dA.p, G(s, 3), st);
   sgemm(0, 1, B, h, h, s->dA.p, P(s, 2), s->dZ.p, nullptr, s->Z1.p, EPI_GELU_BWD, st);  // dZ1
   sgemm(1, 0, s->n_in, h, B, X, s->dZ.p, G(s, 0), nullptr, nullptr, EPI_STORE, st);
-  k_colsum<<<(h + 127) / 128, 128, 0, st>>>(B, h, s->dZ.p, G(s, 1));
+  colsum(B, h, s->dZ.p, G(s, 1), st);
 }
 
 // Inference with ping-pong activations a0, a1 (rows x h each).

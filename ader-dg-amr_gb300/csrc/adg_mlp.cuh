@@ -42,20 +42,24 @@ __global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float*
   const int tid = threadIdx.x;
   const int tx = tid % 16, ty = tid / 16;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  // split-K: block z covers K range [kz0, kz1); partial sums are added
+  // atomically into C (which the caller zeroes) when gridDim.z > 1
+  const int kchunk = (((K + gridDim.z - 1) / gridDim.z) + BK - 1) / BK * BK;
+  const int kz0 = blockIdx.z * kchunk, kz1 = min(K, kz0 + kchunk);
   float acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += BK) {
+  for (int k0 = kz0; k0 < kz1; k0 += BK) {
     for (int i = tid; i < BM * BK; i += 256) {
       const int m = i % BM, k = i / BM;
       const int gm = m0 + m, gk = k0 + k;
       float v = 0.f;
-      if (gm < M && gk < K) v = TA ? A[(size_t)gk * M + gm] : A[(size_t)gm * K + gk];
+      if (gm < M && gk < kz1) v = TA ? A[(size_t)gk * M + gm] : A[(size_t)gm * K + gk];
       As[k][m] = v;
     }
     for (int i = tid; i < BN * BK; i += 256) {
       const int n = i % BN, k = i / BN;
       const int gn = n0 + n, gk = k0 + k;
       float v = 0.f;
-      if (gn < N && gk < K) v = TB ? B[(size_t)gn * K + gk] : B[(size_t)gk * N + gn];
+      if (gn < N && gk < kz1) v = TB ? B[(size_t)gn * K + gk] : B[(size_t)gk * N + gn];
       Bs[k][n] = v;
     }
     __syncthreads();
@@ -83,6 +87,10 @@ __global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float*
       if (gn >= N) continue;
       const size_t o = (size_t)gm * N + gn;
       float v = acc[i][j];
+      if (gridDim.z > 1) {  // split-K partial sum (EPI_STORE only)
+        atomicAdd(&C[o], v);
+        continue;
+      }
       if (epi == EPI_BIAS) {
         v += bias[gn];
       } else if (epi == EPI_BIAS_GELU) {
@@ -97,13 +105,16 @@ __global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float*
   }
 }
 
-// out[n] = sum_m X[m][n]
+// out[n] += sum over this block's rows of X[m][n] (out zeroed by the caller);
+// grid.x covers columns, grid.y splits the rows.
 __global__ void k_colsum(int M, int N, const float* X, float* out) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
+  const int rows = (M + gridDim.y - 1) / gridDim.y;
+  const int m0 = blockIdx.y * rows, m1 = min(M, m0 + rows);
   float s = 0.f;
-  for (int m = 0; m < M; ++m) s += X[(size_t)m * N + n];
-  out[n] = s;
+  for (int m = m0; m < m1; ++m) s += X[(size_t)m * N + n];
+  atomicAdd(&out[n], s);
 }
 
 // dY = (2 / (M N)) (Y - T); loss partial sums into loss_acc (double).

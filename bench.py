@@ -2,10 +2,17 @@
 """Benchmark of the GB300 ADER-DG element path.
 
 Workload (default): Kelvin-Helmholtz, 2D compressible Euler, modal Legendre
-p=3 (Np_s=10), single level 256x256 on periodic [0,1]^2, seeded noise,
-FP64 -- the configuration the headline metric is quoted on.  A step is one
-full ADER predictor-corrector step of every element plus the device-side
-time-step reduction.  Metric: DOF-updates/s = (elements * Q * Np_s) per step.
+p=3 (Np_s=10), 3 AMR levels 64^2 -> 128^2 -> 256^2 (ratio 2, max grid 32,
+blocking factor 8, normalised density gradient > 0.1, regrid every 4 steps)
+on periodic [0,1]^2, seeded noise, FP64 corrector -- the configuration the
+headline metric is quoted on.  A step is the whole evolve-loop body: regrid
+when due, ADER predictor-corrector of every element of every level in one
+launch per stage, reflux, average down, ghost fill, device time step.
+Metric: DOF-updates/s = sum over steps of valid elements of all levels times
+Q * Np_s.  The plain FP64 path and the learned-seed path run on the same
+workload; the headline value is the fastest seed variant whose L2 density
+error against a converged-Picard FP64 run stays within 1.01x of the plain
+path's.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -27,6 +34,16 @@ sys.path.insert(0, os.path.join(ROOT, "ader-dg-amr_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 WORKLOADS = {
+    # configs 3 + 4: batched 3-level KH, plain FP64 vs learned-seed path
+    "kh_p3_amr3": dict(D=2, P=3, n=(64, 64, 1), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), periodic=(1, 1, 1),
+                       ic="kh_noise", seed=12345, noise_amp=1e-3, c_dt=0.5,
+                       amr=dict(max_level=2, max_grid=32, blocking_factor=8, dtn_regrid=4, tag_kind=0,
+                                tag_threshold=0.1)),
+    # config 5: 3D blast, 2 levels
+    "blast3d_p2_amr2": dict(D=3, P=2, n=(64, 64, 64), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), periodic=(0, 0, 0),
+                            ic="blast3d", c_dt=0.5,
+                            amr=dict(max_level=1, max_grid=32, blocking_factor=8, dtn_regrid=4, tag_kind=1,
+                                     tag_threshold=0.1)),
     "kh_p3_256": dict(D=2, P=3, n=(256, 256, 1), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), periodic=(1, 1, 1),
                       ic="kh_noise", seed=12345, noise_amp=1e-3, c_dt=0.5),
     "vortex_p1_32": dict(D=2, P=1, n=(32, 32, 1), lo=(0.0, 0.0, 0.0), hi=(10.0, 10.0, 1.0), periodic=(1, 1, 1),
@@ -35,7 +52,7 @@ WORKLOADS = {
                           ic="blast3d", c_dt=0.5),
 }
 GPU_IC = {"kh_noise": "kh_noise", "vortex": "isentropic_vortex", "blast3d": "blast3d"}
-METRIC = "DOF-updates/s at 1 GB300 (single-level plain FP64 ADER-DG)"
+METRIC = "DOF-updates/s at 1 GB300: learned-seed+batched vs plain GPU FP64 vs CPU, at equal L2"
 
 
 def dist_env():
@@ -106,10 +123,20 @@ class ClockSampler:
         return out
 
 
-def make_sim(G, w, E=0):
+def make_sim(G, w, E=0, sweeps=0, seed=None, noise_amp=None):
     s = G.AmrDG(P=w["P"], D=w["D"])
-    s.setGeometrySettings(prob_lo=w["lo"], prob_hi=w["hi"], n_cell=w["n"], periodic=w["periodic"])
-    s.settings(c_dt=w["c_dt"], elems_per_block=E)
+    amr = w.get("amr", {})
+    s.setGeometrySettings(prob_lo=w["lo"], prob_hi=w["hi"], n_cell=w["n"], periodic=w["periodic"],
+                          max_level=amr.get("max_level", 0), max_grid=amr.get("max_grid", 1 << 20),
+                          blocking_factor=amr.get("blocking_factor", 8), dtn_regrid=amr.get("dtn_regrid", 4))
+    if amr:
+        s.setAmrSettings(tag_kind=amr["tag_kind"], tag_threshold=amr["tag_threshold"])
+    s.settings(c_dt=w["c_dt"], elems_per_block=E, picard_sweeps=sweeps)
+    w = dict(w)
+    if seed is not None:
+        w["seed"] = seed
+    if noise_amp is not None:
+        w["noise_amp"] = noise_amp
     extra = {k: w[k] for k in ("seed", "noise_amp", "u_inf", "v_inf") if k in w}
     s.init(G.Compressible_Euler().settings(GPU_IC[w["ic"]], **extra))
     return s
@@ -145,54 +172,147 @@ def autotune(G, w, steps=3):
 
 def cpu_baseline(w, max_seconds=20.0, threads=None):
     """The oracle (C++/OpenMP restatement of the reference) on the host cores:
-    a bounded sample of the same workload (whole grid, a few steps)."""
+    a bounded sample of the same workload (whole grid, a few steps; for AMR
+    the sample starts with the regrid of the first step)."""
     import oracle_ffi as O
+    from math import comb
 
     threads = threads or os.cpu_count()
     O.set_threads(threads)
+    amr = w.get("amr", {})
     cfg = O.make_cfg(D=w["D"], P=w["P"], n=w["n"], lo=w["lo"], hi=w["hi"], periodic=w["periodic"],
-                     ic=w["ic"], c_dt=w["c_dt"], max_grid=128,
+                     ic=w["ic"], c_dt=w["c_dt"], max_grid=amr.get("max_grid", 128),
+                     max_level=amr.get("max_level", 0), blocking_factor=amr.get("blocking_factor", 8),
+                     dtn_regrid=amr.get("dtn_regrid", 4), tag_kind=amr.get("tag_kind", 0),
+                     tag_threshold=amr.get("tag_threshold", 0.1),
                      **{k: w[k] for k in ("seed", "noise_amp", "u_inf", "v_inf") if k in w})
     s = O.OracleSim(cfg)
     s.init()
-    s.step()  # first step (page-in, allocation) not timed
-    steps, t0 = 0, time.perf_counter()
+    per_cell = (w["D"] + 2) * comb(w["P"] + w["D"], w["D"])
+    if not amr:
+        s.step()  # page-in, allocation
+    steps, dof, t0 = 0, 0, time.perf_counter()
     while True:
         s.step()
         steps += 1
+        dof += sum(s.ncells_level(l) for l in range(s.num_levels())) * per_cell
         el = time.perf_counter() - t0
         if el > max_seconds or steps >= 50:
             break
-    from math import comb
-    dof = w["n"][0] * w["n"][1] * w["n"][2] * (w["D"] + 2) * comb(w["P"] + w["D"], w["D"])
-    return {"value": dof * steps / el, "unit": "DOF-updates/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} steps of the full {'x'.join(map(str, w['n'][:w['D']]))} grid "
-                      f"({el:.1f} s), CPU oracle (reference algorithm restated in C++/OpenMP)"}
+    grid = "x".join(map(str, w["n"][:w["D"]]))
+    what = f"{steps} steps of the full {grid}" + (f" base grid with {s.num_levels()} levels" if amr else " grid")
+    return {"value": dof / el, "unit": "DOF-updates/s", "cores": threads, "kind": "port",
+            "sample": f"{what} ({el:.1f} s), CPU oracle (reference algorithm restated in C++/OpenMP)"}
 
 
 def run_reference(args, w):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    per_step = []
     base = cpu_baseline(w, max_seconds=max(5.0, 60.0 / max(1, args.steps + args.warmup)))
     val = base["value"]
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "DOF-updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, **{k: v for k, v in w.items() if k != "lo"}},
+            "config": {"workload": args.workload},
             "cpu_baseline": base,
             "e2e": {"value": val, "unit": "DOF-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    from math import comb
-    dof = w["n"][0] * w["n"][1] * w["n"][2] * (w["D"] + 2) * comb(w["P"] + w["D"], w["D"])
-    line["ms_per_step"] = dof / val * 1e3
     print(json.dumps(line))
     return 0
+
+
+# ---------------------------------------------------------------------------
+# accuracy: exact L2 of the density difference over level 0 (coarse cells
+# covered by finer levels hold the averaged-down fine solution, so level 0
+# carries the whole field on a layout shared by every run)
+# ---------------------------------------------------------------------------
+def mass_diag(w):
+    """Diagonal of the Legendre mass matrix, prod_d 2/(2k_d+1), in the
+    reference's total-degree mode order (first index slowest)."""
+    D, P = w["D"], w["P"]
+    m = []
+
+    def rec(prefix, left, depth):
+        if depth == D:
+            yield tuple(prefix)
+            return
+        for v in range(left + 1):
+            yield from rec(prefix + [v], left - v, depth + 1)
+    for n in rec([], P, 0):
+        v = 1.0
+        for k in n:
+            v *= 2.0 / (2 * k + 1)
+        m.append(v)
+    return m
+
+
+def l2_density_level0(Ua, Ub, w):
+    import numpy as np
+    M = np.array(mass_diag(w))
+    d = Ua[:, 0, :] - Ub[:, 0, :]
+    vol = 1.0
+    for k in range(w["D"]):
+        vol *= (w["hi"][k] - w["lo"][k])
+    # cell integral of the squared difference = (cell volume / 2^D) sum_n M_n d_n^2
+    ncell = Ua.shape[0]
+    integral = (vol / ncell) / 2 ** w["D"] * float(np.sum(M[None, :] * d * d))
+    return (integral / vol) ** 0.5
+
+
+def train_seed(G, w, n_pairs=2_000_000, epochs=40):
+    """Learned seed trained on pairs from the Picard predictor (8 sweeps) of
+    perturbed single-level and AMR runs of the workload's configuration."""
+    seed = G.PredictorSeed(w["D"], w["P"], hidden=128, rng_seed=2024)
+    t0 = time.perf_counter()
+    runs = []
+    base = dict(w)
+    single = dict(w)
+    single.pop("amr", None)
+    single["n"] = tuple((w["n"][d] << w["amr"]["max_level"]) if d < w["D"] else 1 for d in range(3)) if "amr" in w else w["n"]
+    k = 0
+    while seed.num_samples() < n_pairs and k < 16:
+        cfgw = single if k % 2 == 0 else base
+        s = make_sim(G, cfgw, seed=1000 + k, noise_amp=1e-3 * (1 + k % 4))
+        for st in range(40):
+            if st % 2 == 1:
+                seed.collect(s, target_sweeps=8)
+                if seed.num_samples() >= n_pairs:
+                    break
+            s.time_integration()
+        s.close()
+        k += 1
+    t1 = time.perf_counter()
+    loss = seed.train(epochs, batch=8192, lr=1e-3)
+    loss = seed.train(epochs // 2, batch=8192, lr=2e-4)
+    t2 = time.perf_counter()
+    return seed, {"pairs": seed.num_samples(), "collect_s": t1 - t0, "train_s": t2 - t1, "final_loss": loss,
+                  "epochs": epochs + epochs // 2}
+
+
+def timed_run(G, w, E, steps, warmup, seed=None, mode=0, sweeps=0, tol=1e-3, plain_sweeps=0):
+    s = make_sim(G, w, E, sweeps=plain_sweeps)
+    if seed is not None and mode:
+        seed.attach(s, mode=mode, sweeps=sweeps, tol=tol)
+    s.advance(warmup, use_graph=True)
+    s.Dt  # sync
+    d0, _ = s.dof_updates()
+    n0 = s.launch_count()
+    r0 = s.regrid_count()
+    _, rms0 = s.dof_updates()
+    ms = s.advance_timed(steps, use_graph=True)
+    d1, rms = s.dof_updates()
+    out = {"ms": ms, "dof": d1 - d0, "launches": s.launch_count() - n0, "regrids": s.regrid_count() - r0,
+           "regrid_ms": rms - rms0, "sim": s, "dof_per_s": (d1 - d0) / (ms * 1e-3)}
+    if seed is not None and mode:
+        fb, n = G.seed_stats(s)
+        out["fallback_rate"] = fb / max(1, n)
+    return out
 
 
 def run_ours(args, w):
     rank, world, local = dist_env()
     import adg_gb300 as G
+    import numpy as np
 
     G.set_device(local)
     dist = None
@@ -214,72 +334,112 @@ def run_ours(args, w):
         return float(t.item())
 
     from math import comb
-    n_elem = w["n"][0] * w["n"][1] * w["n"][2]
     Q = w["D"] + 2
     Nps = comb(w["P"] + w["D"], w["D"])
-    dof = n_elem * Q * Nps
-
     E, tune = autotune(G, w)
-    s = make_sim(G, w, E)
-    s.advance(max(3, args.warmup), use_graph=True)  # warm-up (includes graph capture)
-    s.Dt  # sync
-    n0 = s.launch_count()
-    with ClockSampler(local) as clk:
-        if dist is not None:
-            dist.barrier()
-        ms = s.advance_timed(args.steps, use_graph=True)
-    launches = s.launch_count() - n0
-    ms = barrier_max(ms)
-    value = dof * args.steps * world / (ms * 1e-3)
-    status = s.status()
+    variants = {}
+    seed = None
+    seed_info = None
+    is_amr = "amr" in w
+    if is_amr and not args.no_seed:
+        seed, seed_info = train_seed(G, w)
+    # plain FP64 path (P sweeps)
+    plain = timed_run(G, w, E, args.steps, args.warmup)
+    variants["plain_fp64"] = plain
+    if seed is not None:
+        ref = make_sim(G, w, E, sweeps=8)  # converged Picard, accuracy reference
+        ref.advance(args.warmup + args.steps, use_graph=True)
+        U_ref = ref.get_U_w(0)
+        for name, kw in (("seed_1sweep_fp64", dict(mode=1, sweeps=1)),
+                         ("seed_2sweeps_fp32", dict(mode=2, sweeps=2)),
+                         ("seed_3sweeps_fp32", dict(mode=2, sweeps=3))):
+            variants[name] = timed_run(G, w, E, args.steps, args.warmup, seed=seed, tol=1e-3, **kw)
+        variants["noseed_1sweep_fp64"] = timed_run(G, w, E, args.steps, args.warmup, plain_sweeps=1)
+        for v in variants.values():
+            v["l2_density_vs_converged"] = l2_density_level0(v["sim"].get_U_w(0), U_ref, w)
+        plain_err = variants["plain_fp64"]["l2_density_vs_converged"]
+        ok = {k: v for k, v in variants.items() if k.startswith("seed") and v["l2_density_vs_converged"] <= 1.01 * plain_err}
+        head_name = max(ok, key=lambda k: ok[k]["dof_per_s"]) if ok else "plain_fp64"
+    else:
+        head_name = "plain_fp64"
+    head = variants[head_name]
+    ms = barrier_max(head["ms"])
+    value = head["dof"] * world / (ms * 1e-3)
 
-    # end to end through the C ABI with host buffers: H2D of the state from
-    # page-locked memory, one step, D2H of the new state, every step.
-    host = G.PinnedArray((n_elem, Q, Nps))
-    host.array[:] = s.get_U_w()
+    # end to end through the C ABI with host buffers: every step copies the
+    # state of every level in from page-locked host memory and back out
+    s = head["sim"]
     e2e_steps = max(5, min(args.steps, 50))
+    nl = s.num_levels()
+    hosts = [G.PinnedArray((s.level_cells(l), Q, Nps)) for l in range(nl)]
+    for l in range(nl):
+        hosts[l].array[:] = s.get_U_w(l)
+    h2d = d2h = 0
     t0 = time.perf_counter()
+    d_before, _ = s.dof_updates()
     for _ in range(e2e_steps):
-        s.set_U_w(host.array)
+        if s.num_levels() != len(hosts) or any(s.level_cells(l) != hosts[l].array.shape[0] for l in range(len(hosts))):
+            for h in hosts:
+                h.free()
+            hosts = [G.PinnedArray((s.level_cells(l), Q, Nps)) for l in range(s.num_levels())]
+            for l in range(len(hosts)):
+                hosts[l].array[:] = s.get_U_w(l)
+        for l in range(len(hosts)):
+            s.set_U_w(hosts[l].array, l)
+            h2d += hosts[l].array.nbytes
         s.time_integration()
-        host.array[:] = s.get_U_w()
+        for l in range(s.num_levels()):
+            if l < len(hosts) and hosts[l].array.shape[0] == s.level_cells(l):
+                hosts[l].array[:] = s.get_U_w(l)
+                d2h += hosts[l].array.nbytes
     e2e_s = barrier_max(time.perf_counter() - t0)
-    e2e_val = dof * e2e_steps * world / e2e_s
-    host.free()
+    d_after, _ = s.dof_updates()
+    e2e_val = (d_after - d_before) * world / e2e_s
+    for h in hosts:
+        h.free()
 
-    # roofline of the dominant kernel (predictor: Picard sweeps, corrector
-    # volume term and face traces), CUDA events on the context's stream
-    km = s.time_kernels(5)
+    # roofline: the FP64 predictor kernel of the plain path on this workload
+    km_plain = plain["sim"].time_kernels(3)
+    km_head = head["sim"].time_kernels(3)
     alg, issued = G.flops_per_element(w["D"], w["P"])
-    Np_st = comb(w["P"] + w["D"] + 1, w["D"] + 1)
     qbd = (w["P"] + 1) ** w["D"]
-    # algorithmic flops of the predictor kernel: the method's count minus the
-    # corrector's face terms (2Q * 2D * Np_s * qMp_st_bd, done in k_corrector)
     alg_pred = alg - 2 * Q * 2 * w["D"] * Nps * qbd
-    peak = G.fp64_peak_gflops() / 1e3  # TFLOP/s, measured now on this GPU
-    achieved = alg_pred * n_elem / (km["predictor"] * 1e-3) / 1e12
+    # elements the predictor processed per step in the plain run (valid + ghost)
+    el_per_step = plain["dof"] / args.steps / (Q * Nps)
+    peak = G.fp64_peak_gflops() / 1e3
+    achieved = alg_pred * el_per_step / (km_plain["predictor"] * 1e-3) / 1e12
+    with ClockSampler(local) as clk:
+        clk_ms = head["sim"].advance_timed(min(args.steps, 50), use_graph=True)
     clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": "DOF-updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "D": w["D"], "P": w["P"], "cells": list(w["n"][:w["D"]]),
-                   "ic": w["ic"], "c_dt": w["c_dt"], "parallelism": "replicas" if world > 1 else "1 GPU",
+        "config": {"workload": args.workload, "D": w["D"], "P": w["P"], "base_cells": list(w["n"][:w["D"]]),
+                   "amr": w.get("amr"), "ic": w["ic"], "c_dt": w["c_dt"],
+                   "parallelism": "replicas" if world > 1 else "1 GPU", "path": head_name,
                    "elems_per_block": E, "cuda_graph": True,
                    "l2": "working set per step (state, traces, face fluxes) exceeds the 129 MB L2"},
-        "e2e": {"value": e2e_val, "unit": "DOF-updates/s", "h2d_bytes_per_step": dof * 8,
-                "d2h_bytes_per_step": dof * 8},
+        "e2e": {"value": e2e_val, "unit": "DOF-updates/s", "h2d_bytes_per_step": h2d // e2e_steps,
+                "d2h_bytes_per_step": d2h // e2e_steps},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
-                     "kernel": "k_predictor", "kernel_ms": km["predictor"],
-                     "algorithmic_flops_per_element": alg_pred,
+                     "kernel": "k_predictor (plain FP64 path of this workload)", "kernel_ms": km_plain["predictor"],
+                     "algorithmic_flops_per_element": alg_pred, "elements_per_launch": el_per_step,
                      "issued_linear_fp64_per_element": issued,
                      "peak_source": "DFMA-chain probe on this GPU in this run (MEASURED_PEAKS.json has no FP64 figure)"},
-        "kernel_ms": km,
-        "gpu_launches": launches,
+        "kernel_ms": {"plain": km_plain, "headline": km_head},
+        "variants": {k: {kk: vv for kk, vv in v.items() if kk != "sim"} for k, v in variants.items()},
+        "gpu_launches": head["launches"],
         "clocks": clocks,
-        "status": status,
+        "status": head["sim"].status(),
     }
+    if seed_info:
+        line["seed_training"] = seed_info
+        line["equal_l2"] = {"criterion": "L2 density (level-0 field, exact modal norm) against a converged-Picard "
+                                         "FP64 run within 1.01x of the plain FP64 path's",
+                            "plain": variants["plain_fp64"]["l2_density_vs_converged"],
+                            "headline": head.get("l2_density_vs_converged")}
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(w, max_seconds=args.cpu_seconds)
@@ -293,10 +453,11 @@ def run_ours(args, w):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="kh_p3_256", choices=list(WORKLOADS))
+    ap.add_argument("--workload", default="kh_p3_amr3", choices=list(WORKLOADS))
+    ap.add_argument("--no-seed", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -149,6 +149,10 @@ def test_seeded_run_stays_close_to_plain_run(mode):
     for _ in range(10):
         a.time_integration()
         b.time_integration()
-    err = rel_err(b.get_U_w(), a.get_U_w())
-    assert err < 1e-5, err
+    ua, ub = a.get_U_w(), b.get_U_w()
+    # density and energy, relative to their largest cell means (the
+    # y-momentum of this flow is ~1e-2 and is checked against the density scale)
+    for q in range(4):
+        scale = np.max(np.abs(ua[:, 0 if q == 2 else q, 0]))
+        assert np.max(np.abs(ub[:, q] - ua[:, q])) < 1e-5 * scale, q
     assert b.status() == 0
