@@ -94,6 +94,10 @@ def lib():
         "adg_flops_per_element": ([i, i, dp, dp], i),
         "adg_regrid_count": ([vp, ctypes.POINTER(i)], i),
         "adg_dof_updates": ([vp, ctypes.POINTER(ctypes.c_int64), dp], i),
+        "adg_regrid_profile": ([vp, dp, i], i),
+        "adg_leaf_dof_updates": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_seed_set_path": ([vp, i], i),
+        "adg_seed_infer": ([vp, vp, i], i),
         "adg_seed_create": ([i, i, i, ctypes.c_uint64, ctypes.POINTER(vp)], i),
         "adg_seed_destroy": ([vp], i),
         "adg_seed_collect": ([vp, vp, i], i),
@@ -312,6 +316,15 @@ class AmrDG:
         """Predictor H_w of the valid cells of level lev into a device buffer."""
         self._check(self._L.adg_predictor(self.ctx, lev, ctypes.c_void_p(dev_ptr)), "adg_predictor")
 
+    def seed_set_path(self, path):
+        """1: fused tensor-core seed inference (hidden width 128), 0: SIMT kernels."""
+        self._check(self._L.adg_seed_set_path(self.ctx, int(path)), "adg_seed_set_path")
+
+    def seed_infer(self, dev_ptr, path=1):
+        """Seeds H_w of every element of the layout (valid of all levels, then
+        ghosts) into a device buffer of n_elem * Q * Np_st doubles."""
+        self._check(self._L.adg_seed_infer(self.ctx, ctypes.c_void_p(dev_ptr), int(path)), "adg_seed_infer")
+
     def status(self):
         v = ctypes.c_uint32()
         self._check(self._L.adg_status(self.ctx, ctypes.byref(v)), "adg_status")
@@ -340,6 +353,20 @@ class AmrDG:
         n, ms = ctypes.c_int64(), ctypes.c_double()
         self._check(self._L.adg_dof_updates(self.ctx, ctypes.byref(n), ctypes.byref(ms)), "adg_dof_updates")
         return n.value, ms.value
+
+    def leaf_dof_updates(self):
+        """DOF updates so far over leaf elements only."""
+        n = ctypes.c_int64()
+        self._check(self._L.adg_leaf_dof_updates(self.ctx, ctypes.byref(n)), "adg_leaf_dof_updates")
+        return n.value
+
+    def regrid_profile(self):
+        """Host ms spent in regrids by phase: tags+wait, clustering, tables,
+        upload, remap launches, graph update."""
+        ms = (ctypes.c_double * 6)()
+        self._check(self._L.adg_regrid_profile(self.ctx, ms, 6), "adg_regrid_profile")
+        keys = ("tags_wait", "cluster", "tables", "upload", "remap", "graph")
+        return dict(zip(keys, list(ms)))
 
     def regrid_count(self):
         n = ctypes.c_int()

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -24,13 +25,16 @@ template <class T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  // Grows only; a re-growth takes 25% slack so that layouts of slowly
+  // changing size (AMR regrids) do not reallocate every time.
   cudaError_t ensure(size_t count) {
     if (count <= n && p) return cudaSuccess;
+    const size_t cap = p ? count + count / 4 : count;
     if (p) cudaFree(p);
     p = nullptr;
     n = 0;
-    cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
-    if (e == cudaSuccess) n = count;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(cap, 1) * sizeof(T));
+    if (e == cudaSuccess) n = cap;
     return e;
   }
   void release() {
@@ -40,13 +44,20 @@ struct DevBuf {
   }
 };
 
-// t += Dt; Dt = c_dt * min; reset the accumulator (AmrDG.h:1019, 1356).
-__global__ void k_dt_finalize(double* dt, double* t, unsigned long long* min_bits, double c_dt, int advance_time) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    if (advance_time) *t += *dt;
-    *dt = c_dt * __longlong_as_double((long long)*min_bits);
-    *min_bits = (unsigned long long)__double_as_longlong(1.0e300);
-  }
+// A layout table: a view into the packed table buffer of a context.
+template <class T>
+struct TableView {
+  T* p = nullptr;
+  void release() { p = nullptr; }
+};
+
+// Pack W (row-major in x out) of one layer as the B operand: row n = output,
+// K-major with K = Kp (zero padded), Np rows (zero padded), rounded to TF32.
+__global__ void k_seed_pack_tc(const float* W, int in, int out, int Kp, int Np, float* dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Kp * Np) return;
+  const int n = i / Kp, k = i % Kp;
+  dst[tc::kmajor_off(n, k, Kp)] = (n < out && k < in) ? tc::to_tf32(W[(size_t)k * out + n]) : 0.0f;
 }
 
 // FP64 throughput probe: independent DFMA chains.
@@ -86,9 +97,13 @@ struct adg_seed {
   std::mt19937_64 rng;
   long long adam_t = 0;
   std::string err;
+  // weights packed for the tensor-core inference kernel (hidden width 128)
+  DevBuf<float> wpack;
+  long long w_off[4] = {};
+  bool packed = false;
   ~adg_seed() {
     DevBuf<float>* bufs[] = {&params, &grads, &am, &av, &x_mean, &x_istd, &y_mean, &y_std, &X, &T,
-                             &Z1, &A1, &Z2, &A2, &Z3, &A3, &Y, &dY, &dA, &dZ, &Xb, &Tb};
+                             &Z1, &A1, &Z2, &A2, &Z3, &A3, &Y, &dY, &dA, &dZ, &Xb, &Tb, &wpack};
     for (auto* b : bufs) b->release();
     idx.release();
     loss.release();
@@ -112,25 +127,35 @@ struct adg_ctx {
   bool tables_dirty = true;
   long long nstep = 0;  // completed steps (regrid schedule)
   long long dof_updates = 0;  // sum over steps of valid elements * Q * Np_s
+  long long leaf_dof_updates = 0;  // the same over leaf (uncovered) elements
+  size_t n_leaf = 0;               // leaf elements of the current layout
   double regrid_ms = 0.0;     // host wall time spent in regrids
   bool first_step = true;
   int n_regrids = 0;
 
   // device state
   DevBuf<double> Uw, Rvol, Tr, Fnum, Hw_dbg;
-  DevBuf<int> face_left, face_right, elem_face, elem_cell;
-  DevBuf<int8_t> elem_level;
-  DevBuf<double> scal;  // [0] Dt, [1] t
+  TableView<int> face_left, face_right, elem_face, elem_cell;
+  TableView<int8_t> elem_level;
+  DevBuf<double> scal;  // scalar block: [0] Dt, [1] t, Dt/dx per level (kScalDtDx)
+  DevBuf<unsigned int> dt_done;  // blocks of the Dt reduction that have finished
   DevBuf<unsigned long long> min_bits;
   DevBuf<unsigned int> status;
   // AMR tables
-  DevBuf<int> rf_elem, rf_off, rf_face, rf_fine, ad_all, gf_elem, gf_parent;
-  DevBuf<int8_t> rf_dside, gf_child;
+  TableView<int> rf_elem, rf_off, rf_face, rf_fine, ad_all, gf_elem, gf_parent, rf_rec_of_elem;
+  TableView<int8_t> rf_dside, gf_child;
+  // all layout tables packed in one device buffer, uploaded by one copy from
+  // a pinned staging buffer (tab_ev: that copy has completed)
+  DevBuf<uint8_t> tab_dev;
+  uint8_t* tab_host = nullptr;
+  size_t tab_host_cap = 0;
+  cudaEvent_t tab_ev = nullptr;
   std::vector<size_t> ad_off;  // offset (ints) of level lf's records in ad_all
   DevBuf<uint8_t> tags;
   DevBuf<double> Uw_alt;   // regrid target state (swapped with Uw)
-  DevBuf<int> remap_i;     // regrid remap entries: dst | parent | src_old
-  DevBuf<int8_t> remap_c;  // regrid remap child indices
+  TableView<int> remap_i;     // regrid remap entries: dst | parent | src_old
+  TableView<int8_t> remap_c;  // regrid remap child indices
+  double rg_phase_ms[6] = {0, 0, 0, 0, 0, 0};  // regrid host time by phase
   // learned seed
   adg_seed* seed = nullptr;
   int seed_mode = 0, seed_sweeps = 1;
@@ -140,6 +165,7 @@ struct adg_ctx {
   DevBuf<int> fb_list, fb_count;
   DevBuf<unsigned long long> fb_total;
   long long seed_predicted = 0;
+  int seed_path = 1;  // 1: tensor-core inference when the seed supports it, 0: SIMT kernels
 
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -151,11 +177,14 @@ struct adg_ctx {
     if (graph) cudaGraphDestroy(graph);
     Uw.release(); Rvol.release(); Tr.release(); Fnum.release(); Hw_dbg.release();
     face_left.release(); face_right.release(); elem_face.release(); elem_cell.release();
-    elem_level.release(); scal.release(); min_bits.release(); status.release();
+    elem_level.release(); scal.release(); dt_done.release(); min_bits.release(); status.release();
     rf_elem.release(); rf_off.release(); rf_face.release(); rf_fine.release(); ad_all.release();
     gf_elem.release(); gf_parent.release(); rf_dside.release(); gf_child.release(); tags.release();
     sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); fb_list.release(); fb_count.release();
     fb_total.release(); Uw_alt.release(); remap_i.release(); remap_c.release();
+    if (tab_ev) cudaEventSynchronize(tab_ev), cudaEventDestroy(tab_ev);
+    tab_dev.release();
+    if (tab_host) cudaFreeHost(tab_host);
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 };
@@ -189,7 +218,13 @@ LevelGeom level_geom(const adg_ctx* ctx) {
 
 // Upload element and face tables of the current layout and size the work
 // buffers.
-int upload_tables(adg_ctx* ctx) {
+// Remap entries of a regrid, uploaded with the tables.
+struct RemapTable {
+  std::vector<int> dst, par, src;
+  std::vector<int8_t> ch;
+};
+
+int upload_tables(adg_ctx* ctx, const RemapTable* rm = nullptr) {
   const Hierarchy& H = ctx->hier;
   const KernelSet* ks = ctx->ks;
   const int D = ctx->cfg.D, Q = ks->Q;
@@ -198,11 +233,6 @@ int upload_tables(adg_ctx* ctx) {
   ADG_CUDA(ctx->Rvol.ensure(ne * Q * ks->Np_s), "alloc Rvol");
   ADG_CUDA(ctx->Tr.ensure(ne * 2 * D * (2 * Q + 1) * (size_t)ks->NQ_BD), "alloc traces");
   ADG_CUDA(ctx->Fnum.ensure(nf * Q * (size_t)ks->NQ_BD), "alloc Fnum");
-  ADG_CUDA(ctx->face_left.ensure(nf), "alloc faces");
-  ADG_CUDA(ctx->face_right.ensure(nf), "alloc faces");
-  ADG_CUDA(ctx->elem_face.ensure(ne * 2 * D), "alloc elem faces");
-  ADG_CUDA(ctx->elem_cell.ensure(ne * 3), "alloc elem cells");
-  ADG_CUDA(ctx->elem_level.ensure(ne), "alloc elem levels");
   if (ctx->seed) {
     const adg_seed* sd = ctx->seed;
     ADG_CUDA(ctx->sx.ensure(ne * sd->n_in), "alloc seed features");
@@ -212,23 +242,6 @@ int upload_tables(adg_ctx* ctx) {
     ADG_CUDA(ctx->hseed.ensure(ne * (size_t)ks->Q * ks->Np_st), "alloc seed H_w");
     ADG_CUDA(ctx->fb_list.ensure(ne), "alloc fallback list");
   }
-  cudaStream_t s = ctx->stream;
-  ADG_CUDA(cudaMemcpyAsync(ctx->face_left.p, H.face_left.data(), nf * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
-  ADG_CUDA(cudaMemcpyAsync(ctx->face_right.p, H.face_right.data(), nf * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
-  ADG_CUDA(cudaMemcpyAsync(ctx->elem_face.p, H.elem_face.data(), H.elem_face.size() * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
-  ADG_CUDA(cudaMemcpyAsync(ctx->elem_cell.p, H.elem_cell.data(), H.elem_cell.size() * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
-  ADG_CUDA(cudaMemcpyAsync(ctx->elem_level.p, H.elem_level.data(), H.elem_level.size(), cudaMemcpyHostToDevice, s), "h2d");
-  // coarse-fine tables
-  auto up = [&](auto& buf, const auto& vec, const char* what) -> cudaError_t {
-    cudaError_t e = buf.ensure(vec.size());
-    if (e != cudaSuccess || vec.empty()) return e;
-    return cudaMemcpyAsync(buf.p, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice, s);
-  };
-  ADG_CUDA(up(ctx->rf_elem, H.rf_elem, "rf"), "h2d reflux");
-  ADG_CUDA(up(ctx->rf_off, H.rf_off, "rf"), "h2d reflux");
-  ADG_CUDA(up(ctx->rf_face, H.rf_face, "rf"), "h2d reflux");
-  ADG_CUDA(up(ctx->rf_dside, H.rf_dside, "rf"), "h2d reflux");
-  ADG_CUDA(up(ctx->rf_fine, H.rf_fine, "rf"), "h2d reflux");
   std::vector<int> ad;
   ctx->ad_off.assign(H.nlevels() + 1, 0);
   for (int lf = 0; lf < H.nlevels(); ++lf) {
@@ -236,11 +249,80 @@ int upload_tables(adg_ctx* ctx) {
     ad.insert(ad.end(), H.ad_rec[lf].begin(), H.ad_rec[lf].end());
   }
   ctx->ad_off[H.nlevels()] = ad.size();
-  ADG_CUDA(up(ctx->ad_all, ad, "ad"), "h2d average down");
-  ADG_CUDA(up(ctx->gf_elem, H.gf_elem, "gf"), "h2d ghosts");
-  ADG_CUDA(up(ctx->gf_parent, H.gf_parent, "gf"), "h2d ghosts");
-  ADG_CUDA(up(ctx->gf_child, H.gf_child, "gf"), "h2d ghosts");
-  ADG_CUDA(cudaStreamSynchronize(s), "sync tables");
+  {
+    const size_t nov1 = ((size_t)1 << D) + 1;  // one record per covered coarse element
+    ctx->n_leaf = H.n_valid() - ad.size() / nov1;
+  }
+  // pack every table (256-byte aligned) into the pinned staging buffer
+  struct Item {
+    const void* src;
+    size_t bytes, off;
+    std::function<void(uint8_t*)> bind;
+  };
+  std::vector<Item> items;
+  size_t total = 0;
+  auto add = [&](auto& view, const auto& vec) {
+    using T = std::remove_reference_t<decltype(*view.p)>;
+    const size_t bytes = vec.size() * sizeof(vec[0]);
+    items.push_back({vec.data(), bytes, total, [&view](uint8_t* at) { view.p = reinterpret_cast<T*>(at); }});
+    total += (bytes + 255) & ~size_t(255);
+  };
+  add(ctx->face_left, H.face_left);
+  add(ctx->face_right, H.face_right);
+  add(ctx->elem_face, H.elem_face);
+  add(ctx->elem_cell, H.elem_cell);
+  add(ctx->elem_level, H.elem_level);
+  add(ctx->rf_elem, H.rf_elem);
+  add(ctx->rf_off, H.rf_off);
+  add(ctx->rf_face, H.rf_face);
+  add(ctx->rf_dside, H.rf_dside);
+  add(ctx->rf_fine, H.rf_fine);
+  std::vector<int> roe(H.n_valid(), -1);
+  for (size_t r = 0; r < H.rf_elem.size(); ++r) roe[H.rf_elem[r]] = (int)r;
+  add(ctx->rf_rec_of_elem, roe);
+  add(ctx->ad_all, ad);
+  // ghost fills grouped by child index: the warps of the fill kernel then
+  // mostly run a single coarse-to-fine operator
+  std::vector<size_t> gperm(H.gf_elem.size());
+  for (size_t i = 0; i < gperm.size(); ++i) gperm[i] = i;
+  std::stable_sort(gperm.begin(), gperm.end(), [&](size_t x, size_t y) { return H.gf_child[x] < H.gf_child[y]; });
+  std::vector<int> gfe(gperm.size()), gfp(gperm.size());
+  std::vector<int8_t> gfc(gperm.size());
+  for (size_t i = 0; i < gperm.size(); ++i) {
+    gfe[i] = H.gf_elem[gperm[i]];
+    gfp[i] = H.gf_parent[gperm[i]];
+    gfc[i] = H.gf_child[gperm[i]];
+  }
+  add(ctx->gf_elem, gfe);
+  add(ctx->gf_parent, gfp);
+  add(ctx->gf_child, gfc);
+  std::vector<int> remap_packed;
+  if (rm) {
+    const size_t nr = rm->dst.size();
+    remap_packed.resize(3 * nr);
+    std::copy(rm->dst.begin(), rm->dst.end(), remap_packed.begin());
+    std::copy(rm->par.begin(), rm->par.end(), remap_packed.begin() + nr);
+    std::copy(rm->src.begin(), rm->src.end(), remap_packed.begin() + 2 * nr);
+    add(ctx->remap_i, remap_packed);
+    add(ctx->remap_c, rm->ch);
+  }
+  if (!ctx->tab_ev) ADG_CUDA(cudaEventCreateWithFlags(&ctx->tab_ev, cudaEventDisableTiming), "table event");
+  ADG_CUDA(cudaEventSynchronize(ctx->tab_ev), "table staging reuse");  // the previous upload has been read
+  if (total > ctx->tab_host_cap) {
+    if (ctx->tab_host) cudaFreeHost(ctx->tab_host);
+    ctx->tab_host = nullptr;
+    ctx->tab_host_cap = 0;
+    const size_t cap = total + total / 4;
+    ADG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ctx->tab_host), cap, cudaHostAllocDefault), "alloc table staging");
+    ctx->tab_host_cap = cap;
+  }
+  ADG_CUDA(ctx->tab_dev.ensure(std::max<size_t>(total, 256)), "alloc tables");
+  for (const Item& it : items) {
+    if (it.bytes) std::memcpy(ctx->tab_host + it.off, it.src, it.bytes);
+    it.bind(ctx->tab_dev.p + it.off);
+  }
+  ADG_CUDA(cudaMemcpyAsync(ctx->tab_dev.p, ctx->tab_host, total, cudaMemcpyHostToDevice, ctx->stream), "h2d tables");
+  ADG_CUDA(cudaEventRecord(ctx->tab_ev, ctx->stream), "table event");
   ctx->tables_dirty = false;
   ctx->graph_stale = true;  // re-captured before the next replay
   return ADG_OK;
@@ -298,27 +380,17 @@ int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
   ca.elem_level = pa.elem_level;
   ca.geom = pa.geom;
   ca.dt = ctx->scal.p;
+  if (!H.rf_elem.empty()) {  // coarse-fine flux correction (AmrDG.h:1159-1162), fused
+    ca.rec_of_elem = ctx->rf_rec_of_elem.p;
+    ca.rec_off = ctx->rf_off.p;
+    ca.ent_face = ctx->rf_face.p;
+    ca.ent_dside = ctx->rf_dside.p;
+    ca.ent_fine = ctx->rf_fine.p;
+  }
   e = ks->corrector(ca, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "corrector launch");
   ctx->launches++;
   if (ev) cudaEventRecord(ev[3], ctx->stream);
-  if (!H.rf_elem.empty()) {  // coarse-fine flux correction (AmrDG.h:1159-1162)
-    RefluxArgs ra{};
-    ra.Uw = ctx->Uw.p;
-    ra.Fnum = ctx->Fnum.p;
-    ra.rec_elem = ctx->rf_elem.p;
-    ra.rec_off = ctx->rf_off.p;
-    ra.ent_face = ctx->rf_face.p;
-    ra.ent_dside = ctx->rf_dside.p;
-    ra.ent_fine = ctx->rf_fine.p;
-    ra.elem_level = ctx->elem_level.p;
-    ra.nrec = (int)H.rf_elem.size();
-    ra.geom = pa.geom;
-    ra.dt = ctx->scal.p;
-    e = ks->reflux(ra, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "reflux launch");
-    ctx->launches++;
-  }
   return ADG_OK;
 }
 
@@ -365,12 +437,15 @@ int launch_dt(adg_ctx* ctx, int advance_time) {
   da.gamma = ctx->cfg.gamma;
   da.min_bits = ctx->min_bits.p;
   da.status = ctx->status.p;
+  da.scal = ctx->scal.p;
+  da.done = ctx->dt_done.p;
+  da.c_dt = ctx->cfg.c_dt;
+  da.advance_time = advance_time;
+  da.D = ctx->cfg.D;
+  da.geom = g;
   cudaError_t e = ctx->ks->dt_reduce(da, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "dt launch");
-  k_dt_finalize<<<1, 32, 0, ctx->stream>>>(ctx->scal.p, ctx->scal.p + 1, ctx->min_bits.p, ctx->cfg.c_dt, advance_time);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "dt finalize launch");
-  ctx->launches += 2;
+  ctx->launches += 1;
   return ADG_OK;
 }
 
@@ -388,7 +463,12 @@ int launch_step(adg_ctx* ctx, cudaEvent_t* ev = nullptr) {
 // Regrid (AmrDG.h:935-986): refinement indicator on the device, tags to the
 // host, new boxes (amr_grids.hpp), new layout, and the level-by-level remap
 // of the state (RemakeLevel / MakeNewLevelFromCoarse, AmrDG_Level.tpp:52-132).
+double ms_between(std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
 int regrid(adg_ctx* ctx) {
+  auto t0 = std::chrono::steady_clock::now();
   Hierarchy& H = ctx->hier;
   const KernelSet* ks = ctx->ks;
   const int F = H.nlevels() - 1;
@@ -414,6 +494,8 @@ int regrid(adg_ctx* ctx) {
   std::vector<uint8_t> ht(nt);
   ADG_CUDA(cudaMemcpyAsync(ht.data(), ctx->tags.p, nt, cudaMemcpyDeviceToHost, ctx->stream), "tags d2h");
   ADG_CUDA(cudaStreamSynchronize(ctx->stream), "tags sync");
+  auto t1 = std::chrono::steady_clock::now();
+  ctx->rg_phase_ms[0] += ms_between(t0, t1);
   std::vector<amr::TagField> tf(F + 1);
   for (int l = 0; l <= F; ++l) {
     int n[3];
@@ -424,6 +506,12 @@ int regrid(adg_ctx* ctx) {
       if (ht[e]) tf[l].f[tf[l].idx(H.elem_cell[3 * e], H.elem_cell[3 * e + 1], H.elem_cell[3 * e + 2])] = 1;
   }
   std::vector<std::vector<amr::IBox>> ng = amr::make_new_grids(ctx->gp, H.grids, tf);
+  auto t2 = std::chrono::steady_clock::now();
+  ctx->rg_phase_ms[1] += ms_between(t1, t2);
+  if (ng == H.grids) {  // same boxes in the same order: layout and valid data unchanged
+    ctx->n_regrids++;
+    return ADG_OK;
+  }
   Hierarchy NH;
   std::string msg;
   if (!NH.build(ctx->gp, ng, ctx->cfg.reflux_box_quirk, &msg)) return fail(ctx, ADG_ERR_LAYOUT, "regrid: " + msg);
@@ -434,11 +522,10 @@ int regrid(adg_ctx* ctx) {
   double* nU = ctx->Uw_alt.p;
   ADG_CUDA(cudaMemcpyAsync(nU, ctx->Uw.p, H.level_valid_count(0) * Q * Ns * sizeof(double), cudaMemcpyDeviceToDevice,
                            ctx->stream), "regrid copy level 0");
-  std::vector<int> dst, par, src;
-  std::vector<int8_t> ch;
+  RemapTable rm;
   std::vector<size_t> lo(NH.nlevels() + 1, 0);
   for (int l = 1; l < NH.nlevels(); ++l) {
-    lo[l] = dst.size();
+    lo[l] = rm.dst.size();
     for (size_t e = 0; e < NH.n_elem(); ++e) {
       if (NH.elem_level[e] != l) continue;
       const int* c = &NH.elem_cell[3 * e];
@@ -452,44 +539,40 @@ int regrid(adg_ctx* ctx) {
         int oe = H.elem_at(l, c);
         if (H.is_valid_elem(oe)) old = oe;
       }
-      dst.push_back((int)e);
-      par.push_back(NH.cellmap[l - 1][NH.cidx(l - 1, pc)]);
-      src.push_back(old);
-      ch.push_back((int8_t)child);
+      rm.dst.push_back((int)e);
+      rm.par.push_back(NH.cellmap[l - 1][NH.cidx(l - 1, pc)]);
+      rm.src.push_back(old);
+      rm.ch.push_back((int8_t)child);
     }
   }
-  lo[NH.nlevels()] = dst.size();
-  const size_t nr = dst.size();
-  if (nr) {
-    std::vector<int> packed(3 * nr);
-    std::copy(dst.begin(), dst.end(), packed.begin());
-    std::copy(par.begin(), par.end(), packed.begin() + nr);
-    std::copy(src.begin(), src.end(), packed.begin() + 2 * nr);
-    ADG_CUDA(ctx->remap_i.ensure(3 * nr), "alloc remap");
-    ADG_CUDA(ctx->remap_c.ensure(nr), "alloc remap");
-    ADG_CUDA(cudaMemcpyAsync(ctx->remap_i.p, packed.data(), 3 * nr * 4, cudaMemcpyHostToDevice, ctx->stream), "h2d");
-    ADG_CUDA(cudaMemcpyAsync(ctx->remap_c.p, ch.data(), nr, cudaMemcpyHostToDevice, ctx->stream), "h2d");
-    for (int l = 1; l < NH.nlevels(); ++l) {
-      const size_t o = lo[l], n = lo[l + 1] - lo[l];
-      if (!n) continue;
-      ScatterArgs sa{};
-      sa.Uw = nU;
-      sa.Uw_old = ctx->Uw.p;
-      sa.dst = ctx->remap_i.p + o;
-      sa.parent = ctx->remap_i.p + nr + o;
-      sa.src_old = ctx->remap_i.p + 2 * nr + o;
-      sa.child = ctx->remap_c.p + o;
-      sa.n = (int)n;
-      cudaError_t e = ks->scatter(sa, ctx->stream);
-      if (e != cudaSuccess) return cuda_fail(ctx, e, "regrid remap launch");
-      ctx->launches++;
-    }
-  }
-  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "regrid sync");  // pageable sources above
-  std::swap(ctx->Uw, ctx->Uw_alt);
+  lo[NH.nlevels()] = rm.dst.size();
+  const size_t nr = rm.dst.size();
+  auto t3 = std::chrono::steady_clock::now();
+  ctx->rg_phase_ms[2] += ms_between(t2, t3);
   ctx->hier = std::move(NH);
+  int rc = upload_tables(ctx, &rm);
+  if (rc) return rc;
+  auto t4 = std::chrono::steady_clock::now();
+  ctx->rg_phase_ms[3] += ms_between(t3, t4);
+  for (int l = 1; l < ctx->hier.nlevels(); ++l) {
+    const size_t o = lo[l], n = lo[l + 1] - lo[l];
+    if (!n) continue;
+    ScatterArgs sa{};
+    sa.Uw = nU;
+    sa.Uw_old = ctx->Uw.p;
+    sa.dst = ctx->remap_i.p + o;
+    sa.parent = ctx->remap_i.p + nr + o;
+    sa.src_old = ctx->remap_i.p + 2 * nr + o;
+    sa.child = ctx->remap_c.p + o;
+    sa.n = (int)n;
+    cudaError_t e = ks->scatter(sa, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "regrid remap launch");
+    ctx->launches++;
+  }
+  std::swap(ctx->Uw, ctx->Uw_alt);
   ctx->n_regrids++;
-  return upload_tables(ctx);
+  ctx->rg_phase_ms[4] += ms_between(t4, std::chrono::steady_clock::now());
+  return ADG_OK;
 }
 
 bool regrid_due(const adg_ctx* ctx) {
@@ -548,11 +631,14 @@ int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
     ctx->regrid_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   ctx->dof_updates += (long long)ctx->hier.n_valid() * ctx->ks->Q * ctx->ks->Np_s;
+  ctx->leaf_dof_updates += (long long)ctx->n_leaf * ctx->ks->Q * ctx->ks->Np_s;
   ctx->first_step = false;
   if (use_graph && !ev) {
     if (!ctx->graph_exec || ctx->graph_stale) {
+      auto t0 = std::chrono::steady_clock::now();
       int rc = capture_graph(ctx);
       if (rc) return rc;
+      ctx->rg_phase_ms[5] += ms_between(t0, std::chrono::steady_clock::now());
     }
     ADG_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream), "graph launch");
     ctx->launches += ctx->graph_kernels;
@@ -592,16 +678,18 @@ int adg_ctx_create(const adg_config* cfg, adg_ctx** out) {
     return ADG_ERR_CUDA;
   }
   ctx->own_stream = true;
-  if (ctx->scal.ensure(2) != cudaSuccess || ctx->min_bits.ensure(1) != cudaSuccess || ctx->status.ensure(1) != cudaSuccess) {
+  if (ctx->scal.ensure(kScalCount) != cudaSuccess || ctx->dt_done.ensure(1) != cudaSuccess ||
+      ctx->min_bits.ensure(1) != cudaSuccess || ctx->status.ensure(1) != cudaSuccess) {
     delete ctx;
     return ADG_ERR_CUDA;
   }
-  double z[2] = {0.0, 0.0};
+  double z[kScalCount] = {};
   unsigned long long big = 0;
   double huge = 1.0e300;
   std::memcpy(&big, &huge, sizeof(big));
   unsigned int zero = 0;
   if (cudaMemcpy(ctx->scal.p, z, sizeof(z), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(ctx->dt_done.p, 0, sizeof(unsigned int)) != cudaSuccess ||
       cudaMemcpy(ctx->min_bits.p, &big, sizeof(big), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(ctx->status.p, &zero, sizeof(zero), cudaMemcpyHostToDevice) != cudaSuccess) {
     delete ctx;
@@ -780,7 +868,12 @@ int adg_get_dt(adg_ctx* ctx, double* dt) {
 
 int adg_set_dt(adg_ctx* ctx, double dt) {
   if (!ctx || !(dt > 0.0)) return ADG_ERR_ARG;
+  const LevelGeom g = level_geom(ctx);
+  double blk[3 * kMaxLevels];
+  for (int l = 0; l < kMaxLevels; ++l)
+    for (int d = 0; d < 3; ++d) blk[3 * l + d] = d < ctx->cfg.D ? dt / g.dx[l][d] : 0.0;
   ADG_CUDA(cudaMemcpyAsync(ctx->scal.p, &dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "set_dt");
+  ADG_CUDA(cudaMemcpyAsync(ctx->scal.p + kScalDtDx, blk, sizeof(blk), cudaMemcpyHostToDevice, ctx->stream), "set_dt");
   ADG_CUDA(cudaStreamSynchronize(ctx->stream), "set_dt sync");
   return ADG_OK;
 }
@@ -827,6 +920,18 @@ int adg_advance(adg_ctx* ctx, int nsteps, int use_graph) {
     rc = host_step(ctx, use_graph != 0);
     if (rc) return rc;
   }
+  return ADG_OK;
+}
+
+int adg_leaf_dof_updates(const adg_ctx* ctx, int64_t* total) {
+  if (!ctx || !total) return ADG_ERR_ARG;
+  *total = ctx->leaf_dof_updates;
+  return ADG_OK;
+}
+
+int adg_regrid_profile(const adg_ctx* ctx, double* ms, int n) {
+  if (!ctx || !ms || n < 0) return ADG_ERR_ARG;
+  for (int i = 0; i < n && i < 6; ++i) ms[i] = ctx->rg_phase_ms[i];
   return ADG_OK;
 }
 
@@ -1130,18 +1235,70 @@ __global__ void k_accumulate_count(const int* c, unsigned long long* total) {
 
 // Seeded predictor: network inference, seeded sweeps with residual test,
 // fallback of rejected elements to the full Picard predictor.
-int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base) {
+// Pack the weights for k_seed_infer_tc (hidden width 128 only): each layer
+// as a K-major B operand, at 4 KB aligned offsets.
+int seed_pack_tc(adg_seed* s) {
+  s->packed = false;
+  if (s->h != kSeedTcHidden) return ADG_OK;
+  const int K1 = seed_tc_k1(s->n_in), N4 = seed_tc_n4(s->n_out), H = s->h;
+  const int Kp[4] = {K1, H, H, H}, Np[4] = {H, H, H, N4};
+  const int fin[4] = {s->n_in, H, H, H}, fout[4] = {H, H, H, s->n_out};
+  long long o = 0;
+  for (int L = 0; L < 4; ++L) {
+    s->w_off[L] = o;
+    o += ((long long)Kp[L] * Np[L] + 1023) / 1024 * 1024;
+  }
+  if (s->wpack.ensure((size_t)o) != cudaSuccess) return ADG_ERR_CUDA;
+  for (int L = 0; L < 4; ++L) {
+    const int n = Kp[L] * Np[L];
+    k_seed_pack_tc<<<(n + 255) / 256, 256, 0, s->stream>>>(s->params.p + s->off[2 * L], fin[L], fout[L], Kp[L], Np[L],
+                                                            s->wpack.p + s->w_off[L]);
+  }
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return ADG_ERR_CUDA;
+  s->packed = true;
+  return ADG_OK;
+}
+
+// H_w seeds of every element of the current layout into dst: the fused
+// tensor-core kernel (path 1, when the seed is packed for it) or features +
+// four SGEMMs + assembly (path 0).
+int seed_infer(adg_ctx* ctx, double* dst, int path) {
   adg_seed* sd = ctx->seed;
   const Hierarchy& H = ctx->hier;
   const KernelSet* ks = ctx->ks;
   const int n = (int)H.n_elem();
   cudaStream_t st = ctx->stream;
+  const int8_t* lev = H.nlevels() > 1 ? ctx->elem_level.p : nullptr;
+  const LevelGeom geom = level_geom(ctx);
+  if (path == 1 && sd->packed) {
+    SeedTCArgs ta{};
+    ta.Uw = ctx->Uw.p;
+    ta.n = n;
+    ta.elem_level = lev;
+    ta.geom = geom;
+    ta.dt = ctx->scal.p;
+    ta.wpack = sd->wpack.p;
+    for (int L = 0; L < 4; ++L) {
+      ta.w_off[L] = sd->w_off[L];
+      ta.bias[L] = sd->params.p + sd->off[2 * L + 1];
+    }
+    ta.x_mean = sd->x_mean.p;
+    ta.x_istd = sd->x_istd.p;
+    ta.y_mean = sd->y_mean.p;
+    ta.y_std = sd->y_std.p;
+    ta.Hseed = dst;
+    ta.status = ctx->status.p;
+    cudaError_t e = ks->seed_infer_tc(ta, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "seed inference (tensor cores)");
+    ctx->launches += 1;
+    return ADG_OK;
+  }
   SeedFeatArgs fa{};
   fa.Uw = ctx->Uw.p;
   fa.e0 = 0;
   fa.n = n;
-  fa.elem_level = H.nlevels() > 1 ? ctx->elem_level.p : nullptr;
-  fa.geom = base.geom;
+  fa.elem_level = lev;
+  fa.geom = geom;
   fa.dt = ctx->scal.p;
   fa.x_mean = sd->x_mean.p;
   fa.x_istd = sd->x_istd.p;
@@ -1149,9 +1306,19 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base) {
   cudaError_t e = ks->seed_features(fa, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "seed features");
   seed_forward_infer(sd, ctx->sx.p, n, ctx->sy0.p, ctx->sy1.p, ctx->syo.p, st);
-  e = ks->seed_assemble(ctx->Uw.p, ctx->syo.p, sd->y_mean.p, sd->y_std.p, n, fa.elem_level, base.geom, ctx->scal.p,
-                       ctx->hseed.p, st);
+  e = ks->seed_assemble(ctx->Uw.p, ctx->syo.p, sd->y_mean.p, sd->y_std.p, n, lev, geom, ctx->scal.p, dst, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "seed assemble");
+  ctx->launches += 1 + 4 + 1;  // features, 4 GEMMs, assemble
+  return ADG_OK;
+}
+
+int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base) {
+  const int n = (int)ctx->hier.n_elem();
+  const KernelSet* ks = ctx->ks;
+  cudaStream_t st = ctx->stream;
+  int rc = seed_infer(ctx, ctx->hseed.p, ctx->seed_path);
+  if (rc) return rc;
+  cudaError_t e;
   ADG_CUDA(cudaMemsetAsync(ctx->fb_count.p, 0, sizeof(int), st), "fallback reset");
   PredictorArgs pa = base;
   pa.Hseed = ctx->hseed.p;
@@ -1167,7 +1334,7 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base) {
   e = ks->predictor(fb, ctx->E, st, 0);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "fallback predictor");
   k_accumulate_count<<<1, 32, 0, st>>>(ctx->fb_count.p, ctx->fb_total.p);
-  ctx->launches += 4 + 4 + 1;  // features, 4 GEMMs, assemble, 2 predictors, count
+  ctx->launches += 3;  // 2 predictors, count
   ctx->seed_predicted += n;
   return ADG_OK;
 }
@@ -1220,7 +1387,8 @@ int adg_seed_create(int D, int P, int hidden, uint64_t rng_seed, adg_seed** out)
   cudaMemcpy(s->x_mean.p, zin.data(), zin.size() * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(s->x_istd.p, oin.data(), oin.size() * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(s->y_mean.p, zout.data(), zout.size() * 4, cudaMemcpyHostToDevice);
-  if (cudaMemcpy(s->y_std.p, oout.data(), oout.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+  if (cudaMemcpy(s->y_std.p, oout.data(), oout.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+      seed_pack_tc(s) != ADG_OK) {
     delete s;
     return ADG_ERR_CUDA;
   }
@@ -1384,7 +1552,7 @@ int adg_seed_train(adg_seed* s, int epochs, int batch, double lr, double* last_l
     epoch_loss = l / ((double)s->nsamp * s->n_out);
   }
   if (last_loss) *last_loss = epoch_loss;
-  return ADG_OK;
+  return seed_pack_tc(s);
 }
 
 int adg_seed_forward(adg_seed* s, const float* X, int n, float* Y) {
@@ -1452,7 +1620,8 @@ int adg_seed_set_params(adg_seed* s, const float* in) {
   cudaMemcpy(s->y_mean.p, in + o, s->n_out * 4, cudaMemcpyHostToDevice);
   o += s->n_out;
   s->normalised = true;
-  return cudaMemcpy(s->y_std.p, in + o, s->n_out * 4, cudaMemcpyHostToDevice) == cudaSuccess ? ADG_OK : ADG_ERR_CUDA;
+  if (cudaMemcpy(s->y_std.p, in + o, s->n_out * 4, cudaMemcpyHostToDevice) != cudaSuccess) return ADG_ERR_CUDA;
+  return seed_pack_tc(s);
 }
 
 int adg_seed_attach(adg_ctx* ctx, adg_seed* s, int mode, int sweeps, double tol) {
@@ -1473,6 +1642,24 @@ int adg_seed_attach(adg_ctx* ctx, adg_seed* s, int mode, int sweeps, double tol)
     ctx->seed_predicted = 0;
   }
   ctx->tables_dirty = true;  // resizes the inference buffers, drops the graph
+  return ADG_OK;
+}
+
+int adg_seed_set_path(adg_ctx* ctx, int path) {
+  if (!ctx || path < 0 || path > 1) return ADG_ERR_ARG;
+  ctx->seed_path = path;
+  ctx->graph_stale = true;
+  return ADG_OK;
+}
+
+int adg_seed_infer(adg_ctx* ctx, double* dst_dev, int path) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!dst_dev || path < 0 || path > 1) return fail(ctx, ADG_ERR_ARG, "bad seed inference arguments");
+  if (!ctx->seed) return fail(ctx, ADG_ERR_STATE, "no seed attached");
+  rc = seed_infer(ctx, dst_dev, path);
+  if (rc) return rc;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "seed inference");
   return ADG_OK;
 }
 

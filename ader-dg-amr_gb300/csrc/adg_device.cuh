@@ -93,6 +93,8 @@ __device__ __forceinline__ double euler_flux_normal(int d, const double* u, doub
 #pragma unroll
   for (int k = 1; k < D; ++k) ke = fma(u[k + 1], v[k], ke);
   const double p = floor_limit((gamma - 1.0) * fma(-0.5, ke, u[D + 1]));
+  // 1 / max(rho, floor) from the reciprocal already at hand
+  const double rinv_c = (u[0] < kPdeLimit) ? 1.0 / kPdeLimit : r;
   double vd = v[0], md = u[1];
 #pragma unroll
   for (int k = 1; k < D; ++k)
@@ -104,23 +106,23 @@ __device__ __forceinline__ double euler_flux_normal(int d, const double* u, doub
 #pragma unroll
   for (int k = 0; k < D; ++k) F[k + 1] = (k == d) ? fma(md, v[k], p) : md * v[k];
   F[D + 1] = (u[D + 1] + p) * vd;
-  const double rho_c = (u[0] < kPdeLimit) ? kPdeLimit : u[0];
-  const double c = sqrt(gamma * (p / rho_c));
+  const double c = sqrt(gamma * (p * rinv_c));
   return fabs(vd) + c;
 }
 
 // CFL speed max_d(|u_d/rho| + c) at one point (Compressible_Euler.cpp:57-70).
 template <int D>
 __device__ __forceinline__ double euler_cfl_lambda(const double* u, double gamma) {
+  const double r = 1.0 / u[0];
   double ke = 0.0;
 #pragma unroll
-  for (int d = 0; d < D; ++d) ke += (u[d + 1] * u[d + 1]) / u[0];
+  for (int d = 0; d < D; ++d) ke += (u[d + 1] * u[d + 1]) * r;
   const double p = floor_limit((gamma - 1.0) * (u[D + 1] - 0.5 * ke));
-  const double rho_c = (u[0] < kPdeLimit) ? kPdeLimit : u[0];
-  const double c = sqrt(gamma * (p / rho_c));
-  double lam = fabs(u[1] / u[0]) + c;
+  const double rinv_c = (u[0] < kPdeLimit) ? 1.0 / kPdeLimit : r;
+  const double c = sqrt(gamma * (p * rinv_c));
+  double lam = fabs(u[1] * r) + c;
 #pragma unroll
-  for (int d = 1; d < D; ++d) lam = fmax(lam, fabs(u[d + 1] / u[0]) + c);
+  for (int d = 1; d < D; ++d) lam = fmax(lam, fabs(u[d + 1] * r) + c);
   return lam;
 }
 

@@ -82,20 +82,14 @@ struct Impl final : KernelSet {
     return cudaGetLastError();
   }
   cudaError_t dt_reduce(const DtArgs& a, cudaStream_t s) const override {
-    const int bs = 256;
+    const int bs = 64;
     k_dt_reduce<O><<<(a.n_valid + bs - 1) / bs, bs, 0, s>>>(a);
-    return cudaGetLastError();
-  }
-  cudaError_t reflux(const RefluxArgs& a, cudaStream_t s) const override {
-    const long long n = (long long)a.nrec * O::Q;
-    if (n == 0) return cudaSuccess;
-    k_reflux<O><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
     return cudaGetLastError();
   }
   cudaError_t average_down(double* Uw, const int* rec, int nrec, cudaStream_t s) const override {
     const long long n = (long long)nrec * O::Q;
     if (n == 0) return cudaSuccess;
-    k_average_down<O><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(Uw, rec, nrec);
+    k_average_down<O><<<(unsigned)((n + 31) / 32), dim3(32, 1 << O::D), 0, s>>>(Uw, rec, nrec);
     return cudaGetLastError();
   }
   cudaError_t scatter(const ScatterArgs& a, cudaStream_t s) const override {
@@ -128,6 +122,18 @@ struct Impl final : KernelSet {
     if (t == 0) return cudaSuccess;
     k_seed_assemble<O><<<(unsigned)((t + 127) / 128), 128, 0, s>>>(Uw, Y, y_mean, y_std, n, elem_level, geom, dt,
                                                                     Hseed);
+    return cudaGetLastError();
+  }
+  cudaError_t seed_infer_tc(const SeedTCArgs& a, cudaStream_t s) const override {
+    if (a.n <= 0) return cudaSuccess;
+    static bool attr = false;
+    if (!attr) {
+      cudaError_t e =
+          cudaFuncSetAttribute(k_seed_infer_tc<O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSeedTcSmem);
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+    k_seed_infer_tc<O><<<(a.n + kSeedTcRows - 1) / kSeedTcRows, kSeedTcThreads, kSeedTcSmem, s>>>(a);
     return cudaGetLastError();
   }
   cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const override {

@@ -23,13 +23,19 @@ struct LevelGeom {
   double dx[kMaxLevels][3];
 };
 
+// Device scalar block of a context: [0] Dt, [1] t, then Dt/dx_d of level l at
+// kScalDtDx + 3 l + d, refreshed whenever Dt changes so that the element
+// kernels read the ratios instead of dividing per thread.
+constexpr int kScalDtDx = 2;
+constexpr int kScalCount = kScalDtDx + 3 * kMaxLevels;
+
 struct PredictorArgs {
   const double* Uw;
   int n_elem;                 // elements that need a predictor (valid + ghost)
   const int8_t* elem_level;   // nullptr: all level 0
   LevelGeom geom;
   double gamma;
-  const double* dt;           // device scalar
+  const double* dt;           // device scalar block (Dt, t, Dt/dx)
   int sweeps;
   double* Rvol;
   double* Tr;
@@ -96,6 +102,33 @@ __device__ __forceinline__ void picard_sweep(const double* hw, const double* wu,
   __syncthreads();
 }
 
+// One Picard sweep entirely in FP32 (the seeded path's sweeps): H = V hw,
+// F_d = f_d(H), and only the change dlt = -sum_d c_d A_d F_d is returned, so
+// that the caller forms H_w' = W U + dlt in the precision it needs.
+template <class O, int E>
+__device__ __forceinline__ void picard_sweep_f32(const float* hw, const float* c, float* sm, int col, float gm1,
+                                                 float* dlt) {
+  constexpr int D = O::D, NP_ST = O::NP_ST, NQ = O::NQ_ST;
+  constexpr int LD = E * O::Q + 1;
+  O::template vol_eval<float>(RegInT<float>{hw}, ColOutT<float>{sm + col, LD});
+  __syncthreads();
+  flux_stage<O, E, NQ, float>(sm, LD, gm1);
+  __syncthreads();
+  float y[NP_ST];
+  O::template proj<0, float>(ColInT<float>{sm + col, LD}, RegOutT<float>{y});
+#pragma unroll
+  for (int n = 0; n < NP_ST; ++n) dlt[n] = -c[0] * y[n];
+  O::template proj<1, float>(ColInT<float>{sm + NQ * LD + col, LD}, RegOutT<float>{y});
+#pragma unroll
+  for (int n = 0; n < NP_ST; ++n) dlt[n] = fmaf(-c[1], y[n], dlt[n]);
+  if constexpr (D == 3) {
+    O::template proj<2, float>(ColInT<float>{sm + 2 * NQ * LD + col, LD}, RegOutT<float>{y});
+#pragma unroll
+    for (int n = 0; n < NP_ST; ++n) dlt[n] = fmaf(-c[2], y[n], dlt[n]);
+  }
+  __syncthreads();
+}
+
 // MODE 0: plain FP64 Picard (the reference's initial guess, P sweeps);
 // MODE 1 / 2: seeded, `sweeps` sweeps from the learned seed in FP64 / FP32,
 // the first one judging the seed by its residual.
@@ -120,10 +153,9 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   }
   const int e = live ? e_raw : (a.elem_list ? e_raw : (a.n_elem - 1));
   const int lev = a.elem_level ? a.elem_level[e] : 0;
-  const double dt = *a.dt;
   double c[D];
 #pragma unroll
-  for (int d = 0; d < D; ++d) c[d] = dt / a.geom.dx[lev][d];
+  for (int d = 0; d < D; ++d) c[d] = a.dt[kScalDtDx + 3 * lev + d];
   const double gm1 = a.gamma - 1.0;
 
   double u[NP_S];
@@ -187,20 +219,40 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
     // first sweep's change judges the seed (residual relative to the
     // element's largest cell mean), failures go to the fallback list.
     const double* hs = a.Hseed + ((size_t)e * Q + q) * NP_ST;
-#pragma unroll
-    for (int n = 0; n < NP_ST; ++n) hw[n] = hs[n];
     double res = 0.0;
-    for (int s = 0; s < a.sweeps; ++s) {
-      double nw[NP_ST];
-      if constexpr (MODE == 1)
+    if constexpr (MODE == 1) {
+#pragma unroll
+      for (int n = 0; n < NP_ST; ++n) hw[n] = hs[n];
+      for (int s = 0; s < a.sweeps; ++s) {
+        double nw[NP_ST];
         picard_sweep<O, E, double>(hw, wu, c, sm, col, gm1, nw);
-      else
-        picard_sweep<O, E, float>(hw, wu, c, reinterpret_cast<float*>(sm), col, gm1, nw);
-      if (s == 0)
+        if (s == 0)
 #pragma unroll
-        for (int n = 0; n < NP_ST; ++n) res = fmax(res, fabs(nw[n] - hw[n]));
+          for (int n = 0; n < NP_ST; ++n) res = fmax(res, fabs(nw[n] - hw[n]));
 #pragma unroll
-      for (int n = 0; n < NP_ST; ++n) hw[n] = nw[n];
+        for (int n = 0; n < NP_ST; ++n) hw[n] = nw[n];
+      }
+    } else {
+      // FP32 sweeps on a float copy; the final H_w = W U + dlt in FP64
+      float hf[NP_ST], wf[NP_ST], dlt[NP_ST], cf[D];
+#pragma unroll
+      for (int n = 0; n < NP_ST; ++n) hf[n] = (float)hs[n];
+      O::template wu<float>(RegIn{u}, RegOutT<float>{wf});
+#pragma unroll
+      for (int d = 0; d < D; ++d) cf[d] = (float)c[d];
+      float resf = 0.0f;
+      for (int s = 0; s < a.sweeps; ++s) {
+        picard_sweep_f32<O, E>(hf, cf, reinterpret_cast<float*>(sm), col, (float)gm1, dlt);
+#pragma unroll
+        for (int n = 0; n < NP_ST; ++n) {
+          const float nf = wf[n] + dlt[n];
+          if (s == 0) resf = fmaxf(resf, fabsf(nf - hf[n]));
+          hf[n] = nf;
+        }
+      }
+      res = (double)resf;
+#pragma unroll
+      for (int n = 0; n < NP_ST; ++n) hw[n] = a.sweeps > 0 ? wu[n] + (double)dlt[n] : hs[n];
     }
     // per-element reduction over its Q columns through shared memory
     double* red = sm;
@@ -326,6 +378,42 @@ __global__ void k_numflux(FaceArgs a) {
   }
 }
 
+// Runtime child / face index dispatch to the compile-time generated
+// coarse-fine operators.
+template <class O, class In, class Out>
+__device__ __forceinline__ void pcf_rt(int l, const In& in, Out out) {
+  switch (l) {
+    case 0: O::template pcf<0>(in, out); break;
+    case 1: O::template pcf<1>(in, out); break;
+    case 2: O::template pcf<2>(in, out); break;
+    case 3: O::template pcf<3>(in, out); break;
+    default:
+      if constexpr (O::D == 3) {
+        switch (l) {
+          case 4: O::template pcf<4>(in, out); break;
+          case 5: O::template pcf<5>(in, out); break;
+          case 6: O::template pcf<6>(in, out); break;
+          default: O::template pcf<7>(in, out); break;
+        }
+      }
+  }
+}
+
+template <class O, int DD, int S, class In, class Out>
+__device__ __forceinline__ void pflux_k(int k, const In& in, Out out) {
+  if constexpr (O::D == 2) {
+    if (k == 0) O::template pflux<DD, S, 0>(in, out);
+    else O::template pflux<DD, S, 1>(in, out);
+  } else {
+    switch (k) {
+      case 0: O::template pflux<DD, S, 0>(in, out); break;
+      case 1: O::template pflux<DD, S, 1>(in, out); break;
+      case 2: O::template pflux<DD, S, 2>(in, out); break;
+      default: O::template pflux<DD, S, 3>(in, out); break;
+    }
+  }
+}
+
 // Corrector update of the valid elements (AmrDG.tpp:711-738):
 // U_w = (Rvol - sum_d (Dt/dx_d) (Mkbdp[d] Fnum_hi - Mkbdm[d] Fnum_lo)) / M.
 struct CorrectorArgs {
@@ -337,7 +425,68 @@ struct CorrectorArgs {
   const int8_t* elem_level;
   LevelGeom geom;
   const double* dt;
+  // coarse-fine flux corrections applied after the update (nullptr: none):
+  // record of element e = rec_of_elem[e] (-1: none), its face entries
+  // rec_off[r] .. rec_off[r+1]
+  const int* rec_of_elem;
+  const int* rec_off;
+  const int* ent_face;
+  const int8_t* ent_dside;
+  const int* ent_fine;
 };
+
+// Coarse-fine flux correction of one coarse element (FluxRegister CrseAdd /
+// FineAdd / Reflux + L2ProjInterp::reflux, AmrDG.h:1138-1161,
+// AmrDG_Interpolater.tpp:7-72):
+//   corr = sum_faces sgn * (J_c Mkbd Fnum_c - sum_k J_f P_flux[k] Fnum_f[k]),
+//   U_c += (2^D / vol_c) Minv corr,  sgn = +1 on the coarse cell's high face.
+template <class O>
+__device__ __forceinline__ void reflux_add(const CorrectorArgs& a, int r, int lc, int q, double* u) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NB = O::NQ_BD, NFC = 1 << (D - 1);
+  const double dt = a.dt[0];
+  double corr[NP_S];
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) corr[n] = 0.0;
+  for (int x = a.rec_off[r]; x < a.rec_off[r + 1]; ++x) {
+    const int ds = a.ent_dside[x];
+    const int d = ds >> 1, side = ds & 1;
+    double area_c = 1.0, area_f = 1.0;
+    for (int k = 0; k < D; ++k)
+      if (k != d) {
+        area_c *= a.geom.dx[lc][k];
+        area_f *= a.geom.dx[lc + 1][k];
+      }
+    const double Jc = (dt / 2.0) * (area_c / (double)NFC);
+    const double Jf = (dt / 2.0) * (area_f / (double)NFC);
+    double fc[NP_S], ff[NP_S], tmp[NP_S];
+    const double* fnc = a.Fnum + ((size_t)a.ent_face[x] * Q + q) * NB;
+#define ADG_FC(DD, SS) O::template bd_term<DD, SS>(RegIn{fnc}, RegOut{fc})
+    if (d == 0) { if (side) ADG_FC(0, 1); else ADG_FC(0, 0); }
+    else if (d == 1) { if (side) ADG_FC(1, 1); else ADG_FC(1, 0); }
+    else if constexpr (D == 3) { if (side) ADG_FC(2, 1); else ADG_FC(2, 0); }
+#undef ADG_FC
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) ff[n] = 0.0;
+    for (int k = 0; k < NFC; ++k) {
+      const double* fnf = a.Fnum + ((size_t)a.ent_fine[(size_t)x * NFC + k] * Q + q) * NB;
+#define ADG_FF(DD, SS) pflux_k<O, DD, SS>(k, RegIn{fnf}, RegOut{tmp})
+      if (d == 0) { if (side) ADG_FF(0, 1); else ADG_FF(0, 0); }
+      else if (d == 1) { if (side) ADG_FF(1, 1); else ADG_FF(1, 0); }
+      else if constexpr (D == 3) { if (side) ADG_FF(2, 1); else ADG_FF(2, 0); }
+#undef ADG_FF
+#pragma unroll
+      for (int n = 0; n < NP_S; ++n) ff[n] += tmp[n];
+    }
+    const double sgn = side ? 1.0 : -1.0;
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) corr[n] += sgn * (Jc * fc[n] - Jf * ff[n]);
+  }
+  double vol = 1.0;
+  for (int k = 0; k < D; ++k) vol *= a.geom.dx[lc][k];
+  const double inv_jac = (double)(1 << D) / vol;
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) u[n] += inv_jac * (O::minv(n) * corr[n]);
+}
 
 template <class O>
 __global__ void k_corrector(CorrectorArgs a) {
@@ -347,7 +496,6 @@ __global__ void k_corrector(CorrectorArgs a) {
   const int e = (int)(t / Q);
   const int q = (int)(t % Q);
   const int lev = a.elem_level ? a.elem_level[e] : 0;
-  const double dt = *a.dt;
   double R[NP_S];
   const double* rv = a.Rvol + ((size_t)e * Q + q) * NP_S;
 #pragma unroll
@@ -356,7 +504,7 @@ __global__ void k_corrector(CorrectorArgs a) {
   const int* ef = a.elem_face + (size_t)e * NF;
 #define ADG_BD(DD)                                                                      \
   {                                                                                     \
-    const double cd = dt / a.geom.dx[lev][DD];                                          \
+    const double cd = a.dt[kScalDtDx + 3 * lev + DD];                                  \
     const double* flo = a.Fnum + ((size_t)ef[2 * DD + 0] * Q + q) * NB;                 \
     const double* fhi = a.Fnum + ((size_t)ef[2 * DD + 1] * Q + q) * NB;                 \
     O::template bd_term<DD, 1>(RegIn{fhi}, RegOut{bp});                                 \
@@ -367,9 +515,15 @@ __global__ void k_corrector(CorrectorArgs a) {
   ADG_BD(1)
   if constexpr (D == 3) ADG_BD(2)
 #undef ADG_BD
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) R[n] = R[n] * O::minv(n);
+  if (a.rec_of_elem) {
+    const int r = a.rec_of_elem[e];
+    if (r >= 0) reflux_add<O>(a, r, lev, q, R);
+  }
   double* dst = a.Uw + ((size_t)e * Q + q) * NP_S;
 #pragma unroll
-  for (int n = 0; n < NP_S; ++n) dst[n] = R[n] * O::minv(n);
+  for (int n = 0; n < NP_S; ++n) dst[n] = R[n];
 }
 
 // Time step (AmrDG.h:1253-1357): dt_cell = CFL * dx_avg / lambda(U at spatial
@@ -383,6 +537,14 @@ struct DtArgs {
   double gamma;
   unsigned long long* min_bits;
   unsigned int* status;
+  // finalisation by the last block: Dt = c_dt * min, t += old Dt when
+  // advance_time, Dt/dx of every level; min_bits and done reset
+  double* scal;
+  unsigned int* done;
+  double c_dt;
+  int advance_time;
+  int D;
+  LevelGeom geom;
 };
 
 template <class O>
@@ -420,6 +582,24 @@ __global__ void k_dt_reduce(DtArgs a) {
     if (lane == 0) atomicMin(a.min_bits, (unsigned long long)__double_as_longlong(v));
   }
   if (st) atomicOr(a.status, st);
+  // the last block to finish publishes Dt (threadFenceReduction pattern)
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(a.done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    const unsigned long long bits = atomicAdd(a.min_bits, 0ull);
+    const double dt = a.c_dt * __longlong_as_double((long long)bits);
+    if (a.advance_time) a.scal[1] += a.scal[0];
+    a.scal[0] = dt;
+    for (int l = 0; l < kMaxLevels; ++l)
+      for (int d = 0; d < 3; ++d) a.scal[kScalDtDx + 3 * l + d] = d < a.D ? dt / a.geom.dx[l][d] : 0.0;
+    *a.min_bits = (unsigned long long)__double_as_longlong(1.0e300);
+    *a.done = 0u;
+  }
 }
 
 // L2 projection of the initial condition at the spatial GL points
@@ -483,135 +663,50 @@ __global__ void k_init_ic(ICArgs a) {
 // One thread per (element, variable) column; runtime child / face indices are
 // dispatched to the compile-time generated operators.
 // ===========================================================================
-template <class O, class In, class Out>
-__device__ __forceinline__ void pcf_rt(int l, const In& in, Out out) {
-  switch (l) {
-    case 0: O::template pcf<0>(in, out); break;
-    case 1: O::template pcf<1>(in, out); break;
-    case 2: O::template pcf<2>(in, out); break;
-    case 3: O::template pcf<3>(in, out); break;
-    default:
-      if constexpr (O::D == 3) {
-        switch (l) {
-          case 4: O::template pcf<4>(in, out); break;
-          case 5: O::template pcf<5>(in, out); break;
-          case 6: O::template pcf<6>(in, out); break;
-          default: O::template pcf<7>(in, out); break;
-        }
-      }
-  }
-}
-
-template <class O, int DD, int S, class In, class Out>
-__device__ __forceinline__ void pflux_k(int k, const In& in, Out out) {
-  if constexpr (O::D == 2) {
-    if (k == 0) O::template pflux<DD, S, 0>(in, out);
-    else O::template pflux<DD, S, 1>(in, out);
-  } else {
-    switch (k) {
-      case 0: O::template pflux<DD, S, 0>(in, out); break;
-      case 1: O::template pflux<DD, S, 1>(in, out); break;
-      case 2: O::template pflux<DD, S, 2>(in, out); break;
-      default: O::template pflux<DD, S, 3>(in, out); break;
-    }
-  }
-}
-
-// Coarse-fine flux correction (FluxRegister CrseAdd/FineAdd/Reflux +
-// L2ProjInterp::reflux, AmrDG.h:1138-1161, AmrDG_Interpolater.tpp:7-72):
-//   corr = sum_faces sgn * (J_c Mkbd Fnum_c - sum_k J_f P_flux[k] Fnum_f[k]),
-//   U_c += (2^D / vol_c) Minv corr,  sgn = +1 on the coarse cell's high face.
-struct RefluxArgs {
-  double* Uw;
-  const double* Fnum;
-  const int* rec_elem;
-  const int* rec_off;
-  const int* ent_face;
-  const int8_t* ent_dside;
-  const int* ent_fine;
-  const int8_t* elem_level;
-  int nrec;
-  LevelGeom geom;
-  const double* dt;
-};
-
-template <class O>
-__global__ void k_reflux(RefluxArgs a) {
-  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NB = O::NQ_BD, NFC = 1 << (D - 1);
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)a.nrec * Q) return;
-  const int r = (int)(t / Q), q = (int)(t % Q);
-  const int e = a.rec_elem[r];
-  const int lc = a.elem_level[e];
-  const double dt = *a.dt;
-  double corr[NP_S];
-#pragma unroll
-  for (int n = 0; n < NP_S; ++n) corr[n] = 0.0;
-  for (int x = a.rec_off[r]; x < a.rec_off[r + 1]; ++x) {
-    const int ds = a.ent_dside[x];
-    const int d = ds >> 1, side = ds & 1;
-    double area_c = 1.0, area_f = 1.0;
-    for (int k = 0; k < D; ++k)
-      if (k != d) {
-        area_c *= a.geom.dx[lc][k];
-        area_f *= a.geom.dx[lc + 1][k];
-      }
-    const double Jc = (dt / 2.0) * (area_c / (double)NFC);
-    const double Jf = (dt / 2.0) * (area_f / (double)NFC);
-    double fc[NP_S], ff[NP_S], tmp[NP_S];
-    const double* fnc = a.Fnum + ((size_t)a.ent_face[x] * Q + q) * NB;
-#define ADG_FC(DD, SS) O::template bd_term<DD, SS>(RegIn{fnc}, RegOut{fc})
-    if (d == 0) { if (side) ADG_FC(0, 1); else ADG_FC(0, 0); }
-    else if (d == 1) { if (side) ADG_FC(1, 1); else ADG_FC(1, 0); }
-    else if constexpr (D == 3) { if (side) ADG_FC(2, 1); else ADG_FC(2, 0); }
-#undef ADG_FC
-#pragma unroll
-    for (int n = 0; n < NP_S; ++n) ff[n] = 0.0;
-    for (int k = 0; k < NFC; ++k) {
-      const double* fnf = a.Fnum + ((size_t)a.ent_fine[(size_t)x * NFC + k] * Q + q) * NB;
-#define ADG_FF(DD, SS) pflux_k<O, DD, SS>(k, RegIn{fnf}, RegOut{tmp})
-      if (d == 0) { if (side) ADG_FF(0, 1); else ADG_FF(0, 0); }
-      else if (d == 1) { if (side) ADG_FF(1, 1); else ADG_FF(1, 0); }
-      else if constexpr (D == 3) { if (side) ADG_FF(2, 1); else ADG_FF(2, 0); }
-#undef ADG_FF
-#pragma unroll
-      for (int n = 0; n < NP_S; ++n) ff[n] += tmp[n];
-    }
-    const double sgn = side ? 1.0 : -1.0;
-#pragma unroll
-    for (int n = 0; n < NP_S; ++n) corr[n] += sgn * (Jc * fc[n] - Jf * ff[n]);
-  }
-  double vol = 1.0;
-  for (int k = 0; k < D; ++k) vol *= a.geom.dx[lc][k];
-  const double inv_jac = (double)(1 << D) / vol;
-  double* u = a.Uw + ((size_t)e * Q + q) * NP_S;
-#pragma unroll
-  for (int n = 0; n < NP_S; ++n) u[n] += inv_jac * (O::minv(n) * corr[n]);
-}
-
 // average_down / amr_gather (AmrDG_Interpolater.tpp:283-342, 366-398):
 // u_c = 2^-D Minv sum_l P_fc[l] u_f[l].  rec: coarse, fine_0 .. fine_{2^D-1}.
+// Block (32, 2^D): warp l projects child l of 32 (record, variable) pairs, so
+// every warp runs one operator; warp 0 sums the children in order.
 template <class O>
 __global__ void k_average_down(double* Uw, const int* rec, int nrec) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NOV = 1 << D;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nrec * Q) return;
-  const int r = (int)(t / Q), q = (int)(t % Q);
+  __shared__ double part[NOV][NP_S][33];
+  const int L = threadIdx.y;
+  const long long t = (long long)blockIdx.x * 32 + threadIdx.x;
+  const bool live = t < (long long)nrec * Q;
+  const int r = live ? (int)(t / Q) : 0, q = live ? (int)(t % Q) : 0;
   const int* rr = rec + (size_t)r * (NOV + 1);
-  double sum[NP_S], tmp[NP_S];
+  double tmp[NP_S];
+  if (live) {
+    const double* uf = Uw + ((size_t)rr[1 + L] * Q + q) * NP_S;
+    switch (L) {
+      case 0: O::template pfc<0>(RegIn{uf}, RegOut{tmp}); break;
+      case 1: O::template pfc<1>(RegIn{uf}, RegOut{tmp}); break;
+      case 2: O::template pfc<2>(RegIn{uf}, RegOut{tmp}); break;
+      case 3: O::template pfc<3>(RegIn{uf}, RegOut{tmp}); break;
+      default:
+        if constexpr (D == 3) {
+          switch (L) {
+            case 4: O::template pfc<4>(RegIn{uf}, RegOut{tmp}); break;
+            case 5: O::template pfc<5>(RegIn{uf}, RegOut{tmp}); break;
+            case 6: O::template pfc<6>(RegIn{uf}, RegOut{tmp}); break;
+            default: O::template pfc<7>(RegIn{uf}, RegOut{tmp}); break;
+          }
+        }
+    }
 #pragma unroll
-  for (int n = 0; n < NP_S; ++n) sum[n] = 0.0;
-#define ADG_G(L)                                                                      \
-  {                                                                                   \
-    O::template pfc<L>(RegIn{Uw + ((size_t)rr[1 + L] * Q + q) * NP_S}, RegOut{tmp});  \
-    _Pragma("unroll") for (int n = 0; n < NP_S; ++n) sum[n] += tmp[n];                \
+    for (int n = 0; n < NP_S; ++n) part[L][n][threadIdx.x] = tmp[n];
   }
-  ADG_G(0) ADG_G(1) ADG_G(2) ADG_G(3)
-  if constexpr (D == 3) { ADG_G(4) ADG_G(5) ADG_G(6) ADG_G(7) }
-#undef ADG_G
+  __syncthreads();
+  if (L != 0 || !live) return;
   double* uc = Uw + ((size_t)rr[0] * Q + q) * NP_S;
 #pragma unroll
-  for (int n = 0; n < NP_S; ++n) uc[n] = (1.0 / NOV) * (O::minv(n) * sum[n]);
+  for (int n = 0; n < NP_S; ++n) {
+    double sum = 0.0;
+#pragma unroll
+    for (int l = 0; l < NOV; ++l) sum += part[l][n][threadIdx.x];
+    uc[n] = (1.0 / NOV) * (O::minv(n) * sum);
+  }
 }
 
 // Coarse -> fine projection (amr_scatter, AmrDG_Interpolater.tpp:344-364)
@@ -731,10 +826,10 @@ __global__ void k_seed_features(SeedFeatArgs a) {
   if (f < Q * NP_S) {
     // the Euler flux is homogeneous of degree one in U: scale by the cell
     // mean density so the network sees density-free states
-    v = a.Uw[(size_t)e * Q * NP_S + f] / a.Uw[(size_t)e * Q * NP_S];
+    v = a.Uw[(size_t)e * Q * NP_S + f] * (1.0 / a.Uw[(size_t)e * Q * NP_S]);
   } else {
     const int lev = a.elem_level ? a.elem_level[e] : 0;
-    v = *a.dt / a.geom.dx[lev][0];
+    v = a.dt[kScalDtDx + 3 * lev];
   }
   float x = (float)v;
   if (a.x_mean) x = (x - a.x_mean[f]) * a.x_istd[f];
@@ -754,7 +849,7 @@ __global__ void k_seed_targets(SeedFeatArgs a) {
   float* out = a.T + (size_t)i * Q * NP_ST + q * NP_ST;
   // the predictor's change over the step, per unit density and Dt/dx
   const int lev = a.elem_level ? a.elem_level[e] : 0;
-  const double scale = a.Uw[(size_t)e * Q * NP_S] * (*a.dt / a.geom.dx[lev][0]);
+  const double scale = a.Uw[(size_t)e * Q * NP_S] * a.dt[kScalDtDx + 3 * lev];
 #pragma unroll
   for (int n = 0; n < NP_ST; ++n) out[n] = (float)((h[n] - wu[n]) / scale);
 }
@@ -770,7 +865,7 @@ __global__ void k_seed_assemble(const double* Uw, const float* Y, const float* y
   double wu[NP_ST];
   O::wu(RegIn{Uw + ((size_t)e * Q + q) * NP_S}, RegOut{wu});
   const int lev = elem_level ? elem_level[e] : 0;
-  const double scale = Uw[(size_t)e * Q * NP_S] * (*dt / geom.dx[lev][0]);
+  const double scale = Uw[(size_t)e * Q * NP_S] * dt[kScalDtDx + 3 * lev];
   const float* y = Y + (size_t)e * Q * NP_ST + q * NP_ST;
   double* h = Hseed + ((size_t)e * Q + q) * NP_ST;
 #pragma unroll

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "adg_kernels.cuh"
+#include "adg_seed_tc.cuh"
 
 namespace adg {
 
@@ -21,7 +22,6 @@ struct KernelSet {
   virtual cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t dt_reduce(const DtArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const = 0;
-  virtual cudaError_t reflux(const RefluxArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t average_down(double* Uw, const int* rec, int nrec, cudaStream_t s) const = 0;
   virtual cudaError_t scatter(const ScatterArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t tag(const TagArgs& a, cudaStream_t s) const = 0;
@@ -30,6 +30,7 @@ struct KernelSet {
   virtual cudaError_t seed_assemble(const double* Uw, const float* Y, const float* y_mean, const float* y_std, int n,
                                     const int8_t* elem_level, const LevelGeom& geom, const double* dt, double* Hseed,
                                     cudaStream_t s) const = 0;
+  virtual cudaError_t seed_infer_tc(const SeedTCArgs& a, cudaStream_t s) const = 0;
 };
 
 const KernelSet* kernels_D2P1();

@@ -44,11 +44,15 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // Step size and the periodic face tables, written into the scratch on every
 // call (the scratch keeps the previous call's contents, which are never read).
-__global__ void k_noalloc_setup(int D, int nx, int ny, int nz, double dt, double* dt_slot, int* face_left,
-                                int* face_right, int* elem_face) {
+__global__ void k_noalloc_setup(int D, int nx, int ny, int nz, double dt, LevelGeom g, double* dt_slot,
+                                int* face_left, int* face_right, int* elem_face) {
   const long long n = (long long)nx * ny * nz;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t == 0) *dt_slot = dt;
+  if (t == 0) {  // the scalar block the element kernels read: Dt, t, Dt/dx of level 0
+    dt_slot[0] = dt;
+    dt_slot[1] = 0.0;
+    for (int d = 0; d < 3; ++d) dt_slot[kScalDtDx + d] = d < D ? dt / g.dx[0][d] : 0.0;
+  }
   if (t >= n) return;
   const int e = (int)t;
   const int i = e % nx, j = (e / nx) % ny, k = e / (nx * ny);
@@ -89,7 +93,7 @@ extern "C" int adg_ader_step_noalloc(int D, int P, const int n_cell[3], const do
   const size_t nface = (size_t)D * (size_t)n;
   size_t off = 0;
   const size_t o_dt = off;
-  off = align256(off + sizeof(double));
+  off = align256(off + kScalCount * sizeof(double));
   const size_t o_fl = off;
   off = align256(off + nface * sizeof(int));
   const size_t o_fr = off;
@@ -114,15 +118,15 @@ extern "C" int adg_ader_step_noalloc(int D, int P, const int n_cell[3], const do
   int* face_right = (int*)(base + o_fr);
   int* elem_face = (int*)(base + o_ef);
 
-  const int nx = n_cell[0], ny = D > 1 ? n_cell[1] : 1, nz = D > 2 ? n_cell[2] : 1;
-  k_noalloc_setup<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(D, nx, ny, nz, dt, dt_slot, face_left, face_right,
-                                                               elem_face);
-  if (cudaGetLastError() != cudaSuccess) return ADG_ERR_CUDA;
-
   LevelGeom g{};
   for (int l = 0; l < kMaxLevels; ++l)
     for (int d = 0; d < 3; ++d)
       g.dx[l][d] = d < D ? (prob_hi[d] - prob_lo[d]) / (double)(n_cell[d] << l) : 1.0;
+
+  const int nx = n_cell[0], ny = D > 1 ? n_cell[1] : 1, nz = D > 2 ? n_cell[2] : 1;
+  k_noalloc_setup<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(D, nx, ny, nz, dt, g, dt_slot, face_left, face_right,
+                                                               elem_face);
+  if (cudaGetLastError() != cudaSuccess) return ADG_ERR_CUDA;
 
   PredictorArgs pa{};
   pa.Uw = U_w;

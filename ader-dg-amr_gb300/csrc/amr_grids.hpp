@@ -36,6 +36,11 @@ struct IBox {
     for (int d = 0; d < D; ++d) v *= (long long)(hi[d] - lo[d] + 1);
     return v;
   }
+  bool operator==(const IBox& o) const {
+    for (int d = 0; d < 3; ++d)
+      if (lo[d] != o.lo[d] || hi[d] != o.hi[d]) return false;
+    return true;
+  }
   bool contains(int D, const int* c) const {
     for (int d = 0; d < D; ++d)
       if (c[d] < lo[d] || c[d] > hi[d]) return false;

@@ -259,10 +259,26 @@ def l2_density_level0(Ua, Ub, w):
     return (integral / vol) ** 0.5
 
 
-def train_seed(G, w, n_pairs=2_000_000, epochs=40):
+SEED_VARIANTS = {"seed_1sweep_fp64": dict(mode=1, sweeps=1),
+                 "seed_2sweeps_fp32": dict(mode=2, sweeps=2),
+                 "seed_3sweeps_fp32": dict(mode=2, sweeps=3)}
+
+
+def seed_cache_path(name):
+    return os.path.join(ROOT, "ader-dg-amr_gb300", "_build", f"seed_{name}.npy")
+
+
+def train_seed(G, w, n_pairs=2_000_000, epochs=40, cache=None):
     """Learned seed trained on pairs from the Picard predictor (8 sweeps) of
-    perturbed single-level and AMR runs of the workload's configuration."""
+    perturbed single-level and AMR runs of the workload's configuration.
+    With `cache` (a file path), reuse the parameters stored there by an
+    earlier run of the same workload, or store them after training."""
+    import numpy as np
+
     seed = G.PredictorSeed(w["D"], w["P"], hidden=128, rng_seed=2024)
+    if cache and os.path.exists(cache):
+        seed.set_params(np.load(cache))
+        return seed, {"cached": cache}
     t0 = time.perf_counter()
     runs = []
     base = dict(w)
@@ -285,6 +301,9 @@ def train_seed(G, w, n_pairs=2_000_000, epochs=40):
     loss = seed.train(epochs, batch=8192, lr=1e-3)
     loss = seed.train(epochs // 2, batch=8192, lr=2e-4)
     t2 = time.perf_counter()
+    if cache:
+        os.makedirs(os.path.dirname(cache), exist_ok=True)
+        np.save(cache, seed.get_params())
     return seed, {"pairs": seed.num_samples(), "collect_s": t1 - t0, "train_s": t2 - t1, "final_loss": loss,
                   "epochs": epochs + epochs // 2}
 
@@ -296,13 +315,17 @@ def timed_run(G, w, E, steps, warmup, seed=None, mode=0, sweeps=0, tol=1e-3, pla
     s.advance(warmup, use_graph=True)
     s.Dt  # sync
     d0, _ = s.dof_updates()
+    lf0 = s.leaf_dof_updates()
     n0 = s.launch_count()
     r0 = s.regrid_count()
     _, rms0 = s.dof_updates()
+    ph0 = s.regrid_profile()
     ms = s.advance_timed(steps, use_graph=True)
     d1, rms = s.dof_updates()
+    ph1 = s.regrid_profile()
     out = {"ms": ms, "dof": d1 - d0, "launches": s.launch_count() - n0, "regrids": s.regrid_count() - r0,
-           "regrid_ms": rms - rms0, "sim": s, "dof_per_s": (d1 - d0) / (ms * 1e-3)}
+           "regrid_host_ms": {k: ph1[k] - ph0[k] for k in ph1}, "sim": s, "dof_per_s": (d1 - d0) / (ms * 1e-3),
+           "leaf_dof_per_s": (s.leaf_dof_updates() - lf0) / (ms * 1e-3)}
     if seed is not None and mode:
         fb, n = G.seed_stats(s)
         out["fallback_rate"] = fb / max(1, n)
@@ -341,8 +364,17 @@ def run_ours(args, w):
     seed = None
     seed_info = None
     is_amr = "amr" in w
-    if is_amr and not args.no_seed:
-        seed, seed_info = train_seed(G, w)
+    only = args.only
+    if is_amr and not args.no_seed and only != "plain_fp64":
+        seed, seed_info = train_seed(G, w, cache=seed_cache_path(args.workload) if args.seed_cache else None)
+    if only:  # one variant, for profiling: no accuracy reference, no JSON contract line
+        kw = SEED_VARIANTS.get(only, {})
+        r = timed_run(G, w, E, args.steps, args.warmup, seed=seed if kw else None, **kw,
+                      plain_sweeps=1 if only == "noseed_1sweep_fp64" else 0)
+        if rank == 0:
+            print(json.dumps({"variant": only, **{k: v for k, v in r.items() if k != "sim"},
+                              "kernel_ms": r["sim"].time_kernels(3)}))
+        return 0
     # plain FP64 path (P sweeps)
     plain = timed_run(G, w, E, args.steps, args.warmup)
     variants["plain_fp64"] = plain
@@ -350,9 +382,7 @@ def run_ours(args, w):
         ref = make_sim(G, w, E, sweeps=8)  # converged Picard, accuracy reference
         ref.advance(args.warmup + args.steps, use_graph=True)
         U_ref = ref.get_U_w(0)
-        for name, kw in (("seed_1sweep_fp64", dict(mode=1, sweeps=1)),
-                         ("seed_2sweeps_fp32", dict(mode=2, sweeps=2)),
-                         ("seed_3sweeps_fp32", dict(mode=2, sweeps=3))):
+        for name, kw in SEED_VARIANTS.items():
             variants[name] = timed_run(G, w, E, args.steps, args.warmup, seed=seed, tol=1e-3, **kw)
         variants["noseed_1sweep_fp64"] = timed_run(G, w, E, args.steps, args.warmup, plain_sweeps=1)
         for v in variants.values():
@@ -420,6 +450,7 @@ def run_ours(args, w):
                    "parallelism": "replicas" if world > 1 else "1 GPU", "path": head_name,
                    "elems_per_block": E, "cuda_graph": True,
                    "l2": "working set per step (state, traces, face fluxes) exceeds the 129 MB L2"},
+        "leaf_value": head["leaf_dof_per_s"] * world,
         "e2e": {"value": e2e_val, "unit": "DOF-updates/s", "h2d_bytes_per_step": h2d // e2e_steps,
                 "d2h_bytes_per_step": d2h // e2e_steps},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -460,6 +491,11 @@ def main():
     ap.add_argument("--no-seed", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", default=None,
+                    choices=["plain_fp64", "noseed_1sweep_fp64"] + list(SEED_VARIANTS),
+                    help="time one variant only and print its record (profiling runs)")
+    ap.add_argument("--seed-cache", action="store_true",
+                    help="reuse (or store) the trained seed parameters under the package build folder")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     w = WORKLOADS[args.workload]

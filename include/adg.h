@@ -118,6 +118,15 @@ int adg_regrid_count(const adg_ctx* ctx, int* n);
 /* DOF updates done so far (sum over steps of valid elements of every level
  * times Q * Np_s) and the host wall time spent in regrids. */
 int adg_dof_updates(const adg_ctx* ctx, int64_t* total, double* regrid_ms);
+/* The same count over leaf elements only (valid elements not covered by a
+ * finer level).  No reference counterpart. */
+int adg_leaf_dof_updates(const adg_ctx* ctx, int64_t* total);
+/* Host wall time of the regrids so far by phase, ms[0..n) with n <= 6:
+ * [0] tag kernels and the wait for the state, [1] clustering,
+ * [2] hierarchy and remap tables, [3] table upload, [4] remap launches,
+ * [5] CUDA graph capture/update after a layout change.  No reference
+ * counterpart (an instrumentation entry point of this library). */
+int adg_regrid_profile(const adg_ctx* ctx, double* ms, int n);
 int adg_get_boxes(const adg_ctx* ctx, int lev, int* out, int cap, int* nbox);
 int adg_tags(adg_ctx* ctx, int lev, uint8_t* out);
 
@@ -181,6 +190,15 @@ int adg_seed_get_params(adg_seed* s, float* out);
 int adg_seed_set_params(adg_seed* s, const float* in);
 /* mode 0 detaches; 1: sweeps in FP64; 2: sweeps in FP32. */
 int adg_seed_attach(adg_ctx* ctx, adg_seed* s, int mode, int sweeps, double tol);
+/* Which kernels compute the seed during steps: 1 (default) the fused
+ * tensor-core kernel (features, the four layers as TF32 tcgen05 MMAs with
+ * TMEM accumulators, H_w assembly) when the hidden width is 128; 0 the SIMT
+ * kernels (features, four FP32 SGEMMs, assembly).  No reference counterpart. */
+int adg_seed_set_path(adg_ctx* ctx, int path);
+/* The seeds H_w of every element of the current layout (valid elements of
+ * all levels, then the coarse-fine ghosts; Q * Np_st per element) into
+ * dst_dev (device pointer) through the given path.  No reference counterpart. */
+int adg_seed_infer(adg_ctx* ctx, double* dst_dev, int path);
 /* Elements whose seed was rejected (fallback to the full Picard), and
  * elements predicted, since attach. */
 int adg_seed_stats(adg_ctx* ctx, int64_t* fallbacks, int64_t* predicted);

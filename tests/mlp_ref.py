@@ -27,6 +27,28 @@ def forward(layers, X):
     return a, acts, zs
 
 
+def to_tf32(x, rounding):
+    """float32 values reduced to TF32 (10 explicit mantissa bits): rounding
+    'trunc' drops the low 13 bits, 'rn' rounds to nearest even, 'rna' to
+    nearest with ties away from zero."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    if rounding == "rn":
+        u = u + 0x0FFF + ((u >> 13) & 1)
+    elif rounding == "rna":
+        u = u + 0x1000
+    return (u & 0xFFFFE000).astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def forward_tf32(layers, X, rounding):
+    """forward() with every matrix product taking TF32 operands (activations
+    and weights reduced from float32) and accumulating exactly."""
+    a = X
+    for i, (W, b) in enumerate(layers):
+        z = to_tf32(a, rounding) @ to_tf32(W, rounding) + b
+        a = gelu(z) if i < len(layers) - 1 else z
+    return a
+
+
 def loss_and_grads(layers, X, T):
     Y, acts, zs = forward(layers, X)
     n = Y.size

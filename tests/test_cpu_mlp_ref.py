@@ -27,3 +27,13 @@ def test_restatement_backward_matches_finite_differences():
                 lm, _ = mlp_ref.loss_and_grads(layers, X, T)
                 arr[idx] = old
                 assert abs((lp - lm) / (2 * h) - g[li][which][idx]) < 1e-7
+
+
+def test_tf32_reduction():
+    x = np.array([1.0 + 2.0 ** -12, 1.0 + 2.0 ** -10, -3.0 - 2.0 ** -11, 1.0 + 2.0 ** -11 + 2.0 ** -20], np.float32)
+    assert list(mlp_ref.to_tf32(x, "trunc")) == [1.0, 1.0 + 2.0 ** -10, -3.0, 1.0]
+    assert list(mlp_ref.to_tf32(x, "rn")) == [1.0, 1.0 + 2.0 ** -10, -3.0, 1.0 + 2.0 ** -10]
+    # ties: 1 + 2^-11 is halfway between 1 and 1 + 2^-10
+    t = np.array([1.0 + 2.0 ** -11, -(1.0 + 3 * 2.0 ** -11)], np.float32)
+    assert list(mlp_ref.to_tf32(t, "rn")) == [1.0, -(1.0 + 2 * 2.0 ** -10)]
+    assert list(mlp_ref.to_tf32(t, "rna")) == [1.0 + 2.0 ** -10, -(1.0 + 2 * 2.0 ** -10)]

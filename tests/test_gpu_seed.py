@@ -140,6 +140,67 @@ def test_zero_tolerance_falls_back_everywhere_to_the_plain_path():
     assert fb == n == 3 * 32 * 32
 
 
+def _seed_correction(H, U, s, seed):
+    """(H - W U) / (rho_mean Dt/dx): the network's share of the seed."""
+    import oracle_ffi as O
+    W = O.matrix(2, 3, "Mk_h_w_inv") @ O.matrix(2, 3, "Mk_pred")  # a 0/1 selection
+    scale = U[:, 0, 0] * (s.Dt * 64.0)
+    return (H - np.einsum("kn,eqn->eqk", W, U)) / scale[:, None, None]
+
+
+def test_tensor_core_seed_matches_float64_restatement():
+    """The fused tcgen05 inference (TF32 operands, FP32 accumulation) and the
+    SIMT path (FP32) against the float64 restatement of features, network
+    and assembly, on the same state."""
+    torch = pytest.importorskip("torch")
+    seed, _, _ = _trained_seed()
+    s = _kh(seed=31)
+    for _ in range(3):
+        s.time_integration()
+    seed.attach(s, mode=2, sweeps=2, tol=1e-3)
+    U = s.get_U_w()
+    n, Q, Ns = U.shape
+    Nst = s.Np_st
+    out = {}
+    for path in (0, 1):
+        b = torch.full((n * Q * Nst,), float("nan"), dtype=torch.float64, device="cuda")
+        s.seed_infer(b.data_ptr(), path)
+        torch.cuda.synchronize()
+        out[path] = b.cpu().numpy().reshape(n, Q, Nst)
+    assert s.status() == 0
+    p = seed.get_params()
+    nw, _ = seed.num_params()
+    nin, nout = seed.n_in, seed.n_out
+    x_mean, x_istd = p[nw:nw + nin], p[nw + nin:nw + 2 * nin]
+    y_mean, y_std = p[nw + 2 * nin:nw + 2 * nin + nout], p[nw + 2 * nin + nout:]
+    X = np.concatenate([(U.reshape(n, -1) / U[:, :1, 0]).astype(np.float32),
+                        np.full((n, 1), s.Dt * 64.0, dtype=np.float32)], axis=1)
+    X = (X - x_mean) * x_istd
+    layers = _layers64(seed)
+    Y, _, _ = mlp_ref.forward(layers, X.astype(np.float64))
+    # compare in the network's standardised output space
+    y0 = (_seed_correction(out[0], U, s, seed).reshape(n, -1) - y_mean) / y_std
+    y1 = (_seed_correction(out[1], U, s, seed).reshape(n, -1) - y_mean) / y_std
+    assert np.all(np.isfinite(y0)) and np.all(np.isfinite(y1))
+    rms = np.sqrt(np.mean(Y ** 2))
+
+    def err(a, b):
+        return np.max(np.abs(a - b)) / np.max(np.abs(Y)), np.sqrt(np.mean((a - b) ** 2)) / rms
+
+    # SIMT path: FP32 throughout
+    e_max, e_rms = err(y0, Y)
+    assert e_max < 1e-5 and e_rms < 1e-5, (e_max, e_rms)
+    # tensor cores: operands rounded to TF32 (10 mantissa bits, nearest) and
+    # FP32 accumulation; the restatement that rounds its operands likewise
+    # leaves FP32 rounding and the odd activation that lands on the other
+    # side of a TF32 rounding boundary (one TF32 ulp, 1e-3 of it)
+    e_max, e_rms = err(y1, mlp_ref.forward_tf32(layers, X.astype(np.float64), "rna"))
+    assert e_max < 3e-3 and e_rms < 5e-4, (e_max, e_rms)
+    # and what TF32 costs against FP32: about 1e-3 of the outputs
+    e_max, e_rms = err(y1, Y)
+    assert e_max < 1e-2 and e_rms < 3e-3, (e_max, e_rms)
+
+
 @pytest.mark.parametrize("mode", [1, 2])
 def test_seeded_run_stays_close_to_plain_run(mode):
     seed, _, _ = _trained_seed()
