@@ -88,6 +88,7 @@ def lib():
         "adg_fp64_peak_probe": ([dp], i),
         "adg_set_device": ([i], i),
         "adg_advance_timed": ([vp, i, i, dp], i),
+        "adg_advance_timed_flushed": ([vp, i, i, ctypes.c_int64, dp], i),
         "adg_time_kernels": ([vp, i, dp, i], i),
         "adg_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(vp)], i),
         "adg_host_free": ([vp], i),
@@ -111,6 +112,8 @@ def lib():
         "adg_seed_attach": ([vp, vp, i, i, ctypes.c_double], i),
         "adg_seed_stats": ([vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)], i),
         "adg_get_boxes": ([vp, i, ctypes.POINTER(i), i, ctypes.POINTER(i)], i),
+        "adg_set_layout": ([vp, i, ctypes.POINTER(i), ctypes.POINTER(i)], i),
+        "adg_level_cell_coords": ([vp, i, ctypes.POINTER(i)], i),
         "adg_tags": ([vp, i, ctypes.POINTER(ctypes.c_uint8)], i),
     }
     for name, (args, res) in sig.items():
@@ -335,6 +338,13 @@ class AmrDG:
         self._check(self._L.adg_launch_count(self.ctx, ctypes.byref(v)), "adg_launch_count")
         return v.value
 
+    def advance_timed_flushed(self, nsteps, flush_bytes=256 << 20, use_graph=True):
+        """Device ms of nsteps steps with the L2 evicted before each (flush excluded)."""
+        v = ctypes.c_double()
+        self._check(self._L.adg_advance_timed_flushed(self.ctx, int(nsteps), int(bool(use_graph)), int(flush_bytes),
+                                                      ctypes.byref(v)), "adg_advance_timed_flushed")
+        return v.value
+
     def advance_timed(self, nsteps, use_graph=True):
         """n steps bracketed by CUDA events on the context's stream; returns ms."""
         v = ctypes.c_double()
@@ -380,6 +390,23 @@ class AmrDG:
         n = ctypes.c_int()
         self._check(self._L.adg_get_boxes(self.ctx, lev, buf, cap, ctypes.byref(n)), "adg_get_boxes")
         return np.frombuffer(buf, dtype=np.int32, count=6 * n.value).reshape(n.value, 6).copy()
+
+    def set_layout(self, boxes_per_level):
+        """Layout from the caller: one [nbox, 6] array (lo0, lo1, lo2, hi0,
+        hi1, hi2) per level; the state is remapped onto it."""
+        arrs = [np.asarray(b, dtype=np.int32).reshape(-1, 6) for b in boxes_per_level]
+        nbox = (ctypes.c_int * len(arrs))(*[a.shape[0] for a in arrs])
+        flat = np.ascontiguousarray(np.concatenate(arrs, axis=0) if arrs else np.zeros((0, 6), np.int32))
+        self._check(self._L.adg_set_layout(self.ctx, len(arrs), nbox, flat.ctypes.data_as(ctypes.POINTER(ctypes.c_int))),
+                    "adg_set_layout")
+
+    def level_cell_coords(self, lev):
+        """(i, j, k) of the valid cells of level lev in state order: [n, 3]."""
+        n = self.level_cells(lev)
+        out = np.zeros((n, 3), dtype=np.int32)
+        self._check(self._L.adg_level_cell_coords(self.ctx, lev, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))),
+                    "adg_level_cell_coords")
+        return out
 
     def tags(self, lev):
         """Refinement tags of the valid cells of level lev (current state)."""

@@ -152,6 +152,7 @@ struct adg_ctx {
   cudaEvent_t tab_ev = nullptr;
   std::vector<size_t> ad_off;  // offset (ints) of level lf's records in ad_all
   DevBuf<uint8_t> tags;
+  DevBuf<uint8_t> l2_flush;  // written between timed steps to evict the L2
   DevBuf<double> Uw_alt;   // regrid target state (swapped with Uw)
   TableView<int> remap_i;     // regrid remap entries: dst | parent | src_old
   TableView<int8_t> remap_c;  // regrid remap child indices
@@ -181,7 +182,7 @@ struct adg_ctx {
     rf_elem.release(); rf_off.release(); rf_face.release(); rf_fine.release(); ad_all.release();
     gf_elem.release(); gf_parent.release(); rf_dside.release(); gf_child.release(); tags.release();
     sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); fb_list.release(); fb_count.release();
-    fb_total.release(); Uw_alt.release(); remap_i.release(); remap_c.release();
+    fb_total.release(); Uw_alt.release(); remap_i.release(); remap_c.release(); l2_flush.release();
     if (tab_ev) cudaEventSynchronize(tab_ev), cudaEventDestroy(tab_ev);
     tab_dev.release();
     if (tab_host) cudaFreeHost(tab_host);
@@ -396,17 +397,10 @@ int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
 
 // Fine -> coarse average down (finest first) and the coarse -> fine ghost
 // fill (AmrDG.h:999-1015).
-int launch_amr_sync(adg_ctx* ctx) {
+// Coarse -> fine projection into the ghost elements at coarse-fine faces
+// (FillPatchTwoLevels); every ghost's parent is a valid coarse element.
+int launch_ghost_fill(adg_ctx* ctx) {
   const Hierarchy& H = ctx->hier;
-  if (H.nlevels() <= 1) return ADG_OK;
-  const int NOV1 = (1 << ctx->cfg.D) + 1;
-  for (int lf = H.nlevels() - 1; lf >= 1; --lf) {
-    const int nrec = (int)(H.ad_rec[lf].size() / NOV1);
-    if (!nrec) continue;
-    cudaError_t e = ctx->ks->average_down(ctx->Uw.p, ctx->ad_all.p + ctx->ad_off[lf], nrec, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "average down launch");
-    ctx->launches++;
-  }
   if (!H.gf_elem.empty()) {
     ScatterArgs sa{};
     sa.Uw = ctx->Uw.p;
@@ -419,6 +413,20 @@ int launch_amr_sync(adg_ctx* ctx) {
     ctx->launches++;
   }
   return ADG_OK;
+}
+
+int launch_amr_sync(adg_ctx* ctx) {
+  const Hierarchy& H = ctx->hier;
+  if (H.nlevels() <= 1) return ADG_OK;
+  const int NOV1 = (1 << ctx->cfg.D) + 1;
+  for (int lf = H.nlevels() - 1; lf >= 1; --lf) {
+    const int nrec = (int)(H.ad_rec[lf].size() / NOV1);
+    if (!nrec) continue;
+    cudaError_t e = ctx->ks->average_down(ctx->Uw.p, ctx->ad_all.p + ctx->ad_off[lf], nrec, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "average down launch");
+    ctx->launches++;
+  }
+  return launch_ghost_fill(ctx);
 }
 
 // Dt from the current state; advance_time adds the old Dt to t first.
@@ -467,6 +475,9 @@ double ms_between(std::chrono::steady_clock::time_point a, std::chrono::steady_c
   return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
+int apply_layout(adg_ctx* ctx, const std::vector<std::vector<amr::IBox>>& ng,
+                 std::chrono::steady_clock::time_point t2);
+
 int regrid(adg_ctx* ctx) {
   auto t0 = std::chrono::steady_clock::now();
   Hierarchy& H = ctx->hier;
@@ -508,13 +519,22 @@ int regrid(adg_ctx* ctx) {
   std::vector<std::vector<amr::IBox>> ng = amr::make_new_grids(ctx->gp, H.grids, tf);
   auto t2 = std::chrono::steady_clock::now();
   ctx->rg_phase_ms[1] += ms_between(t1, t2);
-  if (ng == H.grids) {  // same boxes in the same order: layout and valid data unchanged
-    ctx->n_regrids++;
-    return ADG_OK;
-  }
+  ctx->n_regrids++;
+  if (ng == H.grids) return ADG_OK;  // same boxes in the same order: layout and valid data unchanged
+  return apply_layout(ctx, ng, t2);
+}
+
+// Switch to the layout of the given boxes per level and remap the state:
+// level 0 is kept, level l takes the old level's data where the cell was
+// valid there and the projection of the new level l-1 elsewhere (FillPatch
+// semantics of RemakeLevel / MakeNewLevelFromCoarse, AmrDG_Level.tpp:52-132).
+int apply_layout(adg_ctx* ctx, const std::vector<std::vector<amr::IBox>>& ng,
+                 std::chrono::steady_clock::time_point t2) {
+  Hierarchy& H = ctx->hier;
+  const KernelSet* ks = ctx->ks;
   Hierarchy NH;
   std::string msg;
-  if (!NH.build(ctx->gp, ng, ctx->cfg.reflux_box_quirk, &msg)) return fail(ctx, ADG_ERR_LAYOUT, "regrid: " + msg);
+  if (!NH.build(ctx->gp, ng, ctx->cfg.reflux_box_quirk, &msg)) return fail(ctx, ADG_ERR_LAYOUT, "layout: " + msg);
   // remap: level 0 is unchanged; level l from the old level l where a cell
   // was valid there, else from the new level l-1 (levels in order on the stream).
   const int Q = ks->Q, Ns = ks->Np_s;
@@ -570,7 +590,6 @@ int regrid(adg_ctx* ctx) {
     ctx->launches++;
   }
   std::swap(ctx->Uw, ctx->Uw_alt);
-  ctx->n_regrids++;
   ctx->rg_phase_ms[4] += ms_between(t4, std::chrono::steady_clock::now());
   return ADG_OK;
 }
@@ -855,6 +874,10 @@ int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem) {
   ADG_CUDA(cudaMemcpyAsync(ctx->Uw.p + off, src, cnt * sizeof(double),
                            mem == ADG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream),
            "set_state copy");
+  if (lev + 1 < ctx->hier.nlevels()) {  // the finer level's ghosts project from this level
+    rc = launch_ghost_fill(ctx);
+    if (rc) return rc;
+  }
   ADG_CUDA(cudaStreamSynchronize(ctx->stream), "set_state sync");
   return ADG_OK;
 }
@@ -960,6 +983,41 @@ int adg_get_boxes(const adg_ctx* ctx, int lev, int* out, int cap, int* nbox) {
   return ADG_OK;
 }
 
+int adg_set_layout(adg_ctx* ctx, int nlev, const int* nbox, const int* boxes) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (nlev < 1 || nlev > ctx->cfg.max_level + 1 || !nbox || !boxes)
+    return fail(ctx, ADG_ERR_ARG, "bad layout arguments");
+  std::vector<std::vector<amr::IBox>> ng(nlev);
+  size_t o = 0;
+  for (int l = 0; l < nlev; ++l) {
+    if (nbox[l] < 0) return fail(ctx, ADG_ERR_ARG, "bad layout arguments");
+    for (int b = 0; b < nbox[l]; ++b, o += 6) {
+      amr::IBox bx;
+      for (int d = 0; d < 3; ++d) {
+        bx.lo[d] = d < ctx->cfg.D ? boxes[o + d] : 0;
+        bx.hi[d] = d < ctx->cfg.D ? boxes[o + 3 + d] : 0;
+      }
+      ng[l].push_back(bx);
+    }
+  }
+  if (ng != ctx->hier.grids) {
+    rc = apply_layout(ctx, ng, std::chrono::steady_clock::now());
+    if (rc) return rc;
+  }
+  ctx->first_step = false;  // the caller owns the layout from now on
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "layout");
+  return ADG_OK;
+}
+
+int adg_level_cell_coords(const adg_ctx* ctx, int lev, int* ijk) {
+  if (!ctx || !ijk || lev < 0 || lev >= ctx->hier.nlevels()) return ADG_ERR_ARG;
+  const Hierarchy& H = ctx->hier;
+  const size_t e0 = H.level_valid_offset(lev), n = H.level_valid_count(lev);
+  std::copy(H.elem_cell.begin() + 3 * e0, H.elem_cell.begin() + 3 * (e0 + n), ijk);
+  return ADG_OK;
+}
+
 int adg_tags(adg_ctx* ctx, int lev, uint8_t* out) {
   int rc = check_ready(ctx);
   if (rc) return rc;
@@ -1011,6 +1069,40 @@ int adg_advance_timed(adg_ctx* ctx, int nsteps, int use_graph, double* ms) {
   if (rc) return rc;
   if (e != cudaSuccess) return cuda_fail(ctx, e, "timed advance");
   *ms = f;
+  return ADG_OK;
+}
+
+int adg_advance_timed_flushed(adg_ctx* ctx, int nsteps, int use_graph, int64_t flush_bytes, double* ms) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!ms || nsteps < 0 || flush_bytes < 0) return ADG_ERR_ARG;
+  if (use_graph && (!ctx->graph_exec || ctx->graph_stale) && !regrid_due(ctx)) {
+    rc = capture_graph(ctx);
+    if (rc) return rc;
+  }
+  if (flush_bytes > 0) ADG_CUDA(ctx->l2_flush.ensure((size_t)flush_bytes), "alloc L2 flush buffer");
+  std::vector<cudaEvent_t> ev(2 * (size_t)nsteps);
+  for (auto& x : ev) ADG_CUDA(cudaEventCreate(&x), "event");
+  for (int k = 0; k < nsteps && rc == ADG_OK; ++k) {
+    if (flush_bytes > 0) {
+      cudaError_t e = cudaMemsetAsync(ctx->l2_flush.p, k & 0xff, (size_t)flush_bytes, ctx->stream);
+      if (e != cudaSuccess) rc = cuda_fail(ctx, e, "L2 flush");
+    }
+    cudaEventRecord(ev[2 * k], ctx->stream);
+    if (rc == ADG_OK) rc = host_step(ctx, use_graph != 0);
+    cudaEventRecord(ev[2 * k + 1], ctx->stream);
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  double total = 0.0;
+  for (int k = 0; k < nsteps && e == cudaSuccess && rc == ADG_OK; ++k) {
+    float f = 0.f;
+    e = cudaEventElapsedTime(&f, ev[2 * k], ev[2 * k + 1]);
+    total += f;
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "timed advance");
+  *ms = total;
   return ADG_OK;
 }
 

@@ -128,6 +128,19 @@ int adg_leaf_dof_updates(const adg_ctx* ctx, int64_t* total);
  * counterpart (an instrumentation entry point of this library). */
 int adg_regrid_profile(const adg_ctx* ctx, double* ms, int n);
 int adg_get_boxes(const adg_ctx* ctx, int lev, int* out, int cap, int* nbox);
+/* Layout from the caller (e.g. the BoxArrays of an AMReX hierarchy after its
+ * regrid, Mesh.h:156-196): nbox[l] boxes of level l < nlev in
+ * boxes[6 * (sum of earlier counts + b) + {lo0,lo1,lo2,hi0,hi1,hi2}], level
+ * cell indices.  Levels must be properly nested; level 0 must cover the
+ * domain.  The state is remapped as AMR_remake_level / AMR_make_new_fine_level
+ * do (AmrDG_Level.tpp:52-132): old data where a cell stays valid, the L2
+ * projection of the coarser level elsewhere.  The context stops regridding
+ * on its own first step (it still regrids every dtn_regrid steps when
+ * dtn_regrid > 0: give 0 to leave the layout to the caller). */
+int adg_set_layout(adg_ctx* ctx, int nlev, const int* nbox, const int* boxes);
+/* Cell indices (i, j, k) of the valid cells of a level in the order of the
+ * level's state arrays (3 ints per cell). */
+int adg_level_cell_coords(const adg_ctx* ctx, int lev, int* ijk);
 int adg_tags(adg_ctx* ctx, int lev, uint8_t* out);
 
 /* Per-stage entry points (parity testing). */
@@ -148,6 +161,11 @@ int adg_set_device(int device);
 /* n steps like adg_advance, bracketed by CUDA events recorded on the
  * context's stream; *ms receives the device time of the n steps. */
 int adg_advance_timed(adg_ctx* ctx, int nsteps, int use_graph, double* ms);
+/* The same with the L2 evicted before every step (a device memset of
+ * flush_bytes, outside the timed region): ms = the sum over the steps of
+ * the device time from the step's start (regrid included) to its end.
+ * No reference counterpart (benchmark timing). */
+int adg_advance_timed_flushed(adg_ctx* ctx, int nsteps, int use_graph, int64_t flush_bytes, double* ms);
 
 /* n steps with CUDA events around every kernel on the context's stream;
  * ms[k] receives the average duration of kernel kind k per step:

@@ -76,3 +76,34 @@ def test_amr_graph_replay_matches_stream_launches():
     assert a.num_levels() == b.num_levels()
     for l in range(a.num_levels()):
         assert np.array_equal(a.get_U_w(l), b.get_U_w(l))
+
+
+def test_caller_supplied_layout_reproduces_the_run():
+    """adg_set_layout: a context given another context's boxes and state (as
+    a caller that owns the hierarchy, e.g. AMReX, would) takes the same
+    steps bit for bit."""
+    case = "kh_p3_amr"
+    a = make_gpu_amr(case)
+    for _ in range(6):
+        a.time_integration()
+    D, P, n, hi, per, ic, extra, amr = AMR_CASES[case]
+    from parity import GPU_IC
+    b = G.AmrDG(P=P, D=D)
+    b.setGeometrySettings(prob_lo=(0, 0, 0), prob_hi=hi, n_cell=n, periodic=per, max_level=amr["max_level"],
+                          max_grid=amr["max_grid"], blocking_factor=amr["blocking_factor"], dtn_regrid=0)
+    b.setAmrSettings(tag_kind=amr["tag_kind"], tag_threshold=amr["tag_threshold"], reflux_box_quirk=1)
+    b.settings(c_dt=0.5)
+    b.init(G.Compressible_Euler().settings(GPU_IC[ic], **extra))
+    b.set_layout([a.boxes(l) for l in range(a.num_levels())])
+    assert b.num_levels() == a.num_levels()
+    for l in range(a.num_levels()):
+        assert np.array_equal(b.boxes(l), a.boxes(l))
+        assert np.array_equal(b.level_cell_coords(l), a.level_cell_coords(l))
+        b.set_U_w(a.get_U_w(l), l)
+    b.Dt = a.Dt
+    for _ in range(2):  # a's next regrid is due at its 8th step
+        a.time_integration()
+        b.time_integration()
+    for l in range(a.num_levels()):
+        assert np.array_equal(a.get_U_w(l), b.get_U_w(l)), l
+    assert a.Dt == b.Dt
