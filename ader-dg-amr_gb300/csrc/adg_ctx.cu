@@ -163,6 +163,7 @@ struct adg_ctx {
   double seed_tol = 1e-3;
   DevBuf<float> sx, sy0, sy1, syo;     // features, ping-pong activations, outputs
   DevBuf<double> hseed;
+  DevBuf<float> hseed_f;  // FP32 seeds for FP32 sweeps (tensor-core path)
   DevBuf<int> fb_list, fb_count;
   DevBuf<unsigned long long> fb_total;
   long long seed_predicted = 0;
@@ -172,6 +173,10 @@ struct adg_ctx {
   cudaGraphExec_t graph_exec = nullptr;
   int graph_kernels = 0;
   bool graph_stale = false;
+  // side stream of the step: the ghost fill runs there beside the average
+  // down and the Dt reduction (disjoint elements)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 
   ~adg_ctx() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
@@ -181,11 +186,14 @@ struct adg_ctx {
     elem_level.release(); scal.release(); dt_done.release(); min_bits.release(); status.release();
     rf_elem.release(); rf_off.release(); rf_face.release(); rf_fine.release(); ad_all.release();
     gf_elem.release(); gf_parent.release(); rf_dside.release(); gf_child.release(); tags.release();
-    sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); fb_list.release(); fb_count.release();
+    sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); hseed_f.release(); fb_list.release(); fb_count.release();
     fb_total.release(); Uw_alt.release(); remap_i.release(); remap_c.release(); l2_flush.release();
     if (tab_ev) cudaEventSynchronize(tab_ev), cudaEventDestroy(tab_ev);
     tab_dev.release();
     if (tab_host) cudaFreeHost(tab_host);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
+    if (side) cudaStreamDestroy(side);
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 };
@@ -241,6 +249,7 @@ int upload_tables(adg_ctx* ctx, const RemapTable* rm = nullptr) {
     ADG_CUDA(ctx->sy1.ensure(ne * sd->h), "alloc seed activations");
     ADG_CUDA(ctx->syo.ensure(ne * sd->n_out), "alloc seed outputs");
     ADG_CUDA(ctx->hseed.ensure(ne * (size_t)ks->Q * ks->Np_st), "alloc seed H_w");
+    ADG_CUDA(ctx->hseed_f.ensure(ne * (size_t)ks->Q * ks->Np_st), "alloc seed H_w");
     ADG_CUDA(ctx->fb_list.ensure(ne), "alloc fallback list");
   }
   std::vector<int> ad;
@@ -382,6 +391,8 @@ int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
   ca.geom = pa.geom;
   ca.dt = ctx->scal.p;
   if (!H.rf_elem.empty()) {  // coarse-fine flux correction (AmrDG.h:1159-1162), fused
+    ca.nrec = (int)H.rf_elem.size();
+    ca.rec_elem = ctx->rf_elem.p;
     ca.rec_of_elem = ctx->rf_rec_of_elem.p;
     ca.rec_off = ctx->rf_off.p;
     ca.ent_face = ctx->rf_face.p;
@@ -415,7 +426,7 @@ int launch_ghost_fill(adg_ctx* ctx) {
   return ADG_OK;
 }
 
-int launch_amr_sync(adg_ctx* ctx) {
+int launch_average_down(adg_ctx* ctx) {
   const Hierarchy& H = ctx->hier;
   if (H.nlevels() <= 1) return ADG_OK;
   const int NOV1 = (1 << ctx->cfg.D) + 1;
@@ -426,7 +437,13 @@ int launch_amr_sync(adg_ctx* ctx) {
     if (e != cudaSuccess) return cuda_fail(ctx, e, "average down launch");
     ctx->launches++;
   }
-  return launch_ghost_fill(ctx);
+  return ADG_OK;
+}
+
+int launch_amr_sync(adg_ctx* ctx) {
+  int rc = launch_average_down(ctx);
+  if (rc) return rc;
+  return ctx->hier.nlevels() > 1 ? launch_ghost_fill(ctx) : ADG_OK;
 }
 
 // Dt from the current state; advance_time adds the old Dt to t first.
@@ -460,11 +477,29 @@ int launch_dt(adg_ctx* ctx, int advance_time) {
 int launch_step(adg_ctx* ctx, cudaEvent_t* ev = nullptr) {
   int rc = launch_ader(ctx, nullptr, ev);
   if (rc) return rc;
-  rc = launch_amr_sync(ctx);
+  const bool fork = !ev && ctx->side && ctx->hier.nlevels() > 1 && !ctx->hier.gf_elem.empty();
+  if (!fork) {
+    rc = launch_amr_sync(ctx);
+    if (rc) return rc;
+    if (ev) cudaEventRecord(ev[4], ctx->stream);
+    rc = launch_dt(ctx, 1);
+    if (ev) cudaEventRecord(ev[5], ctx->stream);
+    return rc;
+  }
+  // ghost fill on the side stream: it reads valid coarse parents (never
+  // covered, so not touched by the average down) and writes only ghosts,
+  // which neither the average down nor the Dt reduction reads
+  ADG_CUDA(cudaEventRecord(ctx->fork_ev, ctx->stream), "fork");
+  ADG_CUDA(cudaStreamWaitEvent(ctx->side, ctx->fork_ev, 0), "fork");
+  cudaStream_t main = ctx->stream;
+  ctx->stream = ctx->side;
+  rc = launch_ghost_fill(ctx);
+  ctx->stream = main;
   if (rc) return rc;
-  if (ev) cudaEventRecord(ev[4], ctx->stream);
-  rc = launch_dt(ctx, 1);
-  if (ev) cudaEventRecord(ev[5], ctx->stream);
+  ADG_CUDA(cudaEventRecord(ctx->join_ev, ctx->side), "join");
+  rc = launch_average_down(ctx);
+  if (rc == ADG_OK) rc = launch_dt(ctx, 1);
+  ADG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0), "join");
   return rc;
 }
 
@@ -697,6 +732,12 @@ int adg_ctx_create(const adg_config* cfg, adg_ctx** out) {
     return ADG_ERR_CUDA;
   }
   ctx->own_stream = true;
+  if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+    delete ctx;
+    return ADG_ERR_CUDA;
+  }
   if (ctx->scal.ensure(kScalCount) != cudaSuccess || ctx->dt_done.ensure(1) != cudaSuccess ||
       ctx->min_bits.ensure(1) != cudaSuccess || ctx->status.ensure(1) != cudaSuccess) {
     delete ctx;
@@ -1319,10 +1360,6 @@ cudaError_t grow_rows(DevBuf<float>& b, size_t keep, size_t need) {
   return e;
 }
 
-__global__ void k_accumulate_count(const int* c, unsigned long long* total) {
-  if (threadIdx.x == 0) *total += (unsigned long long)*c;
-}
-
 }  // namespace
 
 // Seeded predictor: network inference, seeded sweeps with residual test,
@@ -1354,7 +1391,7 @@ int seed_pack_tc(adg_seed* s) {
 // H_w seeds of every element of the current layout into dst: the fused
 // tensor-core kernel (path 1, when the seed is packed for it) or features +
 // four SGEMMs + assembly (path 0).
-int seed_infer(adg_ctx* ctx, double* dst, int path) {
+int seed_infer(adg_ctx* ctx, double* dst, int path, float* dst_f = nullptr) {
   adg_seed* sd = ctx->seed;
   const Hierarchy& H = ctx->hier;
   const KernelSet* ks = ctx->ks;
@@ -1379,6 +1416,7 @@ int seed_infer(adg_ctx* ctx, double* dst, int path) {
     ta.y_mean = sd->y_mean.p;
     ta.y_std = sd->y_std.p;
     ta.Hseed = dst;
+    ta.Hseed_f = dst_f;
     ta.status = ctx->status.p;
     cudaError_t e = ks->seed_infer_tc(ta, st);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "seed inference (tensor cores)");
@@ -1408,12 +1446,15 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base) {
   const int n = (int)ctx->hier.n_elem();
   const KernelSet* ks = ctx->ks;
   cudaStream_t st = ctx->stream;
-  int rc = seed_infer(ctx, ctx->hseed.p, ctx->seed_path);
+  // FP32 sweeps from the tensor-core path take an FP32 seed
+  const bool f32 = ctx->seed_mode == 2 && ctx->seed_path == 1 && ctx->seed->packed;
+  int rc = seed_infer(ctx, ctx->hseed.p, ctx->seed_path, f32 ? ctx->hseed_f.p : nullptr);
   if (rc) return rc;
   cudaError_t e;
   ADG_CUDA(cudaMemsetAsync(ctx->fb_count.p, 0, sizeof(int), st), "fallback reset");
   PredictorArgs pa = base;
   pa.Hseed = ctx->hseed.p;
+  pa.Hseed_f = f32 ? ctx->hseed_f.p : nullptr;
   pa.seed_tol = ctx->seed_tol;
   pa.fb_list = ctx->fb_list.p;
   pa.fb_count = ctx->fb_count.p;
@@ -1423,10 +1464,10 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base) {
   PredictorArgs fb = base;  // full FP64 Picard for the rejected elements
   fb.elem_list = ctx->fb_list.p;
   fb.list_count = ctx->fb_count.p;
+  fb.count_total = ctx->fb_total.p;
   e = ks->predictor(fb, ctx->E, st, 0);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "fallback predictor");
-  k_accumulate_count<<<1, 32, 0, st>>>(ctx->fb_count.p, ctx->fb_total.p);
-  ctx->launches += 3;  // 2 predictors, count
+  ctx->launches += 2;
   ctx->seed_predicted += n;
   return ADG_OK;
 }

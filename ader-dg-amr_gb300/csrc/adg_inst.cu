@@ -76,7 +76,7 @@ struct Impl final : KernelSet {
     return cudaGetLastError();
   }
   cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const override {
-    const long long n = (long long)a.n_valid * O::Q;
+    const long long n = ((long long)a.n_valid + (a.rec_of_elem ? a.nrec : 0)) * O::Q;
     const int bs = 128;
     k_corrector<O><<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(a);
     return cudaGetLastError();

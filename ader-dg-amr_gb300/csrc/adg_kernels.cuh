@@ -43,12 +43,15 @@ struct PredictorArgs {
   // learned seed (modes 1, 2): initial H_w per element, residual tolerance,
   // fallback list of elements whose seed residual exceeds it
   const double* Hseed;
+  const float* Hseed_f;       // FP32 seed (MODE 2; used instead of Hseed when non-null)
   double seed_tol;
   int* fb_list;
   int* fb_count;
-  // optional element list (fallback pass): element = elem_list[i], i < *list_count
+  // optional element list (fallback pass): element = elem_list[i], i < *list_count;
+  // count_total (optional) accumulates *list_count once per launch
   const int* elem_list;
   const int* list_count;
+  unsigned long long* count_total;
 };
 
 // Point-wise flux stage: H at NQ points of E elements (shared, [point][col])
@@ -147,6 +150,7 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   bool live = e_raw < a.n_elem;
   if (a.elem_list) {
     const int cnt = *a.list_count;
+    if (a.count_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.count_total, (unsigned long long)cnt);
     if ((int)(blockIdx.x * E) >= cnt) return;  // whole block idle
     live = e_raw < cnt;
     e_raw = live ? a.elem_list[e_raw] : a.elem_list[cnt - 1];
@@ -218,9 +222,10 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
     // ---- learned seed: H_w from the network, then `sweeps` sweeps; the
     // first sweep's change judges the seed (residual relative to the
     // element's largest cell mean), failures go to the fallback list.
-    const double* hs = a.Hseed + ((size_t)e * Q + q) * NP_ST;
+    const size_t hoff = ((size_t)e * Q + q) * NP_ST;
     double res = 0.0;
     if constexpr (MODE == 1) {
+      const double* hs = a.Hseed + hoff;
 #pragma unroll
       for (int n = 0; n < NP_ST; ++n) hw[n] = hs[n];
       for (int s = 0; s < a.sweeps; ++s) {
@@ -235,8 +240,13 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
     } else {
       // FP32 sweeps on a float copy; the final H_w = W U + dlt in FP64
       float hf[NP_ST], wf[NP_ST], dlt[NP_ST], cf[D];
+      if (a.Hseed_f) {
 #pragma unroll
-      for (int n = 0; n < NP_ST; ++n) hf[n] = (float)hs[n];
+        for (int n = 0; n < NP_ST; ++n) hf[n] = a.Hseed_f[hoff + n];
+      } else {
+#pragma unroll
+        for (int n = 0; n < NP_ST; ++n) hf[n] = (float)a.Hseed[hoff + n];
+      }
       O::template wu<float>(RegIn{u}, RegOutT<float>{wf});
 #pragma unroll
       for (int d = 0; d < D; ++d) cf[d] = (float)c[d];
@@ -252,7 +262,8 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
       }
       res = (double)resf;
 #pragma unroll
-      for (int n = 0; n < NP_ST; ++n) hw[n] = a.sweeps > 0 ? wu[n] + (double)dlt[n] : hs[n];
+      for (int n = 0; n < NP_ST; ++n)
+        hw[n] = a.sweeps > 0 ? wu[n] + (double)dlt[n] : (a.Hseed_f ? (double)hf[n] : a.Hseed[hoff + n]);
     }
     // per-element reduction over its Q columns through shared memory
     double* red = sm;
@@ -426,8 +437,12 @@ struct CorrectorArgs {
   LevelGeom geom;
   const double* dt;
   // coarse-fine flux corrections applied after the update (nullptr: none):
-  // record of element e = rec_of_elem[e] (-1: none), its face entries
-  // rec_off[r] .. rec_off[r+1]
+  // record of element e = rec_of_elem[e] (-1: none), element of record r =
+  // rec_elem[r], its face entries rec_off[r] .. rec_off[r+1].  Elements with a
+  // record are updated by the first nrec * Q threads, so the warps that run
+  // the correction run nothing else and, having the longest chains, start first.
+  int nrec;
+  const int* rec_elem;
   const int* rec_of_elem;
   const int* rec_off;
   const int* ent_face;
@@ -492,9 +507,20 @@ template <class O>
 __global__ void k_corrector(CorrectorArgs a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NB = O::NQ_BD, NF = 2 * D;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (int64_t)a.n_valid * Q) return;
-  const int e = (int)(t / Q);
-  const int q = (int)(t % Q);
+  // record threads first: their chains are the longest, so they start first
+  const int64_t nrq = a.rec_of_elem ? (int64_t)a.nrec * Q : 0;
+  int e, q, r = -1;
+  if (t < nrq) {
+    r = (int)(t / Q);
+    q = (int)(t % Q);
+    e = a.rec_elem[r];
+  } else {
+    const int64_t t2 = t - nrq;
+    if (t2 >= (int64_t)a.n_valid * Q) return;
+    e = (int)(t2 / Q);
+    q = (int)(t2 % Q);
+    if (nrq && a.rec_of_elem[e] >= 0) return;  // updated by a record thread
+  }
   const int lev = a.elem_level ? a.elem_level[e] : 0;
   double R[NP_S];
   const double* rv = a.Rvol + ((size_t)e * Q + q) * NP_S;
@@ -517,10 +543,7 @@ __global__ void k_corrector(CorrectorArgs a) {
 #undef ADG_BD
 #pragma unroll
   for (int n = 0; n < NP_S; ++n) R[n] = R[n] * O::minv(n);
-  if (a.rec_of_elem) {
-    const int r = a.rec_of_elem[e];
-    if (r >= 0) reflux_add<O>(a, r, lev, q, R);
-  }
+  if (r >= 0) reflux_add<O>(a, r, lev, q, R);
   double* dst = a.Uw + ((size_t)e * Q + q) * NP_S;
 #pragma unroll
   for (int n = 0; n < NP_S; ++n) dst[n] = R[n];

@@ -135,6 +135,16 @@ __device__ __forceinline__ float to_tf32(float x) {
   return __uint_as_float(r);
 }
 
+// GELU with tanh(y) = 1 - 2 / (exp(2y) + 1) on the fast exponential and
+// reciprocal; |y| clamped to 15 where tanh is 1 in FP32.  Its error (~1e-7)
+// is far below the TF32 rounding of the activations that follows.
+__device__ __forceinline__ float gelu_fast(float z) {
+  float y = mlp::kGeluK * (z + mlp::kGeluA * z * z * z);
+  y = fminf(fmaxf(y, -15.0f), 15.0f);
+  const float th = 1.0f - __fdividef(2.0f, __expf(2.0f * y) + 1.0f);
+  return 0.5f * z * (1.0f + th);
+}
+
 // Float offset of (row, k) in the canonical K-major layout of a matrix with K
 // columns (K a multiple of 4): core matrix (row/8, k/4) of 8 x 4 floats.
 __host__ __device__ __forceinline__ int kmajor_off(int row, int k, int K) {
@@ -150,7 +160,10 @@ constexpr int kSeedTcHidden = 128;
 constexpr int kSeedTcThreads = 256;
 constexpr int kSeedTcRows = 128;
 constexpr size_t kSeedTcBuf = 65536;                     // one operand buffer
-constexpr size_t kSeedTcSmem = 3 * kSeedTcBuf + 2048 + 1024;  // act, wA, wB, barriers/scalars, alignment slack
+constexpr int kSeedTcUfLd = 52;                           // row stride of the FP32 copy of the states
+constexpr size_t kSeedTcUf = (size_t)128 * kSeedTcUfLd * 4;
+// act, wA, wB, FP32 states, barriers/scalars, alignment slack
+constexpr size_t kSeedTcSmem = 3 * kSeedTcBuf + kSeedTcUf + 2048 + 1024;
 
 __host__ __device__ constexpr int seed_tc_k1(int n_in) { return (n_in + 7) / 8 * 8; }
 __host__ __device__ constexpr int seed_tc_n4(int n_out) { return (n_out + 15) / 16 * 16; }
@@ -168,7 +181,8 @@ struct SeedTCArgs {
   const float* x_istd;
   const float* y_mean;
   const float* y_std;
-  double* Hseed;              // [elem][q][Np_st]
+  double* Hseed;              // [elem][q][Np_st] (FP64 seed), or
+  float* Hseed_f;             // the same in FP32 for FP32 sweeps (used when non-null)
   unsigned int* status;       // kStatusSeedWait on a wait that gave up
 };
 
@@ -189,11 +203,14 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
   uint8_t* base = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   float* act = (float*)base;
   float* wbuf[2] = {(float*)(base + kSeedTcBuf), (float*)(base + 2 * kSeedTcBuf)};
-  uint64_t* bars = (uint64_t*)(base + 3 * kSeedTcBuf);  // [0], [1]: weight buffers, [2]: MMA done
+  float* uf = (float*)(base + 3 * kSeedTcBuf);          // [row][kSeedTcUfLd]: U_w in FP32
+  uint64_t* bars = (uint64_t*)(base + 3 * kSeedTcBuf + kSeedTcUf);  // [0], [1]: weights, [2]: MMA, [3]: states
   uint32_t* tslot = (uint32_t*)(bars + 4);              // TMEM address
   volatile int* issued_flag = (volatile int*)(tslot + 1); // thread 0 issued this layer's MMAs
   double* rowscale = (double*)(bars + 8);                // 128 doubles after the barriers
-  int* wu_src = (int*)(rowscale + kSeedTcRows);          // NP_ST entries
+  float* rowscale_f = (float*)(rowscale + kSeedTcRows);  // the same in FP32
+  int* wu_src = (int*)(rowscale_f + kSeedTcRows);        // NP_ST entries
+  static_assert(Q * NP_S <= kSeedTcUfLd, "state row exceeds the FP32 copy");
 
   const int t = threadIdx.x, warp = t >> 5;
   const int row0 = blockIdx.x * kSeedTcRows;
@@ -202,6 +219,7 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
     tc::mbar_init(&bars[0], 1);
     tc::mbar_init(&bars[1], 1);
     tc::mbar_init(&bars[2], 1);
+    tc::mbar_init(&bars[3], 1);
     tc::fence_mbar_init();
   }
   if (warp == 0) tc::tmem_alloc(tslot, 128);
@@ -219,29 +237,40 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
 
   uint32_t issued[2] = {0, 0}, waited[2] = {0, 0};  // weight copies per buffer (thread 0)
   uint32_t mma_issued = 0, mma_waited = 0;          // MMA batches (thread 0)
+  const int rows = min(kSeedTcRows, a.n - row0);
+  // the tile's states (rows x Q*Np_s doubles, contiguous) go to weight buffer
+  // 1 first; W2 follows there once the features are built
+  const uint32_t ubytes = (uint32_t)rows * Q * NP_S * 8u;
   if (t == 0) {
-    for (int L = 0; L < 2; ++L) {
-      tc::mbar_expect_tx(&bars[L], wbytes(L));
-      tc::bulk_g2s(wbuf[L], a.wpack + a.w_off[L], wbytes(L), &bars[L]);
-      issued[L]++;
-    }
+    tc::mbar_expect_tx(&bars[0], wbytes(0));
+    tc::bulk_g2s(wbuf[0], a.wpack + a.w_off[0], wbytes(0), &bars[0]);
+    issued[0]++;
+    tc::mbar_expect_tx(&bars[3], ubytes);
+    tc::bulk_g2s(wbuf[1], a.Uw + (size_t)row0 * Q * NP_S, ubytes, &bars[3]);
   }
+  const bool u_ok = tc::mbar_wait(&bars[3], 0);
+  if (!u_ok && t == 0) atomicOr(a.status, kStatusSeedWait);
 
   // ---- features of row r (two threads per row, half the columns each)
   {
     const int r = t & (kSeedTcRows - 1), half = t >> 7;
     const int e = row0 + r;
-    const bool live = e < a.n;
-    double rinv = 1.0, cdt = 0.0;
-    const double* u = a.Uw + (size_t)(live ? e : 0) * Q * NP_S;
+    const bool live = r < rows && u_ok;
+    float rinv = 1.0f;
+    double cdt = 0.0;
+    const double* u = reinterpret_cast<const double*>(wbuf[1]) + (size_t)(live ? r : 0) * Q * NP_S;
     if (live) {
       const double rho = u[0];
-      rinv = 1.0 / rho;
+      rinv = (float)(1.0 / rho);
       const int lev = a.elem_level ? a.elem_level[e] : 0;
       cdt = a.dt[kScalDtDx + 3 * lev];
-      if (half == 0) rowscale[r] = rho * cdt;
+      if (half == 0) {
+        rowscale[r] = rho * cdt;
+        rowscale_f[r] = (float)(rho * cdt);
+      }
     } else if (half == 0) {
       rowscale[r] = 0.0;
+      rowscale_f[r] = 0.0f;
     }
     constexpr int HK = K1 / 2;
 #pragma unroll
@@ -252,7 +281,13 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
         const int f = half * HK + k0 + i;
         float x = 0.0f;
         if (live && f < NIN) {
-          x = (f < Q * NP_S) ? (float)(u[f] * rinv) : (float)cdt;
+          if (f < Q * NP_S) {
+            const float uf32 = (float)u[f];
+            uf[r * kSeedTcUfLd + f] = uf32;
+            x = uf32 * rinv;
+          } else {
+            x = (float)cdt;
+          }
           x = (x - a.x_mean[f]) * a.x_istd[f];
         }
         v[i] = tc::to_tf32(x);
@@ -260,16 +295,21 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
       *reinterpret_cast<float4*>(act + tc::kmajor_off(r, half * HK + k0, K1)) = make_float4(v[0], v[1], v[2], v[3]);
     }
   }
-  tc::fence_proxy_async();
+  tc::fence_proxy_async();  // generic reads of buffer 1 and writes of act before the async proxy
   tc::fence_before_sync();
-  __syncthreads();
+  const bool all_u = __syncthreads_and(u_ok) != 0;
+  if (t == 0 && all_u) {  // the states are read: stream W2 into buffer 1
+    tc::mbar_expect_tx(&bars[1], wbytes(1));
+    tc::bulk_g2s(wbuf[1], a.wpack + a.w_off[1], wbytes(1), &bars[1]);
+    issued[1]++;
+  }
 
-  bool ok = true;
+  bool ok = all_u;
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
   const int r = (warp & 3) * 32 + (t & 31);  // this thread's row in the epilogues
   const int chalf = warp >> 2;                // and its half of the columns
 #pragma unroll 1
-  for (int L = 0; L < 4; ++L) {
+  for (int L = 0; L < 4 && ok; ++L) {
     const int wb = L & 1;
     if (t == 0) {
       bool w_ok = tc::mbar_wait(&bars[wb], waited[wb] & 1);
@@ -322,10 +362,10 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
 #pragma unroll
         for (int i = 0; i < 32; i += 4) {
           float4 o;
-          o.x = tc::to_tf32(mlp::gelu(v[i + 0] + __ldg(b + col0 + i + 0)));
-          o.y = tc::to_tf32(mlp::gelu(v[i + 1] + __ldg(b + col0 + i + 1)));
-          o.z = tc::to_tf32(mlp::gelu(v[i + 2] + __ldg(b + col0 + i + 2)));
-          o.w = tc::to_tf32(mlp::gelu(v[i + 3] + __ldg(b + col0 + i + 3)));
+          o.x = tc::to_tf32(tc::gelu_fast(v[i + 0] + __ldg(b + col0 + i + 0)));
+          o.y = tc::to_tf32(tc::gelu_fast(v[i + 1] + __ldg(b + col0 + i + 1)));
+          o.z = tc::to_tf32(tc::gelu_fast(v[i + 2] + __ldg(b + col0 + i + 2)));
+          o.w = tc::to_tf32(tc::gelu_fast(v[i + 3] + __ldg(b + col0 + i + 3)));
           *reinterpret_cast<float4*>(act + tc::kmajor_off(r, col0 + i, H)) = o;
         }
       }
@@ -348,15 +388,18 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
       tc::fence_before_sync();
       __syncthreads();
       // H_seed, coalesced over the tile's contiguous [rows][NOUT] block
-      const int rows = min(kSeedTcRows, a.n - row0);
-      double* dst = a.Hseed + (size_t)row0 * NOUT;
       for (int i = t; i < rows * NOUT; i += kSeedTcThreads) {
         const int rr = i / NOUT, f = i - rr * NOUT;
         const int q = f / NP_ST, k = f - q * NP_ST;
         const int src = wu_src[k];
-        const double wu = src >= 0 ? a.Uw[((size_t)(row0 + rr) * Q + q) * NP_S + src] : 0.0;
-        const float y = act[rr * YLD + f];
-        dst[i] = wu + rowscale[rr] * (double)(y * __ldg(a.y_std + f) + __ldg(a.y_mean + f));
+        const float y = act[rr * YLD + f] * __ldg(a.y_std + f) + __ldg(a.y_mean + f);
+        if (a.Hseed_f) {
+          const float wu = src >= 0 ? uf[rr * kSeedTcUfLd + q * NP_S + src] : 0.0f;
+          a.Hseed_f[(size_t)row0 * NOUT + i] = fmaf(rowscale_f[rr], y, wu);
+        } else {
+          const double wu = src >= 0 ? a.Uw[((size_t)(row0 + rr) * Q + q) * NP_S + src] : 0.0;
+          a.Hseed[(size_t)row0 * NOUT + i] = wu + rowscale[rr] * (double)y;
+        }
       }
     }
   }
