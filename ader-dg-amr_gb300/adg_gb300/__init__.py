@@ -45,6 +45,7 @@ class AdgConfig(ctypes.Structure):
         ("tag_kind", ctypes.c_int), ("tag_threshold", ctypes.c_double), ("grid_eff", ctypes.c_double),
         ("n_error_buf", ctypes.c_int), ("reflux_box_quirk", ctypes.c_int),
         ("picard_sweeps", ctypes.c_int), ("elems_per_block", ctypes.c_int),
+        ("limiter_t", ctypes.c_int), ("tvb_M", ctypes.c_double), ("tvb_c", ctypes.c_double * 8),
     ]
 
 
@@ -97,6 +98,7 @@ def lib():
         "adg_dof_updates": ([vp, ctypes.POINTER(ctypes.c_int64), dp], i),
         "adg_regrid_profile": ([vp, dp, i], i),
         "adg_leaf_dof_updates": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_limited_count": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
         "adg_seed_set_path": ([vp, i], i),
         "adg_seed_infer": ([vp, vp, i], i),
         "adg_seed_create": ([i, i, i, ctypes.c_uint64, ctypes.POINTER(vp)], i),
@@ -181,13 +183,29 @@ class AmrDG:
         self._L = lib()
 
     # ------------------------------------------------------------ settings
-    def settings(self, T=None, c_dt=0.5, picard_sweeps=0, elems_per_block=0):
-        """AmrDG<P>::settings(T, c_dt, ...) (AmrDG.tpp:49-59)."""
+    def settings(self, T=None, c_dt=0.5, picard_sweeps=0, elems_per_block=0, limiter_type="", TVB_M=0.0,
+                 amr_tvb_c=None, t_limit=-1):
+        """AmrDG<P>::settings / Simulation::setNumericalSettings(T, c_dt,
+        limiter_type, TVB_M, AMR_TVB_C, t_limit) (AmrDG.tpp:49-59,
+        Source/main.cpp:147); limiter_type "TVB" with t_limit > 0 limits the
+        finest level every t_limit steps."""
         self.T = T
         self.cfg.c_dt = float(c_dt)
         self.cfg.picard_sweeps = int(picard_sweeps)
         self.cfg.elems_per_block = int(elems_per_block)
+        if limiter_type not in ("", "TVB"):
+            raise ValueError(f"unknown limiter {limiter_type!r}")
+        self.cfg.limiter_t = int(t_limit) if (limiter_type == "TVB" and t_limit > 0) else 0
+        self.cfg.tvb_M = float(TVB_M)
+        for l in range(8):
+            self.cfg.tvb_c[l] = 1.0 if amr_tvb_c is None or l >= len(amr_tvb_c) else float(amr_tvb_c[l])
         return self
+
+    def setNumericalSettings(self, T=None, c_dt=0.5, limiter_type="", TVB_M=0.0, amr_tvb_c=None, t_limit=-1):
+        """Simulation::setNumericalSettings (Source/main.cpp:147)."""
+        return self.settings(T=T, c_dt=c_dt, picard_sweeps=self.cfg.picard_sweeps,
+                             elems_per_block=self.cfg.elems_per_block, limiter_type=limiter_type, TVB_M=TVB_M,
+                             amr_tvb_c=amr_tvb_c, t_limit=t_limit)
 
     def setGeometrySettings(self, prob_lo, prob_hi, n_cell, max_level=0, periodic=None, max_grid=32,
                             blocking_factor=8, dtn_regrid=4):
@@ -354,15 +372,22 @@ class AmrDG:
 
     def time_kernels(self, nsteps=3):
         """Average per-step duration (ms) of each kernel kind, CUDA events."""
-        out = (ctypes.c_double * 5)()
-        self._check(self._L.adg_time_kernels(self.ctx, int(nsteps), out, 5), "adg_time_kernels")
-        return {"predictor": out[0], "numflux": out[1], "corrector": out[2], "dt": out[3], "amr_sync": out[4]}
+        out = (ctypes.c_double * 6)()
+        self._check(self._L.adg_time_kernels(self.ctx, int(nsteps), out, 6), "adg_time_kernels")
+        return {"predictor": out[0], "numflux": out[1], "corrector": out[2], "dt": out[3], "amr_sync": out[4],
+                "seed_inference": out[5]}
 
     def dof_updates(self):
         """(total DOF updates so far, ms of host time spent in regrids)."""
         n, ms = ctypes.c_int64(), ctypes.c_double()
         self._check(self._L.adg_dof_updates(self.ctx, ctypes.byref(n), ctypes.byref(ms)), "adg_dof_updates")
         return n.value, ms.value
+
+    def limited_count(self):
+        """Elements the TVB limiter has modified so far."""
+        n = ctypes.c_int64()
+        self._check(self._L.adg_limited_count(self.ctx, ctypes.byref(n)), "adg_limited_count")
+        return n.value
 
     def leaf_dof_updates(self):
         """DOF updates so far over leaf elements only."""

@@ -153,6 +153,8 @@ struct adg_ctx {
   std::vector<size_t> ad_off;  // offset (ints) of level lf's records in ad_all
   DevBuf<uint8_t> tags;
   DevBuf<uint8_t> l2_flush;  // written between timed steps to evict the L2
+  DevBuf<double> ubar_old;   // [elem][q] cell means at the start of the step (TVB limiter)
+  DevBuf<unsigned long long> limited;  // elements the limiter modified
   DevBuf<double> Uw_alt;   // regrid target state (swapped with Uw)
   TableView<int> remap_i;     // regrid remap entries: dst | parent | src_old
   TableView<int8_t> remap_c;  // regrid remap child indices
@@ -188,6 +190,7 @@ struct adg_ctx {
     gf_elem.release(); gf_parent.release(); rf_dside.release(); gf_child.release(); tags.release();
     sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); hseed_f.release(); fb_list.release(); fb_count.release();
     fb_total.release(); Uw_alt.release(); remap_i.release(); remap_c.release(); l2_flush.release();
+    ubar_old.release(); limited.release();
     if (tab_ev) cudaEventSynchronize(tab_ev), cudaEventDestroy(tab_ev);
     tab_dev.release();
     if (tab_host) cudaFreeHost(tab_host);
@@ -242,6 +245,7 @@ int upload_tables(adg_ctx* ctx, const RemapTable* rm = nullptr) {
   ADG_CUDA(ctx->Rvol.ensure(ne * Q * ks->Np_s), "alloc Rvol");
   ADG_CUDA(ctx->Tr.ensure(ne * 2 * D * (2 * Q + 1) * (size_t)ks->NQ_BD), "alloc traces");
   ADG_CUDA(ctx->Fnum.ensure(nf * Q * (size_t)ks->NQ_BD), "alloc Fnum");
+  if (ctx->cfg.limiter_t > 0) ADG_CUDA(ctx->ubar_old.ensure(ne * Q), "alloc limiter means");
   if (ctx->seed) {
     const adg_seed* sd = ctx->seed;
     ADG_CUDA(ctx->sx.ensure(ne * sd->n_in), "alloc seed features");
@@ -339,7 +343,7 @@ int upload_tables(adg_ctx* ctx, const RemapTable* rm = nullptr) {
 }
 
 }  // namespace
-int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base);
+int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base, cudaEvent_t* ev);
 namespace {
 
 // ADER of every level with the current device Dt (AmrDG.h:1071-1165).
@@ -358,10 +362,11 @@ int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
   pa.Rvol = ctx->Rvol.p;
   pa.Tr = ctx->Tr.p;
   pa.Hw_out = hw_out;
+  pa.ubar_old = ctx->cfg.limiter_t > 0 ? ctx->ubar_old.p : nullptr;
   if (ev) cudaEventRecord(ev[0], ctx->stream);
   cudaError_t e = cudaSuccess;
   if (ctx->seed_mode && ctx->seed) {
-    int rc = launch_seeded_predictor(ctx, pa);
+    int rc = launch_seeded_predictor(ctx, pa, ev);
     if (rc) return rc;
   } else {
     e = ks->predictor(pa, ctx->E, ctx->stream);
@@ -474,9 +479,38 @@ int launch_dt(adg_ctx* ctx, int advance_time) {
   return ADG_OK;
 }
 
+// TVB limiter of the finest level (AmrDG.h:990-997, 1657-1855).
+int launch_limiter(adg_ctx* ctx) {
+  const Hierarchy& H = ctx->hier;
+  const int F = H.nlevels() - 1;
+  const LevelGeom g = level_geom(ctx);
+  double h = g.dx[F][0];
+  for (int d = 1; d < ctx->cfg.D; ++d) h = std::min(h, g.dx[F][d]);
+  LimiterArgs la{};
+  la.Uw = ctx->Uw.p;
+  la.ubar_old = ctx->ubar_old.p;
+  la.elem_face = ctx->elem_face.p;
+  la.face_left = ctx->face_left.p;
+  la.face_right = ctx->face_right.p;
+  la.e0 = (int)H.level_valid_offset(F);
+  la.n = (int)H.level_valid_count(F);
+  for (int d = 0; d < 3; ++d) la.periodic[d] = ctx->cfg.periodic[d];
+  la.gamma = ctx->cfg.gamma;
+  la.thr = ctx->cfg.tvb_c[F] * ctx->cfg.tvb_M * std::pow(h, 2.0);
+  la.count = ctx->limited.p;
+  cudaError_t e = ctx->ks->limit_tvb(la, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "limiter launch");
+  ctx->launches++;
+  return ADG_OK;
+}
+
 int launch_step(adg_ctx* ctx, cudaEvent_t* ev = nullptr) {
   int rc = launch_ader(ctx, nullptr, ev);
   if (rc) return rc;
+  if (ctx->cfg.limiter_t > 0 && ctx->nstep % ctx->cfg.limiter_t == 0) {
+    rc = launch_limiter(ctx);
+    if (rc) return rc;
+  }
   const bool fork = !ev && ctx->side && ctx->hier.nlevels() > 1 && !ctx->hier.gf_elem.empty();
   if (!fork) {
     rc = launch_amr_sync(ctx);
@@ -678,6 +712,7 @@ int capture_graph(adg_ctx* ctx) {
 }
 
 int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
+  if (ctx->cfg.limiter_t > 1) use_graph = false;  // the step's kernels then differ from step to step
   if (regrid_due(ctx)) {
     auto t0 = std::chrono::steady_clock::now();
     int rc = regrid(ctx);
@@ -685,6 +720,7 @@ int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
     ctx->regrid_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   ctx->dof_updates += (long long)ctx->hier.n_valid() * ctx->ks->Q * ctx->ks->Np_s;
+  if (ctx->seed_mode && ctx->seed) ctx->seed_predicted += (long long)ctx->hier.n_elem();
   ctx->leaf_dof_updates += (long long)ctx->n_leaf * ctx->ks->Q * ctx->ks->Np_s;
   ctx->first_step = false;
   if (use_graph && !ev) {
@@ -716,6 +752,7 @@ int adg_ctx_create(const adg_config* cfg, adg_ctx** out) {
   for (int d = 0; d < cfg->D; ++d)
     if (cfg->n_cell[d] <= 0 || !(cfg->prob_hi[d] > cfg->prob_lo[d])) return ADG_ERR_ARG;
   if (cfg->max_level < 0 || cfg->max_level >= kMaxLevels) return ADG_ERR_ARG;
+  if (cfg->limiter_t < 0 || !(cfg->tvb_M >= 0.0)) return ADG_ERR_ARG;
   if (!(cfg->gamma > 1.0) || !(cfg->c_dt > 0.0)) return ADG_ERR_ARG;
   adg_ctx* ctx = new adg_ctx();
   ctx->cfg = *cfg;
@@ -739,6 +776,7 @@ int adg_ctx_create(const adg_config* cfg, adg_ctx** out) {
     return ADG_ERR_CUDA;
   }
   if (ctx->scal.ensure(kScalCount) != cudaSuccess || ctx->dt_done.ensure(1) != cudaSuccess ||
+      ctx->limited.ensure(1) != cudaSuccess ||
       ctx->min_bits.ensure(1) != cudaSuccess || ctx->status.ensure(1) != cudaSuccess) {
     delete ctx;
     return ADG_ERR_CUDA;
@@ -750,6 +788,7 @@ int adg_ctx_create(const adg_config* cfg, adg_ctx** out) {
   unsigned int zero = 0;
   if (cudaMemcpy(ctx->scal.p, z, sizeof(z), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemset(ctx->dt_done.p, 0, sizeof(unsigned int)) != cudaSuccess ||
+      cudaMemset(ctx->limited.p, 0, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMemcpy(ctx->min_bits.p, &big, sizeof(big), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(ctx->status.p, &zero, sizeof(zero), cudaMemcpyHostToDevice) != cudaSuccess) {
     delete ctx;
@@ -963,6 +1002,7 @@ int adg_ader(adg_ctx* ctx) {
   if (rc) return rc;
   rc = launch_ader(ctx, nullptr);
   if (rc) return rc;
+  if (ctx->seed_mode && ctx->seed) ctx->seed_predicted += (long long)ctx->hier.n_elem();
   ADG_CUDA(cudaStreamSynchronize(ctx->stream), "ader sync");
   return ADG_OK;
 }
@@ -984,6 +1024,15 @@ int adg_advance(adg_ctx* ctx, int nsteps, int use_graph) {
     rc = host_step(ctx, use_graph != 0);
     if (rc) return rc;
   }
+  return ADG_OK;
+}
+
+int adg_limited_count(adg_ctx* ctx, int64_t* n) {
+  if (!ctx || !n) return ADG_ERR_ARG;
+  unsigned long long v = 0;
+  ADG_CUDA(cudaMemcpyAsync(&v, ctx->limited.p, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream), "limited count");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "limited count");
+  *n = (int64_t)v;
   return ADG_OK;
 }
 
@@ -1151,16 +1200,19 @@ int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds) {
   int rc = check_ready(ctx);
   if (rc) return rc;
   if (!ms || nkinds < 1 || nsteps < 1) return ADG_ERR_ARG;
-  const int NEV = 6;
+  const int NEV = 7;
+  const bool seeded = ctx->seed_mode && ctx->seed;
   std::vector<cudaEvent_t> ev((size_t)NEV * nsteps);
   for (auto& x : ev) ADG_CUDA(cudaEventCreate(&x), "event");
   for (int s = 0; s < nsteps && rc == ADG_OK; ++s) rc = host_step(ctx, false, &ev[(size_t)s * NEV]);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
-  double acc[5] = {0, 0, 0, 0, 0};
+  double acc[6] = {0, 0, 0, 0, 0, 0};
   if (rc == ADG_OK && e == cudaSuccess) {
-    const int from[5] = {0, 1, 2, 4, 3}, to[5] = {1, 2, 3, 5, 4};
+    // kinds: predictor stage, numflux, corrector, Dt, AMR sync, seed inference
+    const int from[6] = {0, 1, 2, 4, 3, 0}, to[6] = {1, 2, 3, 5, 4, 6};
     for (int s = 0; s < nsteps; ++s)
-      for (int k = 0; k < 5; ++k) {
+      for (int k = 0; k < 6; ++k) {
+        if (k == 5 && !seeded) continue;
         float f = 0.f;
         cudaEventElapsedTime(&f, ev[(size_t)s * NEV + from[k]], ev[(size_t)s * NEV + to[k]]);
         acc[k] += f;
@@ -1169,7 +1221,7 @@ int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds) {
   for (auto& x : ev) cudaEventDestroy(x);
   if (rc) return rc;
   if (e != cudaSuccess) return cuda_fail(ctx, e, "time kernels");
-  for (int k = 0; k < nkinds; ++k) ms[k] = (k < 5) ? acc[k] / nsteps : 0.0;
+  for (int k = 0; k < nkinds; ++k) ms[k] = (k < 6) ? acc[k] / nsteps : 0.0;
   return ADG_OK;
 }
 
@@ -1442,7 +1494,7 @@ int seed_infer(adg_ctx* ctx, double* dst, int path, float* dst_f = nullptr) {
   return ADG_OK;
 }
 
-int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base) {
+int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base, cudaEvent_t* ev) {
   const int n = (int)ctx->hier.n_elem();
   const KernelSet* ks = ctx->ks;
   cudaStream_t st = ctx->stream;
@@ -1450,6 +1502,7 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base) {
   const bool f32 = ctx->seed_mode == 2 && ctx->seed_path == 1 && ctx->seed->packed;
   int rc = seed_infer(ctx, ctx->hseed.p, ctx->seed_path, f32 ? ctx->hseed_f.p : nullptr);
   if (rc) return rc;
+  if (ev) cudaEventRecord(ev[6], st);  // end of the seed inference (stage timing)
   cudaError_t e;
   ADG_CUDA(cudaMemsetAsync(ctx->fb_count.p, 0, sizeof(int), st), "fallback reset");
   PredictorArgs pa = base;
@@ -1468,7 +1521,6 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base) {
   e = ks->predictor(fb, ctx->E, st, 0);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "fallback predictor");
   ctx->launches += 2;
-  ctx->seed_predicted += n;
   return ADG_OK;
 }
 

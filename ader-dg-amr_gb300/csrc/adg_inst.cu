@@ -136,6 +136,11 @@ struct Impl final : KernelSet {
     k_seed_infer_tc<O><<<(a.n + kSeedTcRows - 1) / kSeedTcRows, kSeedTcThreads, kSeedTcSmem, s>>>(a);
     return cudaGetLastError();
   }
+  cudaError_t limit_tvb(const LimiterArgs& a, cudaStream_t s) const override {
+    if (a.n <= 0) return cudaSuccess;
+    k_limit_tvb<O><<<(a.n + 127) / 128, 128, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const override {
     const int bs = 64;
     k_init_ic<O><<<(a.n_elem + bs - 1) / bs, bs, 0, s>>>(a);

@@ -52,6 +52,7 @@ struct PredictorArgs {
   const int* elem_list;
   const int* list_count;
   unsigned long long* count_total;
+  double* ubar_old;           // optional [elem][q]: cell means at the start of the step (TVB limiter)
 };
 
 // Point-wise flux stage: H at NQ points of E elements (shared, [point][col])
@@ -166,6 +167,7 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   const double* src = a.Uw + ((size_t)e * Q + q) * NP_S;
 #pragma unroll
   for (int n = 0; n < NP_S; ++n) u[n] = src[n];
+  if (a.ubar_old && live) a.ubar_old[(size_t)e * Q + q] = u[0];
 
   double wu[NP_ST];
   O::wu(RegIn{u}, RegOut{wu});
@@ -548,6 +550,188 @@ __global__ void k_corrector(CorrectorArgs a) {
 #pragma unroll
   for (int n = 0; n < NP_S; ++n) dst[n] = R[n];
 }
+
+// ---------------------------------------------------------------------------
+// TVB limiter (Limiter_w / Limiter_linear_tvb, AmrDG.h:1657-1855; minmod /
+// minmodB, AmrDG_Limiter.tpp:40-85; eigenvectors, Compressible_Euler.cpp:
+// 138-276).  IEEE operations in the reference's order without contraction,
+// so the troubled-cell decisions are the ones the CPU oracle makes.
+// ---------------------------------------------------------------------------
+#define ADG_M(a, b) __dmul_rn((a), (b))
+#define ADG_A(a, b) __dadd_rn((a), (b))
+#define ADG_S(a, b) __dsub_rn((a), (b))
+#define ADG_V(a, b) __ddiv_rn((a), (b))
+
+template <int D>
+__device__ __forceinline__ void euler_eigenvectors(int d, const double* u, double gamma, double R[D + 2][D + 2],
+                                                   double L[D + 2][D + 2]) {
+  // Soundspeed / Pressure (Compressible_Euler.h:562-604)
+  double prs = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) prs = ADG_A(prs, ADG_V(ADG_M(u[k + 1], u[k + 1]), u[0]));
+  prs = ADG_M(prs, -0.5);
+  prs = ADG_A(prs, u[D + 1]);
+  prs = ADG_M(prs, ADG_S(gamma, 1.0));
+  prs = (prs < kPdeLimit) ? kPdeLimit : prs;
+  const double rho = (u[0] < kPdeLimit) ? kPdeLimit : u[0];
+  const double c = __dsqrt_rn(ADG_M(gamma, ADG_V(prs, rho)));
+  const double g = ADG_S(gamma, 1.0);
+  const double u1 = ADG_V(u[1], u[0]), u2 = ADG_V(u[2], u[0]);
+  const double u3 = (D == 3) ? ADG_V(u[D == 3 ? 3 : 2], u[0]) : 0.0;
+  double ek = ADG_A(ADG_M(u1, u1), ADG_M(u2, u2));
+  if (D == 3) ek = ADG_A(ek, ADG_M(u3, u3));
+  ek = ADG_M(0.5, ek);
+  const double c2 = ADG_M(c, c);
+  const double h = ADG_A(ADG_V(c2, g), ek);
+  const double beta = ADG_V(1.0, ADG_M(2.0, c2));
+  const double phi = ADG_M(g, ek);
+  const double mb = -beta, b2 = ADG_M(2.0, beta), mb2 = ADG_M(-2.0, beta);
+  const double bg = ADG_M(beta, g), mbg = ADG_M(mb, g), b2g = ADG_M(b2, g), mb2g = ADG_M(mb2, g);
+  const double row1[5] = {ADG_S(1.0, ADG_M(b2, phi)), ADG_M(b2g, u1), ADG_M(b2g, u2), ADG_M(b2g, u3), mb2g};
+  const double uv[3] = {u1, u2, u3};
+  const double ud = uv[d];
+  // rows 0 and 2: the acoustic waves of direction d; in row 2 the reference
+  // writes the first other component as -beta*(gamma*u) and a second one
+  // (3D) as -beta*gamma*u, which round differently
+  const int kp = (d == 0) ? 1 : 0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const double uk = uv[k];
+    L[0][k + 1] = (k == d) ? ADG_M(mb, ADG_A(ADG_M(g, uk), c)) : ADG_M(mbg, uk);
+    L[2][k + 1] = (k == d) ? ADG_M(mb, ADG_S(ADG_M(g, uk), c)) : (k == kp ? ADG_M(mb, ADG_M(g, uk)) : ADG_M(mbg, uk));
+  }
+  L[0][0] = ADG_M(beta, ADG_A(phi, ADG_M(c, ud)));
+  L[2][0] = ADG_M(beta, ADG_S(phi, ADG_M(c, ud)));
+  L[0][D + 1] = bg;
+  L[2][D + 1] = bg;
+#pragma unroll
+  for (int k = 0; k < D + 1; ++k) L[1][k] = row1[k];
+  L[1][D + 1] = mb2g;
+  // rows 3 (and 4): the shear waves, and R, as listed per direction
+#pragma unroll
+  for (int i = 0; i < D + 2; ++i)
+#pragma unroll
+    for (int j = 0; j < D + 2; ++j) R[i][j] = 0.0;
+  R[0][0] = 1.0; R[0][1] = 1.0; R[0][2] = 1.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const double uk = uv[k];
+    R[k + 1][0] = (k == d) ? ADG_S(uk, c) : uk;
+    R[k + 1][1] = uk;
+    R[k + 1][2] = (k == d) ? ADG_A(uk, c) : uk;
+  }
+  R[D + 1][0] = ADG_S(h, ADG_M(c, ud));
+  R[D + 1][1] = ek;
+  R[D + 1][2] = ADG_A(h, ADG_M(c, ud));
+  if (D == 2) {
+    const double s0[2][4] = {{u2, 0.0, -1.0, 0.0}, {-u1, 1.0, 0.0, 0.0}};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) L[3][j] = s0[d][j];
+    if (d == 0) { R[2][3] = -1.0; R[3][3] = -u2; }
+    else        { R[1][3] = 1.0;  R[3][3] = u1; }
+  } else {
+    double l3[5] = {0, 0, 0, 0, 0}, l4[5] = {0, 0, 0, 0, 0};
+    if (d == 0) {
+      l3[0] = u2; l3[2] = -1.0; l4[0] = -u3; l4[3] = 1.0;
+      R[2][3] = -1.0; R[3][4] = 1.0; R[4][3] = -u2; R[4][4] = u3;
+    } else if (d == 1) {
+      l3[0] = -u1; l3[1] = 1.0; l4[0] = u3; l4[3] = -1.0;
+      R[1][3] = 1.0; R[3][4] = -1.0; R[4][3] = u1; R[4][4] = -u3;
+    } else {
+      l3[0] = u1; l3[1] = -1.0; l4[0] = -u2; l4[2] = 1.0;
+      R[1][3] = -1.0; R[2][4] = 1.0; R[4][3] = -u1; R[4][4] = u2;
+    }
+#pragma unroll
+    for (int j = 0; j < D + 2; ++j) {
+      L[3][j] = l3[j];
+      L[D == 3 ? 4 : 3][j] = l4[j];
+    }
+  }
+}
+
+__device__ __forceinline__ double minmod3(double a1, double a2, double a3) {
+  const bool same = (signbit(a1) == signbit(a2)) && (signbit(a2) == signbit(a3));
+  if (!same) return 0.0;
+  const double m = fmin(fabs(a1), fmin(fabs(a2), fabs(a3)));
+  return signbit(a1) ? -m : m;
+}
+
+struct LimiterArgs {
+  double* Uw;
+  const double* ubar_old;  // [elem][q] cell means at the start of the step
+  const int* elem_face;
+  const int* face_left;
+  const int* face_right;
+  int e0, n;               // the finest level's valid elements
+  int periodic[3];
+  double gamma;
+  double thr;              // AMR_TVB_C[l] * M * h^2
+  unsigned long long* count;
+};
+
+template <class O>
+__global__ void k_limit_tvb(LimiterArgs a) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int e = a.e0 + i;
+  double ub[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) ub[q] = a.Uw[((size_t)e * Q + q) * NP_S];
+  double res[D][Q];
+  bool troubled = false;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const int s = O::lin_mode(d);
+    const int lo = a.face_left[a.elem_face[(size_t)e * 2 * D + 2 * d]];
+    const int hi = a.face_right[a.elem_face[(size_t)e * 2 * D + 2 * d + 1]];
+    // a physical-boundary neighbour is the element itself: the reference's
+    // ghost there holds the copy made at the start of the step
+    const bool bnd = !a.periodic[d];
+    double um[Q], up[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      um[q] = (bnd && lo == e) ? a.ubar_old[(size_t)e * Q + q] : a.Uw[((size_t)lo * Q + q) * NP_S];
+      up[q] = (bnd && hi == e) ? a.ubar_old[(size_t)e * Q + q] : a.Uw[((size_t)hi * Q + q) * NP_S];
+    }
+    double R[Q][Q], L[Q][Q], v[Q];
+    euler_eigenvectors<D>(d, ub, a.gamma, R, L);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      double Dm = 0.0, Dp = 0.0, Du = 0.0;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        const double hl = ADG_M(0.5, L[q][k]);
+        Dm = ADG_A(Dm, ADG_M(hl, ADG_S(ub[k], um[k])));
+        Dp = ADG_A(Dp, ADG_M(hl, ADG_S(up[k], ub[k])));
+        Du = ADG_A(Du, ADG_M(L[q][k], a.Uw[((size_t)e * Q + k) * NP_S + s]));
+      }
+      v[q] = (fabs(Du) <= a.thr) ? Du : minmod3(Du, Dm, Dp);
+      troubled = troubled || (v[q] != Du);
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      double sum = 0.0;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) sum = ADG_A(sum, ADG_M(R[q][k], v[k]));
+      res[d][q] = sum;
+    }
+  }
+  if (!troubled) return;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    double* uq = a.Uw + ((size_t)e * Q + q) * NP_S;
+#pragma unroll
+    for (int n = 1; n < NP_S; ++n) uq[n] = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) uq[O::lin_mode(d)] = res[d][q];
+  }
+  if (a.count) atomicAdd(a.count, 1ull);
+}
+#undef ADG_M
+#undef ADG_A
+#undef ADG_S
+#undef ADG_V
 
 // Time step (AmrDG.h:1253-1357): dt_cell = CFL * dx_avg / lambda(U at spatial
 // quadrature point 0); block minimum then a global atomic minimum on the

@@ -31,6 +31,7 @@ struct KernelSet {
                                     const int8_t* elem_level, const LevelGeom& geom, const double* dt, double* Hseed,
                                     cudaStream_t s) const = 0;
   virtual cudaError_t seed_infer_tc(const SeedTCArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t limit_tvb(const LimiterArgs& a, cudaStream_t s) const = 0;
 };
 
 const KernelSet* kernels_D2P1();

@@ -779,6 +779,14 @@ def generate(D, P, out_path):
                + sum(counts[f"face_eval{d}{s}"] for d in range(D) for s in range(2))
                + sum(counts[f"bd_term{d}{s}"] for d in range(D) for s in range(2)) + 4 * el.Np_s)
     hdr.append(f"  static constexpr int LINEAR_FP64_PER_COLUMN = {per_col};")
+    # spatial mode of degree 1 in direction d and 0 in the others (the TVB
+    # limiter's slope modes, lin_mode_idx of AmrDG.tpp:174-183)
+    lin = []
+    for d in range(D):
+        lin.append(next(n for n, mi in enumerate(el.mi_s)
+                        if mi[d] == 1 and all(mi[a] == 0 for a in range(D) if a != d)))
+    hdr.append("  static __device__ __forceinline__ int lin_mode(int d) { return "
+               + " : ".join(f"d == {d} ? {lin[d]}" for d in range(D - 1)) + f" : {lin[D - 1]}; }}")
     hdr.append("};")
     hdr.append("}}  // namespace")
     hdr.append("")

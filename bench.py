@@ -40,8 +40,10 @@ WORKLOADS = {
                        amr=dict(max_level=2, max_grid=32, blocking_factor=8, dtn_regrid=4, tag_kind=0,
                                 tag_threshold=0.1)),
     # config 5: 3D blast, 2 levels
+    # (the unlimited scheme does not survive this blast: TVB limiter as the
+    # reference's shock presets use it, every step, M = 10)
     "blast3d_p2_amr2": dict(D=3, P=2, n=(64, 64, 64), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), periodic=(0, 0, 0),
-                            ic="blast3d", c_dt=0.5,
+                            ic="blast3d", c_dt=0.5, limiter=dict(TVB_M=10.0, t_limit=1),
                             amr=dict(max_level=1, max_grid=32, blocking_factor=8, dtn_regrid=4, tag_kind=1,
                                      tag_threshold=0.1)),
     "kh_p3_256": dict(D=2, P=3, n=(256, 256, 1), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), periodic=(1, 1, 1),
@@ -148,7 +150,9 @@ def make_sim(G, w, E=0, sweeps=0, seed=None, noise_amp=None):
                           blocking_factor=amr.get("blocking_factor", 8), dtn_regrid=amr.get("dtn_regrid", 4))
     if amr:
         s.setAmrSettings(tag_kind=amr["tag_kind"], tag_threshold=amr["tag_threshold"])
-    s.settings(c_dt=w["c_dt"], elems_per_block=E, picard_sweeps=sweeps)
+    lim = w.get("limiter")
+    s.settings(c_dt=w["c_dt"], elems_per_block=E, picard_sweeps=sweeps,
+               **(dict(limiter_type="TVB", TVB_M=lim["TVB_M"], t_limit=lim["t_limit"]) if lim else {}))
     w = dict(w)
     if seed is not None:
         w["seed"] = seed
@@ -203,6 +207,7 @@ def cpu_baseline(w, max_seconds=20.0, threads=None):
                      max_level=amr.get("max_level", 0), blocking_factor=amr.get("blocking_factor", 8),
                      dtn_regrid=amr.get("dtn_regrid", 4), tag_kind=amr.get("tag_kind", 0),
                      tag_threshold=amr.get("tag_threshold", 0.1),
+                     **({"t_limit": w["limiter"]["t_limit"], "tvb_M": w["limiter"]["TVB_M"]} if "limiter" in w else {}),
                      **{k: w[k] for k in ("seed", "noise_amp", "u_inf", "v_inf") if k in w})
     s = O.OracleSim(cfg)
     s.init()
@@ -226,7 +231,7 @@ def cpu_baseline(w, max_seconds=20.0, threads=None):
 def base_config(args, w, world):
     """The workload keys both arms report."""
     return {"workload": args.workload, "D": w["D"], "P": w["P"], "base_cells": list(w["n"][:w["D"]]),
-            "amr": w.get("amr"), "ic": w["ic"], "c_dt": w["c_dt"],
+            "amr": w.get("amr"), "ic": w["ic"], "c_dt": w["c_dt"], "limiter": w.get("limiter"),
             "parallelism": "replicas" if world > 1 else "1 GPU"}
 
 
@@ -286,6 +291,20 @@ def l2_density_level0(Ua, Ub, w):
 
 L2_FLUSH_BYTES = 256 << 20  # twice the 129 MB L2: written before every timed step
 
+# DRAM bytes (read + write) of one plain k_predictor launch, from the ncu
+# capture summarised in the named profile (same workload and code)
+PROFILED_TRAFFIC = {
+    "kh_p3_amr3": (33.52e6, "profiles/k_predictor_kh_p3_amr3.md"),
+}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
 SEED_VARIANTS = {"seed_1sweep_fp64": dict(mode=1, sweeps=1),
                  "seed_2sweeps_fp32": dict(mode=2, sweeps=2),
                  "seed_3sweeps_fp32": dict(mode=2, sweeps=3)}
@@ -297,7 +316,8 @@ def seed_cache_path(name):
 
 def train_seed(G, w, n_pairs=2_000_000, epochs=40, cache=None):
     """Learned seed trained on pairs from the Picard predictor (8 sweeps) of
-    perturbed single-level and AMR runs of the workload's configuration.
+    perturbed single-level and AMR runs of the workload's configuration (2D),
+    or of the workload's own AMR run (3D).
     With `cache` (a file path), reuse the parameters stored there by an
     earlier run of the same workload, or store them after training."""
     import numpy as np
@@ -313,6 +333,17 @@ def train_seed(G, w, n_pairs=2_000_000, epochs=40, cache=None):
     single.pop("amr", None)
     single["n"] = tuple((w["n"][d] << w["amr"]["max_level"]) if d < w["D"] else 1 for d in range(3)) if "amr" in w else w["n"]
     k = 0
+    if w["D"] == 3:
+        # the 3D blast has no seeded perturbation and a 128^3 single level is
+        # heavy: pairs from the workload's own AMR run, spread over its course
+        s = make_sim(G, base)
+        for st in range(100):
+            if st % 12 == 11:
+                seed.collect(s, target_sweeps=8)
+                if seed.num_samples() >= n_pairs:
+                    break
+            s.time_integration()
+        s.close()
     while seed.num_samples() < n_pairs and k < 16:
         cfgw = single if k % 2 == 0 else base
         s = make_sim(G, cfgw, seed=1000 + k, noise_amp=1e-3 * (1 + k % 4))
@@ -459,6 +490,31 @@ def run_ours(args, w):
     el_per_step = plain["dof"] / args.steps / (Q * Nps)
     peak = G.fp64_peak_gflops() / 1e3
     achieved = alg_pred * el_per_step / (km_plain["predictor"] * 1e-3) / 1e12
+    traffic, traffic_src = PROFILED_TRAFFIC.get(args.workload, (None, None))
+    seed_roof = None
+    if head_name.startswith("seed") and km_head.get("seed_inference", 0.0) > 0.0:
+        # seeded path: FP64 corrector volume term + face traces in the seeded
+        # predictor, TF32 network on the tensor cores, time-weighted blend
+        D, P = w["D"], w["P"]
+        Nst, qst = comb(P + D + 1, D + 1), (P + 1) ** (D + 1)
+        n_in, n_out, hid = Q * Nps + 1, Q * Nst, 128
+        f64 = 2 * Q * qst * Nst + 2 * D * 2 * Q * qbd * Nst + 2 * Q * D * Nps * qst + 2 * Q * Nps
+        tf32 = 2 * (n_in * hid + 2 * hid * hid + hid * n_out)
+        t_inf = km_head["seed_inference"]
+        t_pred = km_head["predictor"] - t_inf
+        tf32_peak = measured_peaks().get("bf16_tflops", 1900.0) / 2.0
+        a64 = f64 * el_per_step / (t_pred * 1e-3) / 1e12
+        a32 = tf32 * el_per_step / (t_inf * 1e-3) / 1e12
+        seed_roof = {
+            "fp64": {"kernel": "k_predictor (seeded: corrector volume term + face traces in FP64)",
+                     "algorithmic_flops_per_element": f64, "ms": t_pred, "achieved": a64, "peak": peak,
+                     "unit": "TFLOP/s", "frac": a64 / peak},
+            "tf32_tensor": {"kernel": "k_seed_infer_tc (4 layers, tcgen05 kind::tf32)",
+                            "algorithmic_flops_per_element": tf32, "ms": t_inf, "achieved": a32,
+                            "peak": tf32_peak, "unit": "TFLOP/s", "frac": a32 / tf32_peak,
+                            "peak_source": "half the measured dense bf16 burst (MEASURED_PEAKS.json)"},
+            "blended_frac": (a64 / peak * t_pred + a32 / tf32_peak * t_inf) / (t_pred + t_inf),
+        }
     with ClockSampler(local) as clk:
         clk_ms = head["sim"].advance_timed(min(args.steps, 50), use_graph=True)
     clocks = clk.summary()
@@ -473,9 +529,11 @@ def run_ours(args, w):
         "e2e": {"value": e2e_val, "unit": "DOF-updates/s", "h2d_bytes_per_step": h2d // e2e_steps,
                 "d2h_bytes_per_step": d2h // e2e_steps},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                     "seed_path": seed_roof,
                      "kernel": "k_predictor (plain FP64 path of this workload)", "kernel_ms": km_plain["predictor"],
                      "algorithmic_flops_per_element": alg_pred, "elements_per_launch": el_per_step,
+                     "elements_note": "valid elements of all levels (the launch also runs the coarse-fine ghosts)",
                      "issued_linear_fp64_per_element": issued,
                      "peak_source": "DFMA-chain probe on this GPU in this run (MEASURED_PEAKS.json has no FP64 figure)"},
         "kernel_ms": {"plain": km_plain, "headline": km_head},

@@ -65,6 +65,15 @@ typedef struct adg_config {
   int reflux_box_quirk;     /* 1: reference's per-box reflux mask (AmrDG_Interpolater.tpp:41-56) */
   int picard_sweeps;        /* predictor sweeps; <= 0 means P (AmrDG.h:1103-1119) */
   int elems_per_block;      /* 0: autotuned default */
+  /* TVB limiter of the finest level after every limiter_t-th ADER step
+   * (AmrDG.h:990-997, Limiter_w AmrDG.h:1657-1855; 0: off): a linear mode is
+   * kept where |slope| <= tvb_c[l] * tvb_M * h^2 (h the level's smallest cell
+   * size), else the characteristic minmod of the slope and the neighbours'
+   * mean differences (limiter_type "TVB", TVB_M, AMR_TVB_C, t_limit of
+   * setNumericalSettings, Source/main.cpp:147). */
+  int limiter_t;
+  double tvb_M;
+  double tvb_c[8];
 } adg_config;
 
 typedef struct adg_ctx adg_ctx;
@@ -121,6 +130,9 @@ int adg_dof_updates(const adg_ctx* ctx, int64_t* total, double* regrid_ms);
 /* The same count over leaf elements only (valid elements not covered by a
  * finer level).  No reference counterpart. */
 int adg_leaf_dof_updates(const adg_ctx* ctx, int64_t* total);
+/* Elements the TVB limiter has modified so far (the reference's
+ * n_limited_total, AmrDG.h:996). */
+int adg_limited_count(adg_ctx* ctx, int64_t* n);
 /* Host wall time of the regrids so far by phase, ms[0..n) with n <= 6:
  * [0] tag kernels and the wait for the state, [1] clustering,
  * [2] hierarchy and remap tables, [3] table upload, [4] remap launches,
@@ -169,8 +181,10 @@ int adg_advance_timed_flushed(adg_ctx* ctx, int nsteps, int use_graph, int64_t f
 
 /* n steps with CUDA events around every kernel on the context's stream;
  * ms[k] receives the average duration of kernel kind k per step:
- * 0 predictor (+ corrector volume term and face traces), 1 numerical flux,
- * 2 corrector update, 3 time-step reduction, 4 AMR synchronisation. */
+ * 0 predictor (+ corrector volume term and face traces; with a seed
+ * attached: the seed inference, the seeded predictor and the fallback),
+ * 1 numerical flux, 2 corrector update, 3 time-step reduction, 4 AMR
+ * synchronisation, 5 the seed inference alone (0 without a seed). */
 int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds);
 
 /* Page-locked host buffers for host<->device state copies. */

@@ -38,6 +38,11 @@ struct AmrConfig {
   double grid_eff = 0.7;
   int n_error_buf = 1;
   int reflux_box_quirk = 1;
+  // TVB limiter (AmrDG.h:995-997): every t_limit steps (0: off), threshold
+  // tvb_c[l] * tvb_M * h^2
+  int t_limit = 0;
+  double tvb_M = 0.0;
+  double tvb_c[8] = {1, 1, 1, 1, 1, 1, 1, 1};
 };
 
 namespace A = adg::amr;
@@ -50,6 +55,7 @@ class AmrSim {
   std::vector<std::vector<A::IBox>> grids;
   bool first_step = true;
   int n_regrids = 0;
+  long n_limited = 0;
 
   AmrSim(const SimConfig& s, const AmrConfig& a) : sim(s), amr(a) {
     gp.D = s.D;
@@ -642,6 +648,8 @@ class AmrSim {
       first_step = false;
     }
     ader();
+    // limiter on the finest level only (AmrDG.h:990-997)
+    if (amr.t_limit > 0 && sim.nstep % amr.t_limit == 0) n_limited += limit_tvb(finest());
     for (int l = finest(); l > 0; --l) average_down(l);
     if (amr.max_level > 0)
       for (int l = 0; l <= finest(); ++l) fill_patch(l);
@@ -649,6 +657,74 @@ class AmrSim {
     sim.t += sim.Dt;
     sim.Dt = sim.compute_Dt();
     return sim.Dt;
+  }
+
+  // TVB limiter of one level (Limiter_w + Limiter_linear_tvb,
+  // AmrDG.h:1657-1855): after FillBoundary, per valid cell and direction the
+  // left eigenvectors at the cell means project the linear mode and the
+  // halved differences to the neighbours' means; minmodB limits each
+  // characteristic slope; if any changed, all modes above the mean are
+  // dropped and the linear modes take the right-eigenvector images.  The
+  // cell means are never written, so the cells are independent.
+  int limit_tvb(int l) {
+    sim.fill_internal(l);
+    Level& L = sim.lev[l];
+    const int Dd = D(), Q = sim.Q, Ns = sim.Np_s;
+    double h = L.dx[0];
+    for (int d = 1; d < Dd; ++d) h = std::min(h, L.dx[d]);
+    const double thr = amr.tvb_c[l] * amr.tvb_M * std::pow(h, 2.0);
+    int lin[3] = {0, 0, 0};
+    for (int d = 0; d < Dd; ++d)
+      for (int n = 0; n < Ns; ++n) {
+        bool ok = sim.el.mi_s[n][d] == 1;
+        for (int a = 0; a < Dd; ++a)
+          if (a != d && sim.el.mi_s[n][a] != 0) ok = false;
+        if (ok) {
+          lin[d] = n;
+          break;
+        }
+      }
+    auto U = [&](int q, int n, long c) -> double& { return L.Uw[((size_t)q * Ns + n) * L.ncell + c]; };
+    int count = 0;
+#pragma omp parallel for schedule(static) reduction(+ : count)
+    for (long c = 0; c < L.ncell; ++c) {
+      if (L.status[c] != ST_VALID) continue;
+      int ijk[3];
+      L.coords(c, ijk[0], ijk[1], ijk[2]);
+      double ub[5], res[3][5];
+      for (int q = 0; q < Q; ++q) ub[q] = U(q, 0, c);
+      bool troubled = false;
+      for (int d = 0; d < Dd; ++d) {
+        int a[3] = {ijk[0], ijk[1], ijk[2]}, b[3] = {ijk[0], ijk[1], ijk[2]};
+        a[d] -= 1;
+        b[d] += 1;
+        const long cm = L.cell(a[0], a[1], a[2]), cp = L.cell(b[0], b[1], b[2]);
+        double R[5][5], Lm[5][5], v[5];
+        eigenvectors(d, ub, Dd, sim.cfg.gamma, R, Lm);
+        for (int q = 0; q < Q; ++q) {
+          double Dm = 0.0, Dp = 0.0, Du = 0.0;
+          for (int k = 0; k < Q; ++k) {
+            Dm += 0.5 * Lm[q][k] * (ub[k] - U(k, 0, cm));
+            Dp += 0.5 * Lm[q][k] * (U(k, 0, cp) - ub[k]);
+            Du += Lm[q][k] * U(k, lin[d], c);
+          }
+          v[q] = minmodB(Du, Dm, Dp, thr);
+          troubled = troubled || (v[q] != Du);
+        }
+        for (int q = 0; q < Q; ++q) {
+          double sum = 0.0;
+          for (int k = 0; k < Q; ++k) sum += R[q][k] * v[k];
+          res[d][q] = sum;
+        }
+      }
+      if (!troubled) continue;
+      for (int q = 0; q < Q; ++q) {
+        for (int n = 1; n < Ns; ++n) U(q, n, c) = 0.0;
+        for (int d = 0; d < Dd; ++d) U(q, lin[d], c) = res[d][q];
+      }
+      ++count;
+    }
+    return count;
   }
 
   void predictor_only(int l) {

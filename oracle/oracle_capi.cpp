@@ -30,6 +30,9 @@ struct oracle_cfg {
   double grid_eff;
   int n_error_buf;
   int reflux_box_quirk;  // 1: reproduce the reference's per-box reflux mask
+  int t_limit;           // TVB limiter every t_limit steps (0: off)
+  double tvb_M;
+  double tvb_c[8];       // per-level TVB coefficient
 };
 
 void* oracle_create(const oracle_cfg* c) {
@@ -62,6 +65,9 @@ void* oracle_create(const oracle_cfg* c) {
   a.grid_eff = c->grid_eff > 0 ? c->grid_eff : 0.7;
   a.n_error_buf = c->n_error_buf >= 0 ? c->n_error_buf : 1;
   a.reflux_box_quirk = c->reflux_box_quirk;
+  a.t_limit = c->t_limit;
+  a.tvb_M = c->tvb_M;
+  for (int l = 0; l < 8; ++l) a.tvb_c[l] = c->tvb_c[l];
   try {
     return new AmrSim(s, a);
   } catch (...) {
@@ -70,6 +76,8 @@ void* oracle_create(const oracle_cfg* c) {
 }
 
 void oracle_destroy(void* h) { delete (AmrSim*)h; }
+
+long oracle_limited_count(void* h) { return ((AmrSim*)h)->n_limited; }
 
 int oracle_set_threads(int n) {
 #ifdef _OPENMP

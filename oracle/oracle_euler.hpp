@@ -7,6 +7,7 @@
 //   pde_dflux       Source/Model/CompressibleEuler/Compressible_Euler.h:489-518
 //   pde_cfl_lambda  Source/Model/CompressibleEuler/Compressible_Euler.cpp:57-70
 //   PDE_NUMERIC_LIMIT = 10*eps   Compressible_Euler.cpp:50-55
+//   pde_EV_Rmatrix / Lmatrix     Compressible_Euler.cpp:138-276
 //   pde_IC (vortex, KH)          Compressible_Euler.h:120-368
 // The KH variant with sin(4 pi x) + seeded noise and the 3D blast IC are the
 // synthetic workloads of this project; the reference has no 3D IC
@@ -188,6 +189,96 @@ inline double pde_IC(int q, const double* x, int D, double gamma, const ICParams
     }
     return rho * v[q - 1];
   }
+}
+
+// Right / left eigenvectors of the flux Jacobian in direction d at state u
+// (the cell means), R[q][q'] and L[q][q'] as the reference lists them
+// (Compressible_Euler.cpp:138-276), same expressions in the same order.
+inline void eigenvectors(int d, const double* u, int D, double gamma, double R[5][5], double L[5][5]) {
+  const double c = soundspeed(u, D, gamma);
+  const double g = gamma - 1.0;
+  if (D == 2) {
+    const double u1 = u[1] / u[0], u2 = u[2] / u[0];
+    const double ek = 0.5 * (std::pow(u1, 2) + std::pow(u2, 2));
+    const double h = (std::pow(c, 2) / (gamma - 1.0)) + ek;
+    const double beta = 1.0 / (2.0 * std::pow(c, 2));
+    const double phi = g * ek;
+    if (d == 0) {
+      const double r[4][4] = {{1.0, 1.0, 1.0, 0.0}, {u1 - c, u1, u1 + c, 0.0}, {u2, u2, u2, -1.0},
+                              {h - c * u1, ek, h + c * u1, -u2}};
+      const double l[4][4] = {{beta * (phi + c * u1), -beta * (g * u1 + c), -beta * g * u2, beta * g},
+                              {1.0 - 2.0 * beta * phi, 2.0 * beta * g * u1, 2.0 * beta * g * u2, -2.0 * beta * g},
+                              {beta * (phi - c * u1), -beta * (g * u1 - c), -beta * (g * u2), beta * g},
+                              {u2, 0.0, -1.0, 0.0}};
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) R[i][j] = r[i][j], L[i][j] = l[i][j];
+    } else {
+      const double r[4][4] = {{1.0, 1.0, 1.0, 0.0}, {u1, u1, u1, 1.0}, {u2 - c, u2, u2 + c, 0.0},
+                              {h - c * u2, ek, h + c * u2, u1}};
+      const double l[4][4] = {{beta * (phi + c * u2), -beta * g * u1, -beta * (g * u2 + c), beta * g},
+                              {1.0 - 2.0 * beta * phi, 2.0 * beta * g * u1, 2.0 * beta * g * u2, -2.0 * beta * g},
+                              {beta * (phi - c * u2), -beta * (g * u1), -beta * (g * u2 - c), beta * g},
+                              {-u1, 1.0, 0.0, 0.0}};
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) R[i][j] = r[i][j], L[i][j] = l[i][j];
+    }
+    return;
+  }
+  const double u1 = u[1] / u[0], u2 = u[2] / u[0], u3 = u[3] / u[0];
+  const double ek = 0.5 * (std::pow(u1, 2) + std::pow(u2, 2) + std::pow(u3, 2));
+  const double h = (std::pow(c, 2) / (gamma - 1.0)) + ek;
+  const double beta = 1.0 / (2.0 * std::pow(c, 2));
+  const double phi = g * ek;
+  double r[5][5], l[5][5];
+  if (d == 0) {
+    const double rr[5][5] = {{1.0, 1.0, 1.0, 0.0, 0.0}, {u1 - c, u1, u1 + c, 0.0, 0.0}, {u2, u2, u2, -1.0, 0.0},
+                             {u3, u3, u3, 0.0, 1.0}, {h - c * u1, ek, h + c * u1, -u2, u3}};
+    const double ll[5][5] = {
+        {beta * (phi + c * u1), -beta * (g * u1 + c), -beta * g * u2, -beta * g * u3, beta * g},
+        {1.0 - 2.0 * beta * phi, 2.0 * beta * g * u1, 2.0 * beta * g * u2, 2.0 * beta * g * u3, -2.0 * beta * g},
+        {beta * (phi - c * u1), -beta * (g * u1 - c), -beta * (g * u2), -beta * g * u3, beta * g},
+        {u2, 0.0, -1.0, 0.0, 0.0},
+        {-u3, 0.0, 0.0, 1.0, 0.0}};
+    std::copy(&rr[0][0], &rr[0][0] + 25, &r[0][0]);
+    std::copy(&ll[0][0], &ll[0][0] + 25, &l[0][0]);
+  } else if (d == 1) {
+    const double rr[5][5] = {{1.0, 1.0, 1.0, 0.0, 0.0}, {u1, u1, u1, 1.0, 0.0}, {u2 - c, u2, u2 + c, 0.0, 0.0},
+                             {u3, u3, u3, 0.0, -1.0}, {h - c * u2, ek, h + c * u2, u1, -u3}};
+    const double ll[5][5] = {
+        {beta * (phi + c * u2), -beta * g * u1, -beta * (g * u2 + c), -beta * g * u3, beta * g},
+        {1.0 - 2.0 * beta * phi, 2.0 * beta * g * u1, 2.0 * beta * g * u2, 2.0 * beta * g * u3, -2.0 * beta * g},
+        {beta * (phi - c * u2), -beta * (g * u1), -beta * (g * u2 - c), -beta * g * u3, beta * g},
+        {-u1, 1.0, 0.0, 0.0, 0.0},
+        {u3, 0.0, 0.0, -1.0, 0.0}};
+    std::copy(&rr[0][0], &rr[0][0] + 25, &r[0][0]);
+    std::copy(&ll[0][0], &ll[0][0] + 25, &l[0][0]);
+  } else {
+    const double rr[5][5] = {{1.0, 1.0, 1.0, 0.0, 0.0}, {u1, u1, u1, -1.0, 0.0}, {u2, u2, u2, 0.0, 1.0},
+                             {u3 - c, u3, u3 + c, 0.0, 0.0}, {h - c * u3, ek, h + c * u3, -u1, u2}};
+    const double ll[5][5] = {
+        {beta * (phi + c * u3), -beta * g * u1, -beta * g * u2, -beta * (g * u3 + c), beta * g},
+        {1.0 - 2.0 * beta * phi, 2.0 * beta * g * u1, 2.0 * beta * g * u2, 2.0 * beta * g * u3, -2.0 * beta * g},
+        {beta * (phi - c * u3), -beta * (g * u1), -beta * g * u2, -beta * (g * u3 - c), beta * g},
+        {u1, -1.0, 0.0, 0.0, 0.0},
+        {-u2, 0.0, 1.0, 0.0, 0.0}};
+    std::copy(&rr[0][0], &rr[0][0] + 25, &r[0][0]);
+    std::copy(&ll[0][0], &ll[0][0] + 25, &l[0][0]);
+  }
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) R[i][j] = r[i][j], L[i][j] = l[i][j];
+}
+
+// minmod / minmodB (Source/NumericalMethod/AmrDG/AmrDG_Limiter.tpp:40-85).
+inline double minmod(double a1, double a2, double a3) {
+  const bool same = (std::signbit(a1) == std::signbit(a2)) && (std::signbit(a2) == std::signbit(a3));
+  const int sign = std::signbit(a1) ? -1 : +1;
+  if (same) return sign * std::min({std::abs(a1), std::abs(a2), std::abs(a3)});
+  return 0;
+}
+
+inline double minmodB(double a1, double a2, double a3, double thr /* AMR_TVB_C[l] * M * h^2 */) {
+  if (std::abs(a1) <= thr) return a1;
+  return minmod(a1, a2, a3);
 }
 
 }  // namespace oracle

@@ -257,7 +257,9 @@ class Sim {
   // FillBoundary (same level, periodic) followed by the physical BC
   // (outflow = zero-gradient mode copy, AMReX foextrap semantics).
   // BoundaryCondition.h:303-324.
-  void fill_boundary(int l) {
+  // FillBoundary alone: ghost cells that are valid cells of the same level
+  // (other boxes, periodic images) take their current data.
+  void fill_internal(int l) {
     Level& L = lev[l];
     const int ncomp = Q * Np_s;
 #pragma omp parallel for schedule(static)
@@ -273,6 +275,12 @@ class Sim {
       if (L.status[src] != ST_VALID) continue;
       for (int k = 0; k < ncomp; ++k) L.Uw[(size_t)k * L.ncell + c] = L.Uw[(size_t)k * L.ncell + src];
     }
+  }
+
+  void fill_boundary(int l) {
+    Level& L = lev[l];
+    const int ncomp = Q * Np_s;
+    fill_internal(l);
     bool any_nonper = false;
     for (int d = 0; d < D; ++d) any_nonper = any_nonper || !cfg.periodic[d];
     if (!any_nonper) return;

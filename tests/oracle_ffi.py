@@ -29,6 +29,7 @@ class OracleCfg(ctypes.Structure):
         ("dtn_regrid", ctypes.c_int), ("tag_kind", ctypes.c_int),
         ("tag_threshold", ctypes.c_double), ("grid_eff", ctypes.c_double),
         ("n_error_buf", ctypes.c_int), ("reflux_box_quirk", ctypes.c_int),
+        ("t_limit", ctypes.c_int), ("tvb_M", ctypes.c_double), ("tvb_c", ctypes.c_double * 8),
     ]
 
 
@@ -61,6 +62,8 @@ def lib():
         L.oracle_predictor.argtypes = [vp, ctypes.c_int]
         L.oracle_num_levels.argtypes = [vp]
         L.oracle_num_levels.restype = ctypes.c_int
+        L.oracle_limited_count.argtypes = [vp]
+        L.oracle_limited_count.restype = ctypes.c_long
         L.oracle_get_boxes.argtypes = [vp, ctypes.c_int, ip, ctypes.c_int]
         L.oracle_get_boxes.restype = ctypes.c_int
         for f in ("oracle_get_uw", "oracle_set_uw", "oracle_get_uw_grown", "oracle_get_hw_grown"):
@@ -82,7 +85,8 @@ def lib():
 def make_cfg(D=2, P=1, n=(32, 32, 1), lo=(0.0, 0.0, 0.0), hi=(10.0, 10.0, 1.0), periodic=(1, 1, 1),
              ic="vortex", u_inf=1.0, v_inf=0.0, c_dt=0.5, gamma=1.4, seed=12345, noise_amp=1e-3,
              max_grid=1024, max_level=0, blocking_factor=8, dtn_regrid=4, tag_kind=0,
-             tag_threshold=0.1, grid_eff=0.7, n_error_buf=1, reflux_box_quirk=1, xc=5.0, yc=5.0, beta=5.0):
+             tag_threshold=0.1, grid_eff=0.7, n_error_buf=1, reflux_box_quirk=1, xc=5.0, yc=5.0, beta=5.0,
+             t_limit=0, tvb_M=0.0, tvb_c=None):
     c = OracleCfg()
     c.D, c.P, c.gamma, c.c_dt = D, P, gamma, c_dt
     for d in range(3):
@@ -96,6 +100,9 @@ def make_cfg(D=2, P=1, n=(32, 32, 1), lo=(0.0, 0.0, 0.0), hi=(10.0, 10.0, 1.0), 
     c.max_grid, c.max_level, c.blocking_factor, c.dtn_regrid = max_grid, max_level, blocking_factor, dtn_regrid
     c.tag_kind, c.tag_threshold, c.grid_eff, c.n_error_buf = tag_kind, tag_threshold, grid_eff, n_error_buf
     c.reflux_box_quirk = reflux_box_quirk
+    c.t_limit, c.tvb_M = t_limit, tvb_M
+    for l in range(8):
+        c.tvb_c[l] = 1.0 if tvb_c is None else tvb_c[l]
     return c
 
 
@@ -163,6 +170,10 @@ class OracleSim:
     def set_uw(self, arr, lev=0):
         arr = np.ascontiguousarray(arr, dtype=np.float64)
         self.L.oracle_set_uw(self.h, lev, arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+
+    def limited_count(self):
+        """Cells the TVB limiter has modified so far."""
+        return int(self.L.oracle_limited_count(self.h))
 
     def tags(self, lev):
         n = self.ncells_level(lev)

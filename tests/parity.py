@@ -23,10 +23,10 @@ ORACLE_IC = {"vortex": "vortex", "kh_noise": "kh_noise", "blast3d": "blast3d", "
 GPU_IC = {"vortex": "isentropic_vortex", "kh_noise": "kh_noise", "blast3d": "blast3d", "const": "const"}
 
 
-def make_oracle(case, c_dt=0.5, max_grid=1024):
+def make_oracle(case, c_dt=0.5, max_grid=1024, **kw):
     D, P, n, lo, hi, per, ic, extra = CASES[case]
     cfg = O.make_cfg(D=D, P=P, n=n, lo=lo, hi=hi, periodic=per, ic=ORACLE_IC[ic], c_dt=c_dt,
-                     max_grid=max_grid, **extra)
+                     max_grid=max_grid, **extra, **kw)
     s = O.OracleSim(cfg)
     s.init()
     return s
@@ -65,10 +65,10 @@ AMR_CASES = {
 }
 
 
-def make_oracle_amr(case, c_dt=0.5, quirk=1):
+def make_oracle_amr(case, c_dt=0.5, quirk=1, **kw):
     D, P, n, hi, per, ic, extra, amr = AMR_CASES[case]
     cfg = O.make_cfg(D=D, P=P, n=n, hi=hi, periodic=per, ic=ORACLE_IC[ic], c_dt=c_dt, reflux_box_quirk=quirk,
-                     **extra, **amr)
+                     **extra, **amr, **kw)
     s = O.OracleSim(cfg)
     s.init()
     return s
