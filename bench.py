@@ -191,6 +191,68 @@ def autotune(G, w, steps=3):
     return best, db[key]
 
 
+def oracle_sim(w):
+    """The CPU oracle configured as the workload (same boxes as the GPU run)."""
+    import oracle_ffi as O
+
+    amr = w.get("amr", {})
+    cfg = O.make_cfg(D=w["D"], P=w["P"], n=w["n"], lo=w["lo"], hi=w["hi"], periodic=w["periodic"],
+                     ic=w["ic"], c_dt=w["c_dt"], max_grid=amr.get("max_grid", 1 << 20),
+                     max_level=amr.get("max_level", 0), blocking_factor=amr.get("blocking_factor", 8),
+                     dtn_regrid=amr.get("dtn_regrid", 4), tag_kind=amr.get("tag_kind", 0),
+                     tag_threshold=amr.get("tag_threshold", 0.1),
+                     **({"t_limit": w["limiter"]["t_limit"], "tvb_M": w["limiter"]["TVB_M"]} if "limiter" in w else {}),
+                     **{k: w[k] for k in ("seed", "noise_amp", "u_inf", "v_inf") if k in w})
+    return O.OracleSim(cfg)
+
+
+def run_accuracy(args, w):
+    """Plain FP64 GPU path against the CPU oracle on the workload from the
+    same initial state for --steps steps: box layouts, the largest modal
+    difference per level (relative to each variable's largest cell mean) and
+    the exact L2 norm of the density difference over the level-0 field."""
+    import numpy as np
+
+    import adg_gb300 as G
+    import oracle_ffi as O
+
+    O.set_threads(os.cpu_count())
+    o = oracle_sim(w)
+    o.init()
+    g = make_sim(G, w)
+    for l in range(o.num_levels()):
+        g.set_U_w(o.get_uw(l), l)
+    g.Dt = o.dt
+    t_cpu = t_gpu = 0.0
+    same_layout = True
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.step()
+        t1 = time.perf_counter()
+        g.time_integration()
+        g.Dt  # sync
+        t2 = time.perf_counter()
+        t_cpu += t1 - t0
+        t_gpu += t2 - t1
+        same_layout = same_layout and g.num_levels() == o.num_levels() and all(
+            np.array_equal(g.boxes(l), o.boxes(l)) for l in range(o.num_levels()))
+
+    def rel(a, b):
+        scale = np.maximum(np.max(np.abs(b[:, :, 0]), axis=0), 1e-300)
+        return float(np.max(np.max(np.abs(a - b), axis=(0, 2)) / scale))
+
+    levels = [{"level": l, "cells": int(o.ncells_level(l)), "max_rel_modal": rel(g.get_U_w(l), o.get_uw(l))}
+              for l in range(min(o.num_levels(), g.num_levels()))]
+    line = {"accuracy": {"workload": args.workload, "steps": args.steps, "same_layout_every_step": same_layout,
+                         "levels": levels,
+                         "l2_density_level0": l2_density_level0(g.get_U_w(0), o.get_uw(0), w),
+                         "dt_rel": abs(g.Dt - o.dt) / o.dt, "gpu_status": g.status(),
+                         "limited": [g.limited_count(), o.limited_count()] if "limiter" in w else None,
+                         "wall_s": {"oracle": t_cpu, "gpu_stream_steps": t_gpu}}}
+    print(json.dumps(line))
+    return 0
+
+
 def cpu_baseline(w, max_seconds=20.0, threads=None):
     """The oracle (C++/OpenMP restatement of the reference) on the host cores:
     a bounded sample of the same workload (whole grid, the steps after the
@@ -202,14 +264,7 @@ def cpu_baseline(w, max_seconds=20.0, threads=None):
     threads = threads or os.cpu_count()
     O.set_threads(threads)
     amr = w.get("amr", {})
-    cfg = O.make_cfg(D=w["D"], P=w["P"], n=w["n"], lo=w["lo"], hi=w["hi"], periodic=w["periodic"],
-                     ic=w["ic"], c_dt=w["c_dt"], max_grid=amr.get("max_grid", 128),
-                     max_level=amr.get("max_level", 0), blocking_factor=amr.get("blocking_factor", 8),
-                     dtn_regrid=amr.get("dtn_regrid", 4), tag_kind=amr.get("tag_kind", 0),
-                     tag_threshold=amr.get("tag_threshold", 0.1),
-                     **({"t_limit": w["limiter"]["t_limit"], "tvb_M": w["limiter"]["TVB_M"]} if "limiter" in w else {}),
-                     **{k: w[k] for k in ("seed", "noise_amp", "u_inf", "v_inf") if k in w})
-    s = O.OracleSim(cfg)
+    s = oracle_sim(w)
     s.init()
     per_cell = (w["D"] + 2) * comb(w["P"] + w["D"], w["D"])
     s.step()  # untimed, as the GPU arm's warm-up
@@ -571,6 +626,8 @@ def main():
     ap.add_argument("--only", default=None,
                     choices=["plain_fp64", "noseed_1sweep_fp64"] + list(SEED_VARIANTS),
                     help="time one variant only and print its record (profiling runs)")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="compare the plain GPU path with the CPU oracle over --steps steps and print the errors")
     ap.add_argument("--seed-cache", action="store_true",
                     help="reuse (or store) the trained seed parameters under the package build folder")
     args = ap.parse_args()
@@ -578,6 +635,8 @@ def main():
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, w)
+    if args.accuracy:
+        return run_accuracy(args, w)
     return run_ours(args, w)
 
 
