@@ -99,6 +99,7 @@ def lib():
         "adg_regrid_profile": ([vp, dp, i], i),
         "adg_leaf_dof_updates": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
         "adg_limited_count": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_lp_norm": ([vp, i, i, dp], i),
         "adg_seed_set_path": ([vp, i], i),
         "adg_seed_infer": ([vp, vp, i], i),
         "adg_seed_create": ([i, i, i, ctypes.c_uint64, ctypes.POINTER(vp)], i),
@@ -382,6 +383,13 @@ class AmrDG:
         n, ms = ctypes.c_int64(), ctypes.c_double()
         self._check(self._L.adg_dof_updates(self.ctx, ctypes.byref(n), ctypes.byref(ms)), "adg_dof_updates")
         return n.value, ms.value
+
+    def norm(self, p=2, q=0):
+        """LpNorm_DG_AMR: Lp norm of component q minus the analytic initial
+        condition over the leaf cells (AmrDG.h:1399-1578)."""
+        v = ctypes.c_double()
+        self._check(self._L.adg_lp_norm(self.ctx, int(p), int(q), ctypes.byref(v)), "adg_lp_norm")
+        return v.value
 
     def limited_count(self):
         """Elements the TVB limiter has modified so far."""

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -742,6 +743,69 @@ int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
 
 }  // namespace
 
+namespace {
+// ---- quadrature for the Lp norms (host) -----------------------------------
+// Legendre P_n and its derivative by the three-term recurrence.
+void legendre_pd(int n, double x, double* p, double* dp) {
+  double p0 = 1.0, p1 = x, d0 = 0.0, d1 = 1.0;
+  if (n == 0) {
+    *p = 1.0;
+    *dp = 0.0;
+    return;
+  }
+  for (int k = 2; k <= n; ++k) {
+    const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+    const double d2 = d0 + (2.0 * k - 1.0) * p1;
+    p0 = p1;
+    p1 = p2;
+    d0 = d1;
+    d1 = d2;
+  }
+  *p = p1;
+  *dp = d1;
+}
+
+// n-point Gauss-Legendre nodes (Newton from cos(pi (i - 1/4) / (n + 1/2)),
+// in the order x_1, -x_1, x_2, ...) and weights 2 / ((1 - x^2) P_n'(x)^2).
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.clear();
+  for (int i = 1; i <= n / 2; ++i) {
+    double xi = std::cos(3.14159265358979323846 * (i - 0.25) / (n + 0.5));
+    for (int it = 0; it < 100; ++it) {
+      double p, dp;
+      legendre_pd(n, xi, &p, &dp);
+      const double dx = p / dp;
+      xi -= dx;
+      if (std::fabs(dx) < 1e-16) break;
+    }
+    x.push_back(xi);
+    x.push_back(-xi);
+  }
+  if (n % 2) x.push_back(0.0);
+  w.resize(x.size());
+  for (size_t k = 0; k < x.size(); ++k) {
+    double p, dp;
+    legendre_pd(n, x[k], &p, &dp);
+    w[k] = 2.0 / ((1.0 - x[k] * x[k]) * dp * dp);
+  }
+}
+
+// Spatial modes in the reference's order: total degree <= P, first index
+// slowest (MultiIndex, AmrDG.h:62-122).
+void multi_index(int D, int left, int depth, std::array<int, 3>& cur, std::vector<std::array<int, 3>>& out) {
+  if (depth == D) {
+    out.push_back(cur);
+    return;
+  }
+  for (int v = 0; v <= left; ++v) {
+    cur[depth] = v;
+    multi_index(D, left - v, depth + 1, cur, out);
+  }
+  cur[depth] = 0;
+}
+
+}  // namespace
+
 extern "C" {
 
 int adg_ctx_create(const adg_config* cfg, adg_ctx** out) {
@@ -1024,6 +1088,107 @@ int adg_advance(adg_ctx* ctx, int nsteps, int use_graph) {
     rc = host_step(ctx, use_graph != 0);
     if (rc) return rc;
   }
+  return ADG_OK;
+}
+
+int adg_lp_norm(adg_ctx* ctx, int p, int q, double* out) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  const Hierarchy& H = ctx->hier;
+  const KernelSet* ks = ctx->ks;
+  const int D = ctx->cfg.D, P = ctx->cfg.P;
+  if (!out || (p != 1 && p != 2) || q < 0 || q >= ks->Q) return fail(ctx, ADG_ERR_ARG, "bad norm arguments");
+  // points: the method's N = P + 1 GL nodes for p = 1, 2N for p = 2 (AmrDG.h:1399-1578)
+  std::vector<double> x1, w1;
+  gauss_legendre(p == 1 ? P + 1 : 2 * (P + 1), x1, w1);
+  const int N1 = (int)x1.size();
+  int M = 1;
+  for (int d = 0; d < D; ++d) M *= N1;
+  std::vector<std::array<int, 3>> mi;
+  std::array<int, 3> cur{0, 0, 0};
+  multi_index(D, P, 0, cur, mi);
+  std::vector<double> tab((size_t)mi.size() * M + M + 3 * (size_t)M);
+  double* phi = tab.data();
+  double* wq = phi + mi.size() * M;
+  double* qp = wq + M;
+  for (int m = 0; m < M; ++m) {
+    int rem = m, id[3] = {0, 0, 0};
+    for (int d = D - 1; d >= 0; --d) {
+      id[d] = rem % N1;
+      rem /= N1;
+    }
+    wq[m] = 1.0;
+    for (int d = 0; d < 3; ++d) {
+      qp[3 * m + d] = d < D ? x1[id[d]] : 0.0;
+      if (d < D) wq[m] *= w1[id[d]];
+    }
+    for (size_t n = 0; n < mi.size(); ++n) {
+      double v = 1.0;
+      for (int d = 0; d < D; ++d) {
+        double pv, dp;
+        legendre_pd(mi[n][d], x1[id[d]], &pv, &dp);
+        v *= pv;
+      }
+      phi[n * M + m] = v;
+    }
+  }
+  // covered flags (average-down records' coarse elements) and the leaf volume
+  const size_t nv = H.n_valid();
+  std::vector<int8_t> cov(nv, 0);
+  const size_t nov1 = ((size_t)1 << D) + 1;
+  for (int lf = 1; lf < H.nlevels(); ++lf)
+    for (size_t r = 0; r + nov1 <= H.ad_rec[lf].size(); r += nov1) cov[H.ad_rec[lf][r]] = 1;
+  const LevelGeom g = level_geom(ctx);
+  double V_amr = 0.0;
+  for (int l = 0; l < H.nlevels(); ++l) {
+    double vol = 1.0;
+    for (int d = 0; d < D; ++d) vol *= g.dx[l][d];
+    size_t nleaf = 0;
+    for (size_t e = H.level_valid_offset(l); e < H.level_valid_offset(l) + H.level_valid_count(l); ++e)
+      nleaf += cov[e] ? 0 : 1;
+    V_amr += vol * (double)nleaf;
+  }
+  DevBuf<double> dtab, dcell;
+  DevBuf<int8_t> dcov;
+  ADG_CUDA(dtab.ensure(tab.size()), "alloc norm tables");
+  ADG_CUDA(dcell.ensure(nv), "alloc norm cells");
+  ADG_CUDA(dcov.ensure(nv), "alloc norm cells");
+  ADG_CUDA(cudaMemcpyAsync(dtab.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+  ADG_CUDA(cudaMemcpyAsync(dcov.p, cov.data(), nv, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+  LpArgs a{};
+  a.Uw = ctx->Uw.p;
+  a.elem_cell = ctx->elem_cell.p;
+  a.elem_level = H.nlevels() > 1 ? ctx->elem_level.p : nullptr;
+  a.covered = dcov.p;
+  a.n_valid = (int)nv;
+  a.q = q;
+  a.p = p;
+  a.M = M;
+  a.phi = dtab.p;
+  a.wq = dtab.p + mi.size() * M;
+  a.qp = a.wq + M;
+  a.geom = g;
+  for (int d = 0; d < 3; ++d) a.prob_lo[d] = ctx->cfg.prob_lo[d];
+  a.gamma = ctx->cfg.gamma;
+  const adg_config& c = ctx->cfg;
+  a.icp.ic = c.ic;
+  a.icp.u_inf = c.u_inf;
+  a.icp.v_inf = c.v_inf;
+  a.icp.beta = c.beta;
+  a.icp.xc = c.xc;
+  a.icp.yc = c.yc;
+  a.icp.seed = c.seed;
+  a.icp.noise_amp = c.noise_amp;
+  a.cell_out = dcell.p;
+  cudaError_t e = ks->lp_norm(a, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "norm launch");
+  ctx->launches++;
+  std::vector<double> cells(nv);
+  ADG_CUDA(cudaMemcpyAsync(cells.data(), dcell.p, nv * 8, cudaMemcpyDeviceToHost, ctx->stream), "d2h");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "norm sync");
+  double total = 0.0;
+  for (size_t k = 0; k < nv; ++k) total += cells[k];
+  *out = std::pow(total / V_amr, 1.0 / (double)p);
   return ADG_OK;
 }
 

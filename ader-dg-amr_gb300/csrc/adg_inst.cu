@@ -141,6 +141,11 @@ struct Impl final : KernelSet {
     k_limit_tvb<O><<<(a.n + 127) / 128, 128, 0, s>>>(a);
     return cudaGetLastError();
   }
+  cudaError_t lp_norm(const LpArgs& a, cudaStream_t s) const override {
+    if (a.n_valid <= 0) return cudaSuccess;
+    k_lp_norm<O><<<(a.n_valid + 127) / 128, 128, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const override {
     const int bs = 64;
     k_init_ic<O><<<(a.n_elem + bs - 1) / bs, bs, 0, s>>>(a);

@@ -505,6 +505,35 @@ __device__ __forceinline__ void reflux_add(const CorrectorArgs& a, int r, int lc
   for (int n = 0; n < NP_S; ++n) u[n] += inv_jac * (O::minv(n) * corr[n]);
 }
 
+// N consecutive doubles to registers (and back): 16-byte accesses when every
+// run of the array starts on a 16-byte boundary (even run length).
+template <int N>
+__device__ __forceinline__ void load_run(const double* __restrict__ p, double* v) {
+  if constexpr (N % 2 == 0) {
+    const double2* p2 = reinterpret_cast<const double2*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 2; ++i) {
+      const double2 x = __ldg(p2 + i);
+      v[2 * i] = x.x;
+      v[2 * i + 1] = x.y;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = __ldg(p + i);
+  }
+}
+template <int N>
+__device__ __forceinline__ void store_run(double* p, const double* v) {
+  if constexpr (N % 2 == 0) {
+    double2* p2 = reinterpret_cast<double2*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 2; ++i) p2[i] = make_double2(v[2 * i], v[2 * i + 1]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) p[i] = v[i];
+  }
+}
+
 template <class O>
 __global__ void k_corrector(CorrectorArgs a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NB = O::NQ_BD, NF = 2 * D;
@@ -525,18 +554,16 @@ __global__ void k_corrector(CorrectorArgs a) {
   }
   const int lev = a.elem_level ? a.elem_level[e] : 0;
   double R[NP_S];
-  const double* rv = a.Rvol + ((size_t)e * Q + q) * NP_S;
-#pragma unroll
-  for (int n = 0; n < NP_S; ++n) R[n] = rv[n];
-  double bp[NP_S], bm[NP_S];
+  load_run<NP_S>(a.Rvol + ((size_t)e * Q + q) * NP_S, R);
+  double bp[NP_S], bm[NP_S], fv[NB];
   const int* ef = a.elem_face + (size_t)e * NF;
 #define ADG_BD(DD)                                                                      \
   {                                                                                     \
     const double cd = a.dt[kScalDtDx + 3 * lev + DD];                                  \
-    const double* flo = a.Fnum + ((size_t)ef[2 * DD + 0] * Q + q) * NB;                 \
-    const double* fhi = a.Fnum + ((size_t)ef[2 * DD + 1] * Q + q) * NB;                 \
-    O::template bd_term<DD, 1>(RegIn{fhi}, RegOut{bp});                                 \
-    O::template bd_term<DD, 0>(RegIn{flo}, RegOut{bm});                                 \
+    load_run<NB>(a.Fnum + ((size_t)ef[2 * DD + 1] * Q + q) * NB, fv);                  \
+    O::template bd_term<DD, 1>(RegIn{fv}, RegOut{bp});                                  \
+    load_run<NB>(a.Fnum + ((size_t)ef[2 * DD + 0] * Q + q) * NB, fv);                  \
+    O::template bd_term<DD, 0>(RegIn{fv}, RegOut{bm});                                  \
     _Pragma("unroll") for (int n = 0; n < NP_S; ++n) R[n] = fma(-cd, bp[n] - bm[n], R[n]); \
   }
   ADG_BD(0)
@@ -546,9 +573,7 @@ __global__ void k_corrector(CorrectorArgs a) {
 #pragma unroll
   for (int n = 0; n < NP_S; ++n) R[n] = R[n] * O::minv(n);
   if (r >= 0) reflux_add<O>(a, r, lev, q, R);
-  double* dst = a.Uw + ((size_t)e * Q + q) * NP_S;
-#pragma unroll
-  for (int n = 0; n < NP_S; ++n) dst[n] = R[n];
+  store_run<NP_S>(a.Uw + ((size_t)e * Q + q) * NP_S, R);
 }
 
 // ---------------------------------------------------------------------------
@@ -807,6 +832,60 @@ __global__ void k_dt_reduce(DtArgs a) {
     *a.min_bits = (unsigned long long)__double_as_longlong(1.0e300);
     *a.done = 0u;
   }
+}
+
+// Lp norm of the difference to the analytic initial condition over the leaf
+// cells (LpNorm_DG_AMR, AmrDG.h:1399-1578): per valid, uncovered element the
+// sum over the tensor quadrature points of |u_ex - u_h|^p w_m, times
+// vol / 2^D; covered elements give 0.  The host adds the cells in order.
+struct LpArgs {
+  const double* Uw;
+  const int* elem_cell;
+  const int8_t* elem_level;   // nullptr: all level 0
+  const int8_t* covered;      // [valid elem] 1: covered by a finer level
+  int n_valid, q, p, M;       // M quadrature points
+  const double* phi;          // [Np_s][M] basis values
+  const double* wq;           // [M] weights
+  const double* qp;           // [M][3] reference coordinates
+  LevelGeom geom;
+  double prob_lo[3];
+  double gamma;
+  ICParams icp;
+  double* cell_out;           // [valid elem]
+};
+
+template <class O>
+__global__ void k_lp_norm(LpArgs a) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.n_valid) return;
+  if (a.covered && a.covered[e]) {
+    a.cell_out[e] = 0.0;
+    return;
+  }
+  const int lev = a.elem_level ? a.elem_level[e] : 0;
+  double uw[NP_S];
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) uw[n] = a.Uw[((size_t)e * Q + a.q) * NP_S + n];
+  double vol = 1.0;
+  for (int d = 0; d < D; ++d) vol *= a.geom.dx[lev][d];
+  double cell = 0.0;
+  for (int m = 0; m < a.M; ++m) {
+    double uh = 0.0;
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) uh += uw[n] * a.phi[(size_t)n * a.M + m];
+    double x[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < D; ++d) {
+      const double dx = a.geom.dx[lev][d];
+      const double xc = a.prob_lo[d] + (a.elem_cell[3 * e + d] + 0.5) * dx;
+      x[d] = (dx / 2.0) * a.qp[3 * m + d] + xc;
+    }
+    double v[5];
+    pde_ic(x, D, a.gamma, a.icp, 0, 0, v);
+    const double err = fabs(v[a.q] - uh);
+    cell += (a.p == 1 ? err : err * err) * a.wq[m];
+  }
+  a.cell_out[e] = cell * (vol / (double)(1 << D));
 }
 
 // L2 projection of the initial condition at the spatial GL points

@@ -32,6 +32,7 @@ struct KernelSet {
                                     cudaStream_t s) const = 0;
   virtual cudaError_t seed_infer_tc(const SeedTCArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t limit_tvb(const LimiterArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t lp_norm(const LpArgs& a, cudaStream_t s) const = 0;
 };
 
 const KernelSet* kernels_D2P1();

@@ -130,6 +130,13 @@ int adg_dof_updates(const adg_ctx* ctx, int64_t* total, double* regrid_ms);
 /* The same count over leaf elements only (valid elements not covered by a
  * finer level).  No reference counterpart. */
 int adg_leaf_dof_updates(const adg_ctx* ctx, int64_t* total);
+/* Lp norm (p = 1 or 2) of component q of the solution minus the analytic
+ * initial condition, over the leaf cells, with the reference's quadrature
+ * (N = P + 1 GL points per dimension for p = 1, 2N for p = 2):
+ * LpNorm_DG_AMR, AmrDG.h:1399-1578 (the vortex after one period returns to
+ * its initial state, so this is the error the reference's convergence runs
+ * report). */
+int adg_lp_norm(adg_ctx* ctx, int p, int q, double* out);
 /* Elements the TVB limiter has modified so far (the reference's
  * n_limited_total, AmrDG.h:996). */
 int adg_limited_count(adg_ctx* ctx, int64_t* n);
