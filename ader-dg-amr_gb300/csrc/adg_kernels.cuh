@@ -61,6 +61,9 @@ struct PredictorArgs {
 template <class O, int E, int NQ, class T = double>
 __device__ __forceinline__ void flux_stage(T* sm, int ld, T gm1) {
   constexpr int Q = O::Q, D = O::D;
+  // two points per iteration: their independent FP64 chains hide each
+  // other's latency (occupancy is bounded by shared memory, not registers)
+#pragma unroll 2
   for (int it = threadIdx.x; it < E * NQ; it += blockDim.x) {
     const int m = it % NQ;
     const int e = it / NQ;
@@ -334,6 +337,7 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   constexpr int NFIELD = 2 * Q + 1;
   const int e0 = blockIdx.x * E;
   const int limit = a.elem_list ? *a.list_count : a.n_elem;
+#pragma unroll 2
   for (int it = threadIdx.x; it < E * NF * NB; it += blockDim.x) {
     const int m = it % NB;
     const int f = (it / NB) % NF;
