@@ -9,6 +9,7 @@ Reference surface mirrored here:
   AmrDG::evolve / ADER    Source/NumericalMethod/AmrDG/AmrDG.h:853-1165
   AmrDG::set_Dt           Source/NumericalMethod/AmrDG/AmrDG.h:1253-1357
   Compressible_Euler::settings  Source/Model/CompressibleEuler/Compressible_Euler.cpp:5-48
+  Solver::PlotFile / ReadPlotFile  Source/Core/Solver.h:599-652, 922-968
 
 The compute path is the CUDA library only; there is no CPU fallback.  Loading
 fails loudly when the library is missing.
@@ -118,6 +119,11 @@ def lib():
         "adg_set_layout": ([vp, i, ctypes.POINTER(i), ctypes.POINTER(i)], i),
         "adg_level_cell_coords": ([vp, i, ctypes.POINTER(i)], i),
         "adg_tags": ([vp, i, ctypes.POINTER(ctypes.c_uint8)], i),
+        "adg_get_step": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_write_plotfile": ([vp, ctypes.c_char_p, i, i, ctypes.POINTER(ctypes.c_char_p)], i),
+        "adg_read_plotfile": ([vp, ctypes.c_char_p, i, dp], i),
+        "adg_plotfile_info": ([ctypes.c_char_p, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i), dp,
+                               ctypes.POINTER(i), ctypes.c_char_p, i], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -181,6 +187,9 @@ class AmrDG:
         c.reflux_box_quirk, c.picard_sweeps, c.elems_per_block = 1, 0, 0
         self.T = None
         self.ctx = None
+        self.dtn_outplt, self.dt_outplt, self.data_dir, self.restart_tstep = 0, 0.0, "plt", 0
+        self.restart_time = 0.0
+        self._t_last_plt = 0.0
         self._L = lib()
 
     # ------------------------------------------------------------ settings
@@ -223,6 +232,16 @@ class AmrDG:
         c.blocking_factor, c.dtn_regrid = int(blocking_factor), int(dtn_regrid)
         return self
 
+    def setIO(self, n_out=0, t_out=0.0, data_dir="plt", restart_tstep=0):
+        """Simulation::setIO (Simulation.h:155-161): a plotfile every n_out
+        steps and/or every t_out of simulated time into data_dir, and the step
+        to restart from (0: start from the initial condition).  The reference
+        puts data_dir under its Results tree and empties it on a fresh run;
+        here it is the caller's path and nothing is deleted."""
+        self.dtn_outplt, self.dt_outplt = int(n_out), float(t_out)
+        self.data_dir, self.restart_tstep = str(data_dir), int(restart_tstep)
+        return self
+
     def setAmrSettings(self, tag_kind=0, tag_threshold=0.1, grid_eff=0.7, n_error_buf=1, reflux_box_quirk=1):
         c = self.cfg
         c.tag_kind, c.tag_threshold, c.grid_eff = int(tag_kind), float(tag_threshold), float(grid_eff)
@@ -248,6 +267,9 @@ class AmrDG:
             raise AdgError(f"adg_ctx_create failed (status {rc})")
         self.ctx = h
         self._check(self._L.adg_init(self.ctx), "adg_init")
+        if self.restart_tstep > 0:  # Solver::init on restart (Solver.h:571-593)
+            self.restart_time = self.ReadPlotFile(self.restart_tstep)
+        self._t_last_plt = self.time
         return self
 
     def close(self):
@@ -296,15 +318,69 @@ class AmrDG:
         self._check(self._L.adg_advance(self.ctx, int(nsteps), int(bool(use_graph))), "adg_advance")
 
     def evolve(self, nsteps=None, T=None):
-        """AmrDG::evolve: fixed step count, or until T with the last step clamped."""
+        """AmrDG::evolve (AmrDG.h:853-1030): fixed step count, or until T with
+        the last step clamped; plotfiles as set by setIO: the initial state on
+        a fresh start, then after every step n with n % n_out == 0, else when
+        t_out has passed since the last one."""
         T = T if T is not None else self.T
-        if nsteps is not None:
-            self.advance(nsteps)
+        out = self.dtn_outplt > 0 or self.dt_outplt > 0
+        if out and self.step == 0:
+            self.PlotFile(0)
+        if nsteps is not None and self.dt_outplt <= 0:
+            left = int(nsteps)
+            while left > 0:  # graph replay between plotfile steps
+                k = left
+                if self.dtn_outplt > 0:
+                    k = min(k, self.dtn_outplt - self.step % self.dtn_outplt)
+                self.advance(k)
+                left -= k
+                self._maybe_plot()
             return
-        while self.time < T:
-            if T - self.time < self.Dt:
+        n_done = 0
+        while (nsteps is not None and n_done < nsteps) or (nsteps is None and self.time < T):
+            if nsteps is None and T - self.time < self.Dt:
                 self.Dt = T - self.time
             self.time_integration()
+            n_done += 1
+            self._maybe_plot()
+
+    def _maybe_plot(self):
+        n, t = self.step, self.time
+        if self.dtn_outplt > 0 and n % self.dtn_outplt == 0:
+            self.PlotFile(n)
+        elif self.dt_outplt > 0 and t - self._t_last_plt >= self.dt_outplt - 1e-12:
+            self.PlotFile(n)
+            self._t_last_plt = t
+
+    @property
+    def step(self):
+        """Completed steps (the evolve loop's n; continues after a restart)."""
+        v = ctypes.c_int64()
+        self._check(self._L.adg_get_step(self.ctx, ctypes.byref(v)), "adg_get_step")
+        return v.value
+
+    # ------------------------------------------------------------ plotfiles
+    def PlotFile(self, tstep, level=-1, data_dir=None, var_names=None):
+        """Solver::PlotFile (Solver.h:922-968): per conserved variable q the
+        AMReX plotfile <data_dir>/tstep_<tstep>_q_<q>_plt with the modes of
+        U_w as components "<name>_<m>"; level -1 writes every level."""
+        d = (data_dir if data_dir is not None else self.data_dir).encode()
+        names = None
+        if var_names is not None:
+            if len(var_names) != self.Q:
+                raise ValueError(f"need {self.Q} variable names")
+            names = (ctypes.c_char_p * self.Q)(*[n.encode() for n in var_names])
+        self._check(self._L.adg_write_plotfile(self.ctx, d, int(tstep), int(level), names), "adg_write_plotfile")
+
+    def ReadPlotFile(self, tstep, data_dir=None):
+        """Solver::ReadPlotFile (Solver.h:599-652) + the FillPatch of Solver::init:
+        boxes, state, time and step count from the plotfiles of tstep.
+        Returns the time read."""
+        d = (data_dir if data_dir is not None else self.data_dir).encode()
+        t = ctypes.c_double()
+        self._check(self._L.adg_read_plotfile(self.ctx, d, int(tstep), ctypes.byref(t)), "adg_read_plotfile")
+        self._t_last_plt = t.value
+        return t.value
 
     # ------------------------------------------------------------ state
     def num_levels(self):
@@ -556,6 +632,21 @@ def seed_stats(sim):
     if rc != ADG_OK:
         raise AdgError("adg_seed_stats failed")
     return a.value, b.value
+
+
+def plotfile_info(path):
+    """Header of one plotfile directory (no context, no GPU needed):
+    dict(dim, ncomp, finest_level, time, step); raises AdgError when the
+    plotfile is missing or malformed."""
+    i = ctypes.c_int
+    dim, nc, fin, st = i(), i(), i(), i()
+    t = ctypes.c_double()
+    err = ctypes.create_string_buffer(512)
+    rc = lib().adg_plotfile_info(str(path).encode(), ctypes.byref(dim), ctypes.byref(nc), ctypes.byref(fin),
+                                 ctypes.byref(t), ctypes.byref(st), err, 512)
+    if rc != ADG_OK:
+        raise AdgError(f"adg_plotfile_info failed (status {rc}): {err.value.decode()}")
+    return dict(dim=dim.value, ncomp=nc.value, finest_level=fin.value, time=t.value, step=st.value)
 
 
 def set_device(dev):

@@ -17,6 +17,7 @@
 #include "adg_kernelset.hpp"
 #include "adg_layout.hpp"
 #include "adg_mlp.cuh"
+#include "plotfile.hpp"
 #include <random>
 
 namespace adg {
@@ -1295,6 +1296,176 @@ int adg_tags(adg_ctx* ctx, int lev, uint8_t* out) {
   ctx->launches++;
   ADG_CUDA(cudaMemcpyAsync(out, ctx->tags.p, ta.n, cudaMemcpyDeviceToHost, ctx->stream), "tags d2h");
   ADG_CUDA(cudaStreamSynchronize(ctx->stream), "tags sync");
+  return ADG_OK;
+}
+
+int adg_get_step(const adg_ctx* ctx, int64_t* n) {
+  if (!ctx || !n) return ADG_ERR_ARG;
+  *n = (int64_t)ctx->nstep;
+  return ADG_OK;
+}
+
+// Solver::PlotFile (Source/Core/Solver.h:922-968): per q one plotfile whose
+// components are the Np_s modes of U_w(l, q) on the valid boxes of each level.
+int adg_write_plotfile(adg_ctx* ctx, const char* data_dir, int tstep, int level, const char* const* var_names) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  const Hierarchy& H = ctx->hier;
+  const int D = ctx->cfg.D, Q = ctx->ks->Q, Ns = ctx->ks->Np_s;
+  if (!data_dir || tstep < 0 || level >= H.nlevels()) return fail(ctx, ADG_ERR_ARG, "bad plotfile arguments");
+  if (var_names)
+    for (int q = 0; q < Q; ++q)
+      if (!var_names[q] || !var_names[q][0] || std::strpbrk(var_names[q], " \t\r\n"))
+        return fail(ctx, ADG_ERR_ARG, "variable names must be non-empty words");
+  const int l0 = level < 0 ? 0 : level, l1 = level < 0 ? H.nlevels() - 1 : level;
+  std::vector<double> hs(H.n_valid() * Q * Ns);
+  double t = 0.0;
+  ADG_CUDA(cudaMemcpyAsync(hs.data(), ctx->Uw.p, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+           "plotfile state d2h");
+  ADG_CUDA(cudaMemcpyAsync(&t, ctx->scal.p + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "plotfile time");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "plotfile sync");
+  // Compressible_Euler::VarNames (Compressible_Euler.h:15-24); that list is
+  // ordered for 2D, so 3D names momentum_z before energy_density.
+  static const char* const names2[] = {"mass_density", "momentum_x", "momentum_y", "energy_density"};
+  static const char* const names3[] = {"mass_density", "momentum_x", "momentum_y", "momentum_z", "energy_density"};
+  const LevelGeom g = level_geom(ctx);
+  for (int q = 0; q < Q; ++q) {
+    plt::Meta m;
+    m.D = D;
+    m.ncomp = Ns;
+    m.time = t;
+    for (int d = 0; d < D; ++d) {
+      m.prob_lo[d] = ctx->cfg.prob_lo[d];
+      m.prob_hi[d] = ctx->cfg.prob_hi[d];
+    }
+    const std::string base = var_names ? var_names[q] : (D == 3 ? names3[q] : names2[q]);
+    for (int k = 0; k < Ns; ++k) m.names.push_back(base + "_" + std::to_string(k));
+    std::vector<plt::LevelData> data;
+    for (int l = l0; l <= l1; ++l) {
+      plt::LevelMeta L;
+      L.boxes = H.grids[l];
+      for (int d = 0; d < 3; ++d) L.domain.hi[d] = d < D ? (ctx->cfg.n_cell[d] << l) - 1 : 0;
+      for (int d = 0; d < D; ++d) L.dx[d] = g.dx[l][d];
+      L.step = tstep;
+      m.levels.push_back(L);
+      if (l < l1) m.ref_ratio.push_back(2);
+      plt::LevelData ld(L.boxes.size());
+      for (size_t b = 0; b < L.boxes.size(); ++b) {
+        const amr::IBox& bx = L.boxes[b];
+        const size_t nc = (size_t)bx.volume(D);
+        std::vector<double>& v = ld[b];
+        v.resize(nc * Ns);
+        size_t o = 0;
+        for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
+          for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
+            for (int i = bx.lo[0]; i <= bx.hi[0]; ++i, ++o) {
+              const int c[3] = {i, j, k};
+              const size_t e = (size_t)H.cellmap[l][H.cidx(l, c)];
+              const double* u = &hs[(e * Q + q) * Ns];
+              for (int k2 = 0; k2 < Ns; ++k2) v[k2 * nc + o] = u[k2];
+            }
+      }
+      data.push_back(std::move(ld));
+    }
+    std::string err;
+    const std::string dir =
+        std::string(data_dir) + "/tstep_" + std::to_string(tstep) + "_q_" + std::to_string(q) + "_plt";
+    if (!plt::write(dir, m, data, &err)) return fail(ctx, ADG_ERR_IO, err);
+  }
+  return ADG_OK;
+}
+
+// Solver::ReadPlotFile (Source/Core/Solver.h:599-652) and the FillPatch of
+// every restored level that follows it (Solver.h:572-593).
+int adg_read_plotfile(adg_ctx* ctx, const char* data_dir, int tstep, double* time) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!data_dir || tstep < 0) return fail(ctx, ADG_ERR_ARG, "bad plotfile arguments");
+  const int D = ctx->cfg.D, Q = ctx->ks->Q, Ns = ctx->ks->Np_s;
+  std::vector<plt::Meta> meta(Q);
+  std::vector<std::vector<plt::LevelData>> data(Q);
+  std::string err;
+  for (int q = 0; q < Q; ++q) {
+    const std::string dir =
+        std::string(data_dir) + "/tstep_" + std::to_string(tstep) + "_q_" + std::to_string(q) + "_plt";
+    if (!plt::read(dir, ctx->cfg.max_level + 1, &meta[q], &data[q], &err)) return fail(ctx, ADG_ERR_IO, err);
+    if (meta[q].D != D) return fail(ctx, ADG_ERR_IO, dir + ": dimension differs from the configuration");
+    if (meta[q].ncomp != Ns) return fail(ctx, ADG_ERR_IO, dir + ": component count is not Np_s");
+  }
+  const plt::Meta& m0 = meta[0];
+  const int nlev = std::min((int)m0.levels.size(), ctx->cfg.max_level + 1);  // ReadPlotFile caps at max_level
+  std::vector<std::vector<amr::IBox>> ng(nlev);
+  for (int l = 0; l < nlev; ++l) {
+    const amr::IBox& dom = m0.levels[l].domain;
+    for (int d = 0; d < D; ++d)
+      if (dom.lo[d] != 0 || dom.hi[d] != (ctx->cfg.n_cell[d] << l) - 1)
+        return fail(ctx, ADG_ERR_IO, "plotfile level " + std::to_string(l) + " domain differs from the configuration");
+    if (l > 0 && m0.ref_ratio[l - 1] != 2) return fail(ctx, ADG_ERR_IO, "plotfile refinement ratio is not 2");
+    ng[l] = m0.levels[l].boxes;
+    for (int q = 1; q < Q; ++q)
+      if ((int)meta[q].levels.size() <= l || !(meta[q].levels[l].boxes == ng[l]))
+        return fail(ctx, ADG_ERR_IO, "plotfiles of the variables have different boxes");
+  }
+  for (int q = 1; q < Q; ++q)
+    if (meta[q].time != m0.time) return fail(ctx, ADG_ERR_IO, "plotfiles of the variables have different times");
+  if (ng != ctx->hier.grids) {
+    rc = apply_layout(ctx, ng, std::chrono::steady_clock::now());  // checks nesting before any change
+    if (rc) return rc;
+  }
+  const Hierarchy& H = ctx->hier;
+  std::vector<double> hs(H.n_valid() * Q * Ns);
+  for (int q = 0; q < Q; ++q)
+    for (int l = 0; l < nlev; ++l)
+      for (size_t b = 0; b < ng[l].size(); ++b) {
+        const amr::IBox& bx = ng[l][b];
+        const size_t nc = (size_t)bx.volume(D);
+        const std::vector<double>& v = data[q][l][b];
+        size_t o = 0;
+        for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
+          for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
+            for (int i = bx.lo[0]; i <= bx.hi[0]; ++i, ++o) {
+              const int c[3] = {i, j, k};
+              const size_t e = (size_t)H.cellmap[l][H.cidx(l, c)];
+              double* u = &hs[(e * Q + q) * Ns];
+              for (int k2 = 0; k2 < Ns; ++k2) u[k2] = v[k2 * nc + o];
+            }
+      }
+  const double t = m0.time;
+  ADG_CUDA(cudaMemcpyAsync(ctx->Uw.p, hs.data(), hs.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+           "plotfile state h2d");
+  ADG_CUDA(cudaMemcpyAsync(ctx->scal.p + 1, &t, sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "plotfile time");
+  if (H.nlevels() > 1) {
+    rc = launch_ghost_fill(ctx);
+    if (rc) return rc;
+  }
+  rc = launch_dt(ctx, 0);
+  if (rc) return rc;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "plotfile restart sync");
+  ctx->nstep = m0.levels[0].step;
+  ctx->first_step = true;  // the evolve loop regrids before its first step after a restart
+  if (time) *time = t;
+  return ADG_OK;
+}
+
+int adg_plotfile_info(const char* plotfile_dir, int* dim, int* ncomp, int* finest_level, double* time, int* step,
+                      char* err, int err_cap) {
+  if (!plotfile_dir) return ADG_ERR_ARG;
+  plt::Meta m;
+  std::string e;
+  if (!plt::read(plotfile_dir, 0, &m, nullptr, &e)) {
+    if (err && err_cap > 0) {
+      const size_t n = std::min(e.size(), (size_t)err_cap - 1);
+      std::memcpy(err, e.data(), n);
+      err[n] = '\0';
+    }
+    return ADG_ERR_IO;
+  }
+  if (dim) *dim = m.D;
+  if (ncomp) *ncomp = m.ncomp;
+  if (finest_level) *finest_level = (int)m.levels.size() - 1;
+  if (time) *time = m.time;
+  if (step) *step = m.levels[0].step;
+  if (err && err_cap > 0) err[0] = '\0';
   return ADG_OK;
 }
 

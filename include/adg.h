@@ -31,6 +31,7 @@ extern "C" {
 #define ADG_ERR_NUMERIC 4      /* device status: NaN or non-positive density */
 #define ADG_ERR_STATE 5        /* call out of order (e.g. step before init) */
 #define ADG_ERR_NOALLOC_CAPACITY 6 /* problem larger than the fixed scratch of adg_ader_step_noalloc */
+#define ADG_ERR_IO 7           /* plotfile missing, malformed or not matching the configuration */
 
 #define ADG_MEM_HOST 0
 #define ADG_MEM_DEVICE 1
@@ -161,6 +162,41 @@ int adg_set_layout(adg_ctx* ctx, int nlev, const int* nbox, const int* boxes);
  * level's state arrays (3 ints per cell). */
 int adg_level_cell_coords(const adg_ctx* ctx, int lev, int* ijk);
 int adg_tags(adg_ctx* ctx, int lev, uint8_t* out);
+
+/* Completed steps of the evolve loop (the reference's n, AmrDG.h:868-877,
+ * 1012); a restart from a plotfile continues its count. */
+int adg_get_step(const adg_ctx* ctx, int64_t* n);
+
+/* Plotfiles (checkpoint / restart).
+ *
+ * adg_write_plotfile replaces Solver::PlotFile (Source/Core/Solver.h:922-968):
+ * one AMReX plotfile per conserved variable q, <data_dir>/tstep_<tstep>_q_<q>_plt,
+ * holding the Np_s modal coefficients of U_w as components named
+ * "<var_names[q]>_<m>", the level hierarchy (boxes, domains, cell sizes,
+ * refinement ratio 2), the current time and tstep as every level's step.
+ * level < 0 writes every level, level >= 0 only that one.  var_names NULL:
+ * the reference's Compressible_Euler names (mass_density, momentum_x,
+ * momentum_y, energy_density in 2D; momentum_z before energy_density in 3D).
+ * Directories are created as needed; existing files are overwritten.
+ *
+ * adg_read_plotfile replaces Solver::ReadPlotFile (Source/Core/Solver.h:599-652)
+ * and the FillPatch that follows it in Solver::init (:572-593): it reads the
+ * Q plotfiles of tstep, restores the boxes of levels 0..min(finest, max_level),
+ * the state, the time and the step count, fills the coarse-fine ghosts and
+ * recomputes Dt; the next step regrids first, as the reference's evolve loop
+ * does after a restart (AmrDG.h:868-877, 938-940).  Everything is checked
+ * (dimension, component count, level-0 domain, ratio 2, consistent boxes over
+ * q) before the context changes: on ADG_ERR_IO it is as before the call.
+ * time may be NULL. */
+int adg_write_plotfile(adg_ctx* ctx, const char* data_dir, int tstep, int level, const char* const* var_names);
+int adg_read_plotfile(adg_ctx* ctx, const char* data_dir, int tstep, double* time);
+/* Header of one plotfile directory without a context or a GPU (all levels'
+ * multifab and FAB headers are checked, no data is read): dimension,
+ * component count, finest level, time and level-0 step.  Any output may be
+ * NULL.  Returns ADG_ERR_IO for a missing or malformed plotfile, with the
+ * reason in err (err_cap bytes, may be NULL). */
+int adg_plotfile_info(const char* plotfile_dir, int* dim, int* ncomp, int* finest_level, double* time, int* step,
+                      char* err, int err_cap);
 
 /* Per-stage entry points (parity testing). */
 /* Predictor only for level lev: writes H_w (Q * Np_st per cell, element-major)
