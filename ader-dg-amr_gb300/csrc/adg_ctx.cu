@@ -161,6 +161,17 @@ struct adg_ctx {
   TableView<int> remap_i;     // regrid remap entries: dst | parent | src_old
   TableView<int8_t> remap_c;  // regrid remap child indices
   double rg_phase_ms[6] = {0, 0, 0, 0, 0, 0};  // regrid host time by phase
+  // regrid tags in pinned host memory (tag_ev: their copy has landed)
+  uint8_t* tags_host = nullptr;
+  size_t tags_host_cap = 0;
+  cudaEvent_t tag_ev = nullptr;
+  // device state of a step that overlaps the host's clustering, restored
+  // when the clustering changes the boxes: every element's state, the
+  // scalar block, the limiter and fallback counters and the status word
+  DevBuf<double> snap_Uw, snap_scal;
+  DevBuf<unsigned long long> snap_cnt;
+  DevBuf<unsigned int> snap_status;
+  int n_rollbacks = 0;
   // learned seed
   adg_seed* seed = nullptr;
   int seed_mode = 0, seed_sweeps = 1;
@@ -194,6 +205,9 @@ struct adg_ctx {
     fb_total.release(); Uw_alt.release(); remap_i.release(); remap_c.release(); l2_flush.release();
     ubar_old.release(); limited.release();
     if (tab_ev) cudaEventSynchronize(tab_ev), cudaEventDestroy(tab_ev);
+    if (tag_ev) cudaEventSynchronize(tag_ev), cudaEventDestroy(tag_ev);
+    if (tags_host) cudaFreeHost(tags_host);
+    snap_Uw.release(); snap_scal.release(); snap_cnt.release(); snap_status.release();
     tab_dev.release();
     if (tab_host) cudaFreeHost(tab_host);
     if (fork_ev) cudaEventDestroy(fork_ev);
@@ -245,8 +259,8 @@ int upload_tables(adg_ctx* ctx, const RemapTable* rm = nullptr) {
   const size_t ne = H.n_elem();
   const size_t nf = H.face_left.size();
   ADG_CUDA(ctx->Rvol.ensure(ne * Q * ks->Np_s), "alloc Rvol");
-  ADG_CUDA(ctx->Tr.ensure(ne * 2 * D * (2 * Q + 1) * (size_t)ks->NQ_BD), "alloc traces");
-  ADG_CUDA(ctx->Fnum.ensure(nf * Q * (size_t)ks->NQ_BD), "alloc Fnum");
+  ADG_CUDA(ctx->Tr.ensure(ne * 2 * D * (size_t)ks->TR_TILE), "alloc traces");
+  ADG_CUDA(ctx->Fnum.ensure(nf * Q * (size_t)ks->NM), "alloc Fnum");
   if (ctx->cfg.limiter_t > 0) ADG_CUDA(ctx->ubar_old.ensure(ne * Q), "alloc limiter means");
   if (ctx->seed) {
     const adg_seed* sd = ctx->seed;
@@ -549,8 +563,9 @@ double ms_between(std::chrono::steady_clock::time_point a, std::chrono::steady_c
 int apply_layout(adg_ctx* ctx, const std::vector<std::vector<amr::IBox>>& ng,
                  std::chrono::steady_clock::time_point t2);
 
-int regrid(adg_ctx* ctx) {
-  auto t0 = std::chrono::steady_clock::now();
+// Regrid, device half: the refinement indicator of every level that may be
+// refined, its tags copied into pinned host memory (tag_ev marks the copy).
+int regrid_tags(adg_ctx* ctx, size_t* nt_out) {
   Hierarchy& H = ctx->hier;
   const KernelSet* ks = ctx->ks;
   const int F = H.nlevels() - 1;
@@ -573,26 +588,96 @@ int regrid(adg_ctx* ctx) {
     if (e != cudaSuccess) return cuda_fail(ctx, e, "tag launch");
     ctx->launches++;
   }
-  std::vector<uint8_t> ht(nt);
-  ADG_CUDA(cudaMemcpyAsync(ht.data(), ctx->tags.p, nt, cudaMemcpyDeviceToHost, ctx->stream), "tags d2h");
-  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "tags sync");
+  if (!ctx->tag_ev) ADG_CUDA(cudaEventCreateWithFlags(&ctx->tag_ev, cudaEventDisableTiming), "tag event");
+  ADG_CUDA(cudaEventSynchronize(ctx->tag_ev), "tag buffer reuse");  // the previous copy has been read
+  if (nt > ctx->tags_host_cap) {
+    if (ctx->tags_host) cudaFreeHost(ctx->tags_host);
+    ctx->tags_host = nullptr;
+    ctx->tags_host_cap = 0;
+    ADG_CUDA(cudaMallocHost(&ctx->tags_host, nt + nt / 4), "pinned tags");
+    ctx->tags_host_cap = nt + nt / 4;
+  }
+  ADG_CUDA(cudaMemcpyAsync(ctx->tags_host, ctx->tags.p, nt, cudaMemcpyDeviceToHost, ctx->stream), "tags d2h");
+  ADG_CUDA(cudaEventRecord(ctx->tag_ev, ctx->stream), "tag event");
+  *nt_out = nt;
+  return ADG_OK;
+}
+
+// Regrid, host half: wait for the tags only, then the new boxes
+// (amr_grids.hpp) from the current ones.
+int regrid_boxes(adg_ctx* ctx, size_t nt, std::vector<std::vector<amr::IBox>>* ng) {
+  Hierarchy& H = ctx->hier;
+  auto t0 = std::chrono::steady_clock::now();
+  ADG_CUDA(cudaEventSynchronize(ctx->tag_ev), "tags wait");
   auto t1 = std::chrono::steady_clock::now();
   ctx->rg_phase_ms[0] += ms_between(t0, t1);
+  const int F = H.nlevels() - 1;
+  const int max_crse = std::min(F, ctx->cfg.max_level - 1);
+  const uint8_t* ht = ctx->tags_host;
   std::vector<amr::TagField> tf(F + 1);
   for (int l = 0; l <= F; ++l) {
     int n[3];
     H.dims(l, n);
     tf[l].init(n);
     if (l > max_crse) continue;
-    for (size_t e = H.level_valid_offset(l); e < H.level_valid_offset(l) + H.level_valid_count(l); ++e)
+    for (size_t e = H.level_valid_offset(l); e < H.level_valid_offset(l) + H.level_valid_count(l) && e < nt; ++e)
       if (ht[e]) tf[l].f[tf[l].idx(H.elem_cell[3 * e], H.elem_cell[3 * e + 1], H.elem_cell[3 * e + 2])] = 1;
   }
-  std::vector<std::vector<amr::IBox>> ng = amr::make_new_grids(ctx->gp, H.grids, tf);
-  auto t2 = std::chrono::steady_clock::now();
-  ctx->rg_phase_ms[1] += ms_between(t1, t2);
+  *ng = amr::make_new_grids(ctx->gp, H.grids, tf);
+  ctx->rg_phase_ms[1] += ms_between(t1, std::chrono::steady_clock::now());
   ctx->n_regrids++;
-  if (ng == H.grids) return ADG_OK;  // same boxes in the same order: layout and valid data unchanged
-  return apply_layout(ctx, ng, t2);
+  return ADG_OK;
+}
+
+// Regrid (AmrDG.h:935-986), synchronous: tags, boxes, and a new layout with
+// the state remapped when the boxes changed.
+int regrid(adg_ctx* ctx) {
+  size_t nt = 0;
+  int rc = regrid_tags(ctx, &nt);
+  if (rc) return rc;
+  std::vector<std::vector<amr::IBox>> ng;
+  rc = regrid_boxes(ctx, nt, &ng);
+  if (rc) return rc;
+  if (ng == ctx->hier.grids) return ADG_OK;  // same boxes in the same order: layout and valid data unchanged
+  return apply_layout(ctx, ng, std::chrono::steady_clock::now());
+}
+
+// What a step changes beyond its scratch, copied on the stream before a step
+// that runs while the host clusters, and back if the boxes change.
+int snapshot_step_state(adg_ctx* ctx) {
+  const size_t nu = ctx->hier.n_elem() * ctx->ks->Q * ctx->ks->Np_s;
+  ADG_CUDA(ctx->snap_Uw.ensure(nu), "alloc snapshot");
+  ADG_CUDA(ctx->snap_scal.ensure(kScalCount), "alloc snapshot");
+  ADG_CUDA(ctx->snap_cnt.ensure(2), "alloc snapshot");
+  ADG_CUDA(ctx->snap_status.ensure(1), "alloc snapshot");
+  cudaStream_t s = ctx->stream;
+  ADG_CUDA(cudaMemcpyAsync(ctx->snap_Uw.p, ctx->Uw.p, nu * sizeof(double), cudaMemcpyDeviceToDevice, s), "snapshot");
+  ADG_CUDA(cudaMemcpyAsync(ctx->snap_scal.p, ctx->scal.p, kScalCount * sizeof(double), cudaMemcpyDeviceToDevice, s),
+           "snapshot");
+  ADG_CUDA(cudaMemcpyAsync(ctx->snap_cnt.p, ctx->limited.p, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s),
+           "snapshot");
+  if (ctx->fb_total.p)
+    ADG_CUDA(cudaMemcpyAsync(ctx->snap_cnt.p + 1, ctx->fb_total.p, sizeof(unsigned long long),
+                             cudaMemcpyDeviceToDevice, s), "snapshot");
+  ADG_CUDA(cudaMemcpyAsync(ctx->snap_status.p, ctx->status.p, sizeof(unsigned int), cudaMemcpyDeviceToDevice, s),
+           "snapshot");
+  return ADG_OK;
+}
+
+int restore_step_state(adg_ctx* ctx) {
+  const size_t nu = ctx->hier.n_elem() * ctx->ks->Q * ctx->ks->Np_s;
+  cudaStream_t s = ctx->stream;
+  ADG_CUDA(cudaMemcpyAsync(ctx->Uw.p, ctx->snap_Uw.p, nu * sizeof(double), cudaMemcpyDeviceToDevice, s), "restore");
+  ADG_CUDA(cudaMemcpyAsync(ctx->scal.p, ctx->snap_scal.p, kScalCount * sizeof(double), cudaMemcpyDeviceToDevice, s),
+           "restore");
+  ADG_CUDA(cudaMemcpyAsync(ctx->limited.p, ctx->snap_cnt.p, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s),
+           "restore");
+  if (ctx->fb_total.p)
+    ADG_CUDA(cudaMemcpyAsync(ctx->fb_total.p, ctx->snap_cnt.p + 1, sizeof(unsigned long long),
+                             cudaMemcpyDeviceToDevice, s), "restore");
+  ADG_CUDA(cudaMemcpyAsync(ctx->status.p, ctx->snap_status.p, sizeof(unsigned int), cudaMemcpyDeviceToDevice, s),
+           "restore");
+  return ADG_OK;
 }
 
 // Switch to the layout of the given boxes per level and remap the state:
@@ -713,18 +798,9 @@ int capture_graph(adg_ctx* ctx) {
   return ADG_OK;
 }
 
-int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
-  if (ctx->cfg.limiter_t > 1) use_graph = false;  // the step's kernels then differ from step to step
-  if (regrid_due(ctx)) {
-    auto t0 = std::chrono::steady_clock::now();
-    int rc = regrid(ctx);
-    if (rc) return rc;
-    ctx->regrid_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-  }
-  ctx->dof_updates += (long long)ctx->hier.n_valid() * ctx->ks->Q * ctx->ks->Np_s;
-  if (ctx->seed_mode && ctx->seed) ctx->seed_predicted += (long long)ctx->hier.n_elem();
-  ctx->leaf_dof_updates += (long long)ctx->n_leaf * ctx->ks->Q * ctx->ks->Np_s;
-  ctx->first_step = false;
+// The step's kernels on the current layout: the captured graph (updated or
+// re-captured after a layout change) or direct launches.
+int launch_one_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
   if (use_graph && !ev) {
     if (!ctx->graph_exec || ctx->graph_stale) {
       auto t0 = std::chrono::steady_clock::now();
@@ -734,10 +810,56 @@ int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
     }
     ADG_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream), "graph launch");
     ctx->launches += ctx->graph_kernels;
-  } else {
-    int rc = launch_step(ctx, ev);
-    if (rc) return rc;
+    return ADG_OK;
   }
+  return launch_step(ctx, ev);
+}
+
+void count_step(adg_ctx* ctx) {
+  ctx->dof_updates += (long long)ctx->hier.n_valid() * ctx->ks->Q * ctx->ks->Np_s;
+  if (ctx->seed_mode && ctx->seed) ctx->seed_predicted += (long long)ctx->hier.n_elem();
+  ctx->leaf_dof_updates += (long long)ctx->n_leaf * ctx->ks->Q * ctx->ks->Np_s;
+}
+
+// One evolve-loop body.  A due regrid normally overlaps the step: the tags
+// go to the host, the step runs on the current boxes while the host
+// clusters, and only if the clustering changes the boxes is the step's state
+// restored, the new layout applied and the step run again; either way the
+// result is the one of regridding first.  The first step and the per-stage
+// timing path regrid synchronously.
+int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
+  if (ctx->cfg.limiter_t > 1) use_graph = false;  // the step's kernels then differ from step to step
+  int rc = ADG_OK;
+  if (regrid_due(ctx) && !ctx->first_step && !ev) {
+    auto t0 = std::chrono::steady_clock::now();
+    size_t nt = 0;
+    rc = regrid_tags(ctx, &nt);
+    if (rc == ADG_OK) rc = snapshot_step_state(ctx);
+    if (rc == ADG_OK) rc = launch_one_step(ctx, use_graph, nullptr);
+    std::vector<std::vector<amr::IBox>> ng;
+    if (rc == ADG_OK) rc = regrid_boxes(ctx, nt, &ng);
+    if (rc == ADG_OK && ng != ctx->hier.grids) {
+      ctx->n_rollbacks++;
+      rc = restore_step_state(ctx);
+      if (rc == ADG_OK) rc = apply_layout(ctx, ng, std::chrono::steady_clock::now());
+      if (rc == ADG_OK) rc = launch_one_step(ctx, use_graph, nullptr);
+    }
+    if (rc) return rc;
+    ctx->regrid_ms += ms_between(t0, std::chrono::steady_clock::now());
+    count_step(ctx);
+    ctx->nstep++;
+    return ADG_OK;
+  }
+  if (regrid_due(ctx)) {
+    auto t0 = std::chrono::steady_clock::now();
+    rc = regrid(ctx);
+    if (rc) return rc;
+    ctx->regrid_ms += ms_between(t0, std::chrono::steady_clock::now());
+  }
+  count_step(ctx);
+  ctx->first_step = false;
+  rc = launch_one_step(ctx, use_graph, ev);
+  if (rc) return rc;
   ctx->nstep++;
   return ADG_OK;
 }

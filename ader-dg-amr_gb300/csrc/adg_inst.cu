@@ -9,15 +9,27 @@ namespace {
 
 using O = ADG_NS::Ops;
 
-template <int E>
+// Dynamic shared memory of k_predictor per phase (ld = E Q + 1 slots per point):
+//   FP64 sweeps             D NQ_ST ld doubles   (MODE 0 first sweep: D NQ_INIT)
+//   FP32 sweeps (MODE 2)    D NQ_ST ld floats
+//   final volume slices     (1 + D) NQ_S ld doubles
+//   face traces             2 NQ_BD ld doubles   (one direction at a time)
+//   seed residual           2 E Q doubles
+template <int E, int MODE>
 constexpr size_t smem_bytes() {
-  constexpr int a = O::D * O::NQ_ST, b = 2 * O::D * O::NQ_BD;
-  return (size_t)(a > b ? a : b) * (E * O::Q + 1) * sizeof(double);
+  constexpr size_t ld = E * O::Q + 1;
+  constexpr size_t sweeps = MODE == 2 ? O::D * O::NQ_ST * ld * sizeof(float) : O::D * O::NQ_ST * ld * sizeof(double);
+  constexpr size_t fin = (1 + O::D) * O::NQ_S * ld * sizeof(double);
+  constexpr size_t faces = 2 * O::NQ_BD * ld * sizeof(double);
+  constexpr size_t red = 2 * E * O::Q * sizeof(double);
+  constexpr size_t m1 = sweeps > fin ? sweeps : fin;
+  constexpr size_t m2 = faces > red ? faces : red;
+  return m1 > m2 ? m1 : m2;
 }
 
 template <int E, int MODE>
 cudaError_t launch_predictor_mode(const PredictorArgs& a, cudaStream_t s) {
-  constexpr size_t smem = smem_bytes<E>();
+  constexpr size_t smem = smem_bytes<E, MODE>();
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_predictor<O, E, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -46,12 +58,14 @@ struct Impl final : KernelSet {
     NQ_ST = O::NQ_ST;
     NQ_BD = O::NQ_BD;
     NQ_S = O::NQ_S;
+    NM = O::NM;
+    TR_TILE = tr_tile<O>();
     linear_fp64_per_column = O::LINEAR_FP64_PER_COLUMN;
   }
 #if ADG_D == 2
   std::vector<int> elems_per_block_choices() const override { return {8, 16, 32}; }
   size_t predictor_smem(int E) const override {
-    return E == 8 ? smem_bytes<8>() : E == 16 ? smem_bytes<16>() : smem_bytes<32>();
+    return E == 8 ? smem_bytes<8, 0>() : E == 16 ? smem_bytes<16, 0>() : smem_bytes<32, 0>();
   }
   cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s, int mode) const override {
     if (E == 8) return launch_predictor<8>(a, s, mode);
@@ -61,7 +75,7 @@ struct Impl final : KernelSet {
 #else
   std::vector<int> elems_per_block_choices() const override { return {4, 8, 16}; }
   size_t predictor_smem(int E) const override {
-    return E == 4 ? smem_bytes<4>() : E == 8 ? smem_bytes<8>() : smem_bytes<16>();
+    return E == 4 ? smem_bytes<4, 0>() : E == 8 ? smem_bytes<8, 0>() : smem_bytes<16, 0>();
   }
   cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s, int mode) const override {
     if (E == 4) return launch_predictor<4>(a, s, mode);
@@ -70,9 +84,9 @@ struct Impl final : KernelSet {
   }
 #endif
   cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s) const override {
-    const long long n = nface * O::NQ_BD;
-    const int bs = 256;
-    k_numflux<O><<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(a);
+    if (nface <= 0) return cudaSuccess;
+    constexpr int FB = numflux_faces_per_block<O>();
+    k_numflux<O><<<(unsigned)((nface + FB - 1) / FB), FB * O::NQ_BD, 0, s>>>(a);
     return cudaGetLastError();
   }
   cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const override {
@@ -82,14 +96,13 @@ struct Impl final : KernelSet {
     return cudaGetLastError();
   }
   cudaError_t dt_reduce(const DtArgs& a, cudaStream_t s) const override {
-    const int bs = 64;
-    k_dt_reduce<O><<<(a.n_valid + bs - 1) / bs, bs, 0, s>>>(a);
+    k_dt_reduce<O><<<(a.n_valid + kDtElems - 1) / kDtElems, 128, 0, s>>>(a);
     return cudaGetLastError();
   }
   cudaError_t average_down(double* Uw, const int* rec, int nrec, cudaStream_t s) const override {
-    const long long n = (long long)nrec * O::Q;
-    if (n == 0) return cudaSuccess;
-    k_average_down<O><<<(unsigned)((n + 31) / 32), dim3(32, 1 << O::D), 0, s>>>(Uw, rec, nrec);
+    if (nrec <= 0) return cudaSuccess;
+    constexpr int RB = ad_records_per_block<O>();
+    k_average_down<O><<<(unsigned)((nrec + RB - 1) / RB), dim3(RB * O::Q, 1 << O::D), 0, s>>>(Uw, rec, nrec);
     return cudaGetLastError();
   }
   cudaError_t scatter(const ScatterArgs& a, cudaStream_t s) const override {

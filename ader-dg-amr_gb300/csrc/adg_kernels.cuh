@@ -3,8 +3,11 @@
 // Data layout (HBM, FP64):
 //   Uw    [elem][q][n]                 n < Np_s   (spatial modes)
 //   Rvol  [elem][q][n]                 M U + sum_d (Dt/dx_d) Sk_corr[d] F_d
-//   Tr    [elem][face 2d+s][field][m]  field: u_q (Q), f_q (Q), |un|+c (1); m < NQ_BD
-//   Fnum  [face][q][m]                 local Lax-Friedrichs flux at face points
+//   Tr    [elem][face 2d+s][tile]      tile = field * NQ_BD + t * NS_BD + x (time node t,
+//                                      spatial face point x < NS_BD = NQ_BD / N), field: u_q (Q),
+//                                      f_q (Q), |un|+c (1); tiles padded to an even count of doubles
+//   Fnum  [face][q][j]                 tangential moments (j < NM) of the local
+//                                      Lax-Friedrichs flux over the face
 // Element-level work is organised in "columns": one thread owns one
 // (element, variable) pair and runs the generated straight-line FP64
 // operators on it; point-wise physics runs one thread per (element, point).
@@ -13,6 +16,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "adg_async.cuh"
 #include "adg_device.cuh"
 
 namespace adg {
@@ -28,6 +32,14 @@ struct LevelGeom {
 // kernels read the ratios instead of dividing per thread.
 constexpr int kScalDtDx = 2;
 constexpr int kScalCount = kScalDtDx + 3 * kMaxLevels;
+
+// Doubles per (element, face) trace tile in Tr: the 2Q+1 fields at the NQ_BD
+// face points, padded to an even count so that every tile starts on a
+// 16-byte boundary.
+template <class O>
+constexpr int tr_tile() {
+  return ((2 * O::Q + 1) * O::NQ_BD + 1) & ~1;
+}
 
 struct PredictorArgs {
   const double* Uw;
@@ -136,13 +148,90 @@ __device__ __forceinline__ void picard_sweep_f32(const float* hw, const float* c
   __syncthreads();
 }
 
+// Point-wise fluxes of time slice K (H at the NS spatial points of time node
+// K in sh, shared [point][col]) accumulated into the time integrals
+// Fbar_d = sum_k w_k F_d(., t_k) (fbar, shared [d][point][col]); K = 0
+// initialises.  The sum runs in the order of vol_term's time stage.
+template <class O, int E, int K>
+__device__ __forceinline__ void flux_slice_accumulate(const double* sh, double* fbar, int ld, double gm1) {
+  constexpr int Q = O::Q, D = O::D, NS = O::NQ_S;
+  const double w = O::weight(K);
+#pragma unroll 2
+  for (int it = threadIdx.x; it < E * NS; it += blockDim.x) {
+    const int m = it % NS;
+    const int e = it / NS;
+    const double* base = sh + m * ld + e * Q;
+    double u[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) u[q] = base[q];
+    double F[D * Q];
+    euler_flux_all<D, double>(u, gm1, F);
+    double* fb = fbar + m * ld + e * Q;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        double& dst = fb[d * NS * ld + q];
+        dst = K == 0 ? w * F[d * Q + q] : fma(w, F[d * Q + q], dst);
+      }
+  }
+}
+
+// Volume fluxes of the final H_w, one time slice after the other: shared
+// memory holds (1 + D) NS ld doubles instead of the D NQ_ST ld of all
+// space-time points at once.
+template <class O, int E, int K>
+__device__ __forceinline__ void final_volume_flux(const double* hw, double* sh, double* fbar, int col, int ld,
+                                                  double gm1) {
+  O::template vol_eval_slice<K>(RegIn{hw}, ColOut{sh + col, ld});
+  __syncthreads();
+  flux_slice_accumulate<O, E, K>(sh, fbar, ld, gm1);
+  __syncthreads();
+  if constexpr (K + 1 < O::N) final_volume_flux<O, E, K + 1>(hw, sh, fbar, col, ld, gm1);
+}
+
+// Face traces of direction DIR: H at the points of its two faces
+// (AmrDG.tpp:437-493), then the normal flux and wave speed there
+// (AmrDG.h:1207-1251), written to Tr.
+template <class O, int E, int DIR>
+__device__ __forceinline__ void face_traces(const double* hw, double* sm, int col, int ld, const PredictorArgs& a,
+                                            int e0, int limit) {
+  constexpr int D = O::D, Q = O::Q, NB = O::NQ_BD, NF = 2 * D, TT = tr_tile<O>();
+  O::template face_eval<DIR, 0>(RegIn{hw}, ColOut{sm + col, ld});
+  O::template face_eval<DIR, 1>(RegIn{hw}, ColOut{sm + NB * ld + col, ld});
+  __syncthreads();
+#pragma unroll 2
+  for (int it = threadIdx.x; it < E * 2 * NB; it += blockDim.x) {
+    const int m = it % NB;
+    const int side = (it / NB) & 1;
+    const int ee = it / (2 * NB);
+    if (e0 + ee >= limit) continue;
+    const int elem = a.elem_list ? a.elem_list[e0 + ee] : e0 + ee;
+    const double* h = sm + (side * NB + m) * ld + ee * Q;
+    double uu[Q], F[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) uu[k] = h[k];
+    const double df = euler_flux_normal<D>(DIR, uu, a.gamma, F);
+    // face_eval's point m = x N + t (time fastest) goes to t NS_BD + x
+    constexpr int NSB = NB / O::N;
+    double* t = a.Tr + ((size_t)elem * NF + 2 * DIR + side) * TT + (m % O::N) * NSB + m / O::N;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      t[k * NB] = uu[k];
+      t[(Q + k) * NB] = F[k];
+    }
+    t[2 * Q * NB] = df;
+  }
+  __syncthreads();
+}
+
 // MODE 0: plain FP64 Picard (the reference's initial guess, P sweeps);
 // MODE 1 / 2: seeded, `sweeps` sweeps from the learned seed in FP64 / FP32,
 // the first one judging the seed by its residual.
 template <class O, int E, int MODE = 0>
 __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NP_ST = O::NP_ST;
-  constexpr int NQ = O::NQ_ST, NB = O::NQ_BD, NI = O::NQ_INIT;
+  constexpr int NQ = O::NQ_ST, NI = O::NQ_INIT;
   constexpr int NCOL = E * Q;
   constexpr int LD = NCOL + 1;  // odd stride: conflict-free point-major access
   extern __shared__ double sm[];
@@ -295,23 +384,24 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
     for (int n = 0; n < NP_ST; ++n) dst[n] = hw[n];
   }
 
-  // ---- corrector volume term (AmrDG.tpp:696-709): M U + sum_d c_d Sk_corr[d] F_d
-  O::vol_eval(RegIn{hw}, ColOut{sm + col, LD});
-  __syncthreads();
-  flux_stage<O, E, NQ>(sm, LD, gm1);
-  __syncthreads();
+  // ---- corrector volume term (AmrDG.tpp:696-709): M U + sum_d c_d Sk_corr[d] F_d,
+  // one time slice of points at a time (the slice's H, then its fluxes
+  // accumulated into the time integral of F_d at the spatial points)
   {
+    constexpr int NS = O::NQ_S;
+    double* fbar = sm + NS * LD;
+    final_volume_flux<O, E, 0>(hw, sm, fbar, col, LD, gm1);
     double R[NP_S], v[NP_S];
 #pragma unroll
     for (int n = 0; n < NP_S; ++n) R[n] = O::mdiag(n) * u[n];
-    O::template vol_term<0>(ColIn{sm + col, LD}, RegOut{v});
+    O::template vol_term_sp<0>(ColIn{fbar + col, LD}, RegOut{v});
 #pragma unroll
     for (int n = 0; n < NP_S; ++n) R[n] = fma(c[0], v[n], R[n]);
-    O::template vol_term<1>(ColIn{sm + NQ * LD + col, LD}, RegOut{v});
+    O::template vol_term_sp<1>(ColIn{fbar + NS * LD + col, LD}, RegOut{v});
 #pragma unroll
     for (int n = 0; n < NP_S; ++n) R[n] = fma(c[1], v[n], R[n]);
     if constexpr (D == 3) {
-      O::template vol_term<2>(ColIn{sm + 2 * NQ * LD + col, LD}, RegOut{v});
+      O::template vol_term_sp<2>(ColIn{fbar + 2 * NS * LD + col, LD}, RegOut{v});
 #pragma unroll
       for (int n = 0; n < NP_S; ++n) R[n] = fma(c[2], v[n], R[n]);
     }
@@ -323,39 +413,41 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   }
   __syncthreads();
 
-  // ---- face traces of H (AmrDG.tpp:437-493) and face physics (AmrDG.h:1207-1251)
-  O::template face_eval<0, 0>(RegIn{hw}, ColOut{sm + 0 * NB * LD + col, LD});
-  O::template face_eval<0, 1>(RegIn{hw}, ColOut{sm + 1 * NB * LD + col, LD});
-  O::template face_eval<1, 0>(RegIn{hw}, ColOut{sm + 2 * NB * LD + col, LD});
-  O::template face_eval<1, 1>(RegIn{hw}, ColOut{sm + 3 * NB * LD + col, LD});
-  if constexpr (D == 3) {
-    O::template face_eval<2, 0>(RegIn{hw}, ColOut{sm + 4 * NB * LD + col, LD});
-    O::template face_eval<2, 1>(RegIn{hw}, ColOut{sm + 5 * NB * LD + col, LD});
-  }
-  __syncthreads();
-  constexpr int NF = 2 * D;
-  constexpr int NFIELD = 2 * Q + 1;
+  // ---- face traces of H (AmrDG.tpp:437-493) and face physics (AmrDG.h:1207-1251),
+  // the two faces of one direction at a time
   const int e0 = blockIdx.x * E;
   const int limit = a.elem_list ? *a.list_count : a.n_elem;
-#pragma unroll 2
-  for (int it = threadIdx.x; it < E * NF * NB; it += blockDim.x) {
-    const int m = it % NB;
-    const int f = (it / NB) % NF;
-    const int ee = it / (NB * NF);
-    if (e0 + ee >= limit) continue;
-    const int elem = a.elem_list ? a.elem_list[e0 + ee] : e0 + ee;
-    const double* h = sm + (f * NB + m) * LD + ee * Q;
-    double uu[Q], F[Q];
+  face_traces<O, E, 0>(hw, sm, col, LD, a, e0, limit);
+  face_traces<O, E, 1>(hw, sm, col, LD, a, e0, limit);
+  if constexpr (D == 3) face_traces<O, E, 2>(hw, sm, col, LD, a, e0, limit);
+}
+
+// N consecutive doubles to registers (and back): 16-byte accesses when every
+// run of the array starts on a 16-byte boundary (even run length).
+template <int N>
+__device__ __forceinline__ void load_run(const double* __restrict__ p, double* v) {
+  if constexpr (N % 2 == 0) {
+    const double2* p2 = reinterpret_cast<const double2*>(p);
 #pragma unroll
-    for (int k = 0; k < Q; ++k) uu[k] = h[k];
-    const double df = euler_flux_normal<D>(f >> 1, uu, a.gamma, F);
-    double* t = a.Tr + (((size_t)elem * NF + f) * NFIELD) * NB + m;
-#pragma unroll
-    for (int k = 0; k < Q; ++k) {
-      t[k * NB] = uu[k];
-      t[(Q + k) * NB] = F[k];
+    for (int i = 0; i < N / 2; ++i) {
+      const double2 x = __ldg(p2 + i);
+      v[2 * i] = x.x;
+      v[2 * i + 1] = x.y;
     }
-    t[2 * Q * NB] = df;
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = __ldg(p + i);
+  }
+}
+template <int N>
+__device__ __forceinline__ void store_run(double* p, const double* v) {
+  if constexpr (N % 2 == 0) {
+    double2* p2 = reinterpret_cast<double2*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 2; ++i) p2[i] = make_double2(v[2 * i], v[2 * i + 1]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) p[i] = v[i];
   }
 }
 
@@ -370,28 +462,64 @@ struct FaceArgs {
   double* Fnum;
 };
 
+// Faces per block of k_numflux: one thread per (face, point), about 256.
+template <class O>
+constexpr int numflux_faces_per_block() {
+  return 256 / O::NQ_BD > 0 ? 256 / O::NQ_BD : 1;
+}
+
+// Numerical flux of FB faces per block, as the tangential moments of the LLF
+// flux (AmrDG_NumericalFlux.tpp:4-41) over each face, the only part of the
+// flux the corrector's boundary operators and the coarse-fine corrections
+// read (Mkbd, P_flux_fc).
+//   Phase 1, thread (face, point): (w_t / 2) (fL + fR - C (uR - uL)).
+//   Phase 2, thread (face, variable, spatial point x): the time integral at x.
+//   Phase 3, thread (face, variable): the tangential moments (face_mom_sp).
 template <class O>
 __global__ void k_numflux(FaceArgs a) {
-  constexpr int D = O::D, Q = O::Q, NB = O::NQ_BD, NF = 2 * D, NFIELD = 2 * Q + 1;
-  const int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int D = O::D, Q = O::Q, N = O::N, NB = O::NQ_BD, NSB = NB / N, NF = 2 * D, NM = O::NM;
+  constexpr int TT = tr_tile<O>(), FB = numflux_faces_per_block<O>(), NT = FB * NB;
+  constexpr int LDH = NB + 1, LDG = NSB + 1;  // padded column strides
+  __shared__ double h[FB * Q * LDH];
+  __shared__ double g[FB * Q * LDG];
   const int64_t nface = a.face_off[D];
-  if (it >= nface * NB) return;
-  const int m = (int)(it % NB);
-  const int f = (int)(it / NB);
-  int d = 0;
+  const int64_t fbase = (int64_t)blockIdx.x * FB;
+  const int nfb = (int)(nface - fbase < FB ? nface - fbase : FB);
+  {
+    const int lf = threadIdx.x / NB, m = threadIdx.x % NB;  // m = t NSB + x
+    if (lf < nfb) {
+      const int64_t f = fbase + lf;
+      int d = 0;
 #pragma unroll
-  for (int k = 1; k < D; ++k)
-    if (f >= a.face_off[k]) d = k;
-  const int L = a.face_left[f], R = a.face_right[f];
-  const double* tl = a.Tr + (((size_t)L * NF + 2 * d + 1) * NFIELD) * NB + m;
-  const double* tr = a.Tr + (((size_t)R * NF + 2 * d + 0) * NFIELD) * NB + m;
-  const double C = fmax(fabs(tl[2 * Q * NB]), fabs(tr[2 * Q * NB]));
-  double* out = a.Fnum + (size_t)f * Q * NB + m;
+      for (int k = 1; k < D; ++k)
+        if (f >= a.face_off[k]) d = k;
+      const int L = a.face_left[f], R = a.face_right[f];
+      const double* tl = a.Tr + ((size_t)L * NF + 2 * d + 1) * TT + m;
+      const double* tr = a.Tr + ((size_t)R * NF + 2 * d + 0) * TT + m;
+      const double C = fmax(fabs(tl[2 * Q * NB]), fabs(tr[2 * Q * NB]));
+      const double hw = 0.5 * O::weight(m / NSB);
 #pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    const double uL = tl[q * NB], uR = tr[q * NB];
-    const double fL = tl[(Q + q) * NB], fR = tr[(Q + q) * NB];
-    out[q * NB] = 0.5 * fma(-C, uR - uL, fL + fR);
+      for (int q = 0; q < Q; ++q) {
+        const double uL = tl[q * NB], uR = tr[q * NB];
+        const double fL = tl[(Q + q) * NB], fR = tr[(Q + q) * NB];
+        h[(lf * Q + q) * LDH + m] = hw * fma(-C, uR - uL, fL + fR);
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nfb * Q * NSB; i += NT) {
+    const int x = i % NSB, c = i / NSB;  // c = face * Q + q
+    const double* hc = h + c * LDH + x;
+    double sum = hc[0];
+#pragma unroll
+    for (int t = 1; t < N; ++t) sum += hc[t * NSB];
+    g[c * LDG + x] = sum;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < nfb * Q; c += NT) {
+    double mom[NM];
+    O::face_mom_sp(ColIn{g + c * LDG, 1}, RegOut{mom});
+    store_run<NM>(a.Fnum + ((size_t)fbase * Q + c) * NM, mom);
   }
 }
 
@@ -417,16 +545,16 @@ __device__ __forceinline__ void pcf_rt(int l, const In& in, Out out) {
 }
 
 template <class O, int DD, int S, class In, class Out>
-__device__ __forceinline__ void pflux_k(int k, const In& in, Out out) {
+__device__ __forceinline__ void pflux_mom_k(int k, const In& in, Out out) {
   if constexpr (O::D == 2) {
-    if (k == 0) O::template pflux<DD, S, 0>(in, out);
-    else O::template pflux<DD, S, 1>(in, out);
+    if (k == 0) O::template pflux_mom<DD, S, 0>(in, out);
+    else O::template pflux_mom<DD, S, 1>(in, out);
   } else {
     switch (k) {
-      case 0: O::template pflux<DD, S, 0>(in, out); break;
-      case 1: O::template pflux<DD, S, 1>(in, out); break;
-      case 2: O::template pflux<DD, S, 2>(in, out); break;
-      default: O::template pflux<DD, S, 3>(in, out); break;
+      case 0: O::template pflux_mom<DD, S, 0>(in, out); break;
+      case 1: O::template pflux_mom<DD, S, 1>(in, out); break;
+      case 2: O::template pflux_mom<DD, S, 2>(in, out); break;
+      default: O::template pflux_mom<DD, S, 3>(in, out); break;
     }
   }
 }
@@ -463,7 +591,7 @@ struct CorrectorArgs {
 //   U_c += (2^D / vol_c) Minv corr,  sgn = +1 on the coarse cell's high face.
 template <class O>
 __device__ __forceinline__ void reflux_add(const CorrectorArgs& a, int r, int lc, int q, double* u) {
-  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NB = O::NQ_BD, NFC = 1 << (D - 1);
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NM = O::NM, NFC = 1 << (D - 1);
   const double dt = a.dt[0];
   double corr[NP_S];
 #pragma unroll
@@ -479,9 +607,9 @@ __device__ __forceinline__ void reflux_add(const CorrectorArgs& a, int r, int lc
       }
     const double Jc = (dt / 2.0) * (area_c / (double)NFC);
     const double Jf = (dt / 2.0) * (area_f / (double)NFC);
-    double fc[NP_S], ff[NP_S], tmp[NP_S];
-    const double* fnc = a.Fnum + ((size_t)a.ent_face[x] * Q + q) * NB;
-#define ADG_FC(DD, SS) O::template bd_term<DD, SS>(RegIn{fnc}, RegOut{fc})
+    double fc[NP_S], ff[NP_S], tmp[NP_S], mc[NM];
+    load_run<NM>(a.Fnum + ((size_t)a.ent_face[x] * Q + q) * NM, mc);
+#define ADG_FC(DD, SS) O::template bd_mom<DD, SS>(RegIn{mc}, RegOut{fc})
     if (d == 0) { if (side) ADG_FC(0, 1); else ADG_FC(0, 0); }
     else if (d == 1) { if (side) ADG_FC(1, 1); else ADG_FC(1, 0); }
     else if constexpr (D == 3) { if (side) ADG_FC(2, 1); else ADG_FC(2, 0); }
@@ -489,8 +617,9 @@ __device__ __forceinline__ void reflux_add(const CorrectorArgs& a, int r, int lc
 #pragma unroll
     for (int n = 0; n < NP_S; ++n) ff[n] = 0.0;
     for (int k = 0; k < NFC; ++k) {
-      const double* fnf = a.Fnum + ((size_t)a.ent_fine[(size_t)x * NFC + k] * Q + q) * NB;
-#define ADG_FF(DD, SS) pflux_k<O, DD, SS>(k, RegIn{fnf}, RegOut{tmp})
+      double mf[NM];
+      load_run<NM>(a.Fnum + ((size_t)a.ent_fine[(size_t)x * NFC + k] * Q + q) * NM, mf);
+#define ADG_FF(DD, SS) pflux_mom_k<O, DD, SS>(k, RegIn{mf}, RegOut{tmp})
       if (d == 0) { if (side) ADG_FF(0, 1); else ADG_FF(0, 0); }
       else if (d == 1) { if (side) ADG_FF(1, 1); else ADG_FF(1, 0); }
       else if constexpr (D == 3) { if (side) ADG_FF(2, 1); else ADG_FF(2, 0); }
@@ -509,38 +638,9 @@ __device__ __forceinline__ void reflux_add(const CorrectorArgs& a, int r, int lc
   for (int n = 0; n < NP_S; ++n) u[n] += inv_jac * (O::minv(n) * corr[n]);
 }
 
-// N consecutive doubles to registers (and back): 16-byte accesses when every
-// run of the array starts on a 16-byte boundary (even run length).
-template <int N>
-__device__ __forceinline__ void load_run(const double* __restrict__ p, double* v) {
-  if constexpr (N % 2 == 0) {
-    const double2* p2 = reinterpret_cast<const double2*>(p);
-#pragma unroll
-    for (int i = 0; i < N / 2; ++i) {
-      const double2 x = __ldg(p2 + i);
-      v[2 * i] = x.x;
-      v[2 * i + 1] = x.y;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < N; ++i) v[i] = __ldg(p + i);
-  }
-}
-template <int N>
-__device__ __forceinline__ void store_run(double* p, const double* v) {
-  if constexpr (N % 2 == 0) {
-    double2* p2 = reinterpret_cast<double2*>(p);
-#pragma unroll
-    for (int i = 0; i < N / 2; ++i) p2[i] = make_double2(v[2 * i], v[2 * i + 1]);
-  } else {
-#pragma unroll
-    for (int i = 0; i < N; ++i) p[i] = v[i];
-  }
-}
-
 template <class O>
 __global__ void k_corrector(CorrectorArgs a) {
-  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NB = O::NQ_BD, NF = 2 * D;
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NM = O::NM, NF = 2 * D;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   // record threads first: their chains are the longest, so they start first
   const int64_t nrq = a.rec_of_elem ? (int64_t)a.nrec * Q : 0;
@@ -559,15 +659,17 @@ __global__ void k_corrector(CorrectorArgs a) {
   const int lev = a.elem_level ? a.elem_level[e] : 0;
   double R[NP_S];
   load_run<NP_S>(a.Rvol + ((size_t)e * Q + q) * NP_S, R);
-  double bp[NP_S], bm[NP_S], fv[NB];
+  // every load first (Rvol, then the moments of the 2D faces), then the update
+  double mf[NF][NM];
   const int* ef = a.elem_face + (size_t)e * NF;
+#pragma unroll
+  for (int k = 0; k < NF; ++k) load_run<NM>(a.Fnum + ((size_t)ef[k] * Q + q) * NM, mf[k]);
+  double bp[NP_S], bm[NP_S];
 #define ADG_BD(DD)                                                                      \
   {                                                                                     \
     const double cd = a.dt[kScalDtDx + 3 * lev + DD];                                  \
-    load_run<NB>(a.Fnum + ((size_t)ef[2 * DD + 1] * Q + q) * NB, fv);                  \
-    O::template bd_term<DD, 1>(RegIn{fv}, RegOut{bp});                                  \
-    load_run<NB>(a.Fnum + ((size_t)ef[2 * DD + 0] * Q + q) * NB, fv);                  \
-    O::template bd_term<DD, 0>(RegIn{fv}, RegOut{bm});                                  \
+    O::template bd_mom<DD, 1>(RegIn{mf[2 * DD + 1]}, RegOut{bp});                       \
+    O::template bd_mom<DD, 0>(RegIn{mf[2 * DD + 0]}, RegOut{bm});                       \
     _Pragma("unroll") for (int n = 0; n < NP_S; ++n) R[n] = fma(-cd, bp[n] - bm[n], R[n]); \
   }
   ADG_BD(0)
@@ -783,26 +885,40 @@ struct DtArgs {
   LevelGeom geom;
 };
 
+// Elements per block of k_dt_reduce (block of 128 threads).
+constexpr int kDtElems = 32;
+
 template <class O>
 __global__ void k_dt_reduce(DtArgs a) {
-  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, EL = Q * NP_S, EB = kDtElems;
+  static_assert(EL % 2 == 0, "element blocks must be whole 16-byte units");
+  // the block's states (contiguous) staged with coalesced 16-byte loads
+  __shared__ __align__(16) double st[EB * EL];
+  __shared__ double upt[EB][Q + 1];
+  const int e0 = blockIdx.x * EB;
+  const int ne = a.n_valid - e0 < EB ? a.n_valid - e0 : EB;
+  for (int i = threadIdx.x; i < ne * (EL / 2); i += blockDim.x)
+    reinterpret_cast<double2*>(st)[i] = __ldg(reinterpret_cast<const double2*>(a.Uw + (size_t)e0 * EL) + i);
+  __syncthreads();
+  for (int i = threadIdx.x; i < ne * Q; i += blockDim.x) {
+    double v;
+    O::u_pt0(RegIn{st + (i / Q) * EL + (i % Q) * NP_S}, RegOut{&v});
+    upt[i / Q][i % Q] = v;
+  }
+  __syncthreads();
   double dtc = 1.0e300;
-  unsigned int st = 0;
-  if (e < a.n_valid) {
+  unsigned int st_bits = 0;
+  if ((int)threadIdx.x < ne) {
+    const int e = e0 + threadIdx.x;
     const int lev = a.elem_level ? a.elem_level[e] : 0;
     double u[Q];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      double v;
-      O::u_pt0(RegIn{a.Uw + ((size_t)e * Q + q) * NP_S}, RegOut{&v});
-      u[q] = v;
-    }
+    for (int q = 0; q < Q; ++q) u[q] = upt[threadIdx.x][q];
     const double lam = euler_cfl_lambda<D>(u, a.gamma);
     dtc = O::CFL * (a.dx_avg[lev] / lam);
-    if (!(u[0] > 0.0)) st |= kStatusNonPositiveDensity;
+    if (!(u[0] > 0.0)) st_bits |= kStatusNonPositiveDensity;
     if (!(dtc == dtc) || !(lam == lam)) {
-      st |= kStatusNaN;
+      st_bits |= kStatusNaN;
       dtc = 1.0e300;
     }
   }
@@ -817,7 +933,7 @@ __global__ void k_dt_reduce(DtArgs a) {
     for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
     if (lane == 0) atomicMin(a.min_bits, (unsigned long long)__double_as_longlong(v));
   }
-  if (st) atomicOr(a.status, st);
+  if (st_bits) atomicOr(a.status, st_bits);
   // the last block to finish publishes Dt (threadFenceReduction pattern)
   __shared__ bool last;
   if (threadIdx.x == 0) {
@@ -957,18 +1073,39 @@ __global__ void k_init_ic(ICArgs a) {
 // u_c = 2^-D Minv sum_l P_fc[l] u_f[l].  rec: coarse, fine_0 .. fine_{2^D-1}.
 // Block (32, 2^D): warp l projects child l of 32 (record, variable) pairs, so
 // every warp runs one operator; warp 0 sums the children in order.
+// Records per block of k_average_down.
+template <class O>
+constexpr int ad_records_per_block() {
+  return O::D == 2 ? 8 : 4;
+}
+
+// Block (RB Q, 2^D): records r0 .. r0+RB-1; the children's states are staged
+// in shared memory with coalesced 16-byte loads (each element's Q Np_s
+// doubles are contiguous), thread (r, q, child) projects one child, row 0
+// sums and scales, and the coarse states leave through shared memory again.
 template <class O>
 __global__ void k_average_down(double* Uw, const int* rec, int nrec) {
-  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NOV = 1 << D;
-  __shared__ double part[NOV][NP_S][33];
-  const int L = threadIdx.y;
-  const long long t = (long long)blockIdx.x * 32 + threadIdx.x;
-  const bool live = t < (long long)nrec * Q;
-  const int r = live ? (int)(t / Q) : 0, q = live ? (int)(t % Q) : 0;
-  const int* rr = rec + (size_t)r * (NOV + 1);
-  double tmp[NP_S];
-  if (live) {
-    const double* uf = Uw + ((size_t)rr[1 + L] * Q + q) * NP_S;
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NOV = 1 << D, RB = ad_records_per_block<O>();
+  constexpr int EL = Q * NP_S, EL2 = EL / 2, NT = RB * Q * NOV;
+  static_assert(EL % 2 == 0, "element blocks must be whole 16-byte units");
+  __shared__ __align__(16) double fine[NOV * RB * EL];
+  __shared__ double part[NOV][NP_S][RB * Q + 1];
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int r0 = blockIdx.x * RB;
+  const int nr = nrec - r0 < RB ? nrec - r0 : RB;
+  for (int i = tid; i < NOV * nr * EL2; i += NT) {
+    const int L = i / (nr * EL2), rem = i % (nr * EL2);
+    const int r = rem / EL2, off = rem % EL2;
+    const int e = rec[(size_t)(r0 + r) * (NOV + 1) + 1 + L];
+    reinterpret_cast<double2*>(fine)[(L * RB + r) * EL2 + off] =
+        __ldg(reinterpret_cast<const double2*>(Uw + (size_t)e * EL) + off);
+  }
+  __syncthreads();
+  const int x = threadIdx.x, L = threadIdx.y;
+  const int r = x / Q, q = x % Q;
+  if (r < nr) {
+    const double* uf = fine + (L * RB + r) * EL + q * NP_S;
+    double tmp[NP_S];
     switch (L) {
       case 0: O::template pfc<0>(RegIn{uf}, RegOut{tmp}); break;
       case 1: O::template pfc<1>(RegIn{uf}, RegOut{tmp}); break;
@@ -985,17 +1122,24 @@ __global__ void k_average_down(double* Uw, const int* rec, int nrec) {
         }
     }
 #pragma unroll
-    for (int n = 0; n < NP_S; ++n) part[L][n][threadIdx.x] = tmp[n];
+    for (int n = 0; n < NP_S; ++n) part[L][n][x] = tmp[n];
   }
   __syncthreads();
-  if (L != 0 || !live) return;
-  double* uc = Uw + ((size_t)rr[0] * Q + q) * NP_S;
+  double* out = fine;  // the children are consumed: [RB][EL] coarse states
+  if (L == 0 && r < nr) {
 #pragma unroll
-  for (int n = 0; n < NP_S; ++n) {
-    double sum = 0.0;
+    for (int n = 0; n < NP_S; ++n) {
+      double sum = 0.0;
 #pragma unroll
-    for (int l = 0; l < NOV; ++l) sum += part[l][n][threadIdx.x];
-    uc[n] = (1.0 / NOV) * (O::minv(n) * sum);
+      for (int l = 0; l < NOV; ++l) sum += part[l][n][x];
+      out[r * EL + q * NP_S + n] = (1.0 / NOV) * (O::minv(n) * sum);
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < nr * EL2; i += NT) {
+    const int rr = i / EL2, off = i % EL2;
+    reinterpret_cast<double2*>(Uw + (size_t)rec[(size_t)(r0 + rr) * (NOV + 1)] * EL)[off] =
+        reinterpret_cast<const double2*>(out)[rr * EL2 + off];
   }
 }
 

@@ -13,6 +13,8 @@ namespace adg {
 
 struct KernelSet {
   int D, P, Q, Np_s, Np_st, NQ_ST, NQ_BD, NQ_S;
+  int NM;       // tangential flux moments per face and variable (Fnum entries)
+  int TR_TILE;  // doubles per (element, face) trace tile (Tr entries)
   int linear_fp64_per_column;
   virtual ~KernelSet() = default;
   virtual std::vector<int> elems_per_block_choices() const = 0;

@@ -103,9 +103,9 @@ extern "C" int adg_ader_step_noalloc(int D, int P, const int n_cell[3], const do
   const size_t o_rv = off;
   off = align256(off + (size_t)n * Q * ks->Np_s * sizeof(double));
   const size_t o_tr = off;
-  off = align256(off + (size_t)n * 2 * D * (2 * Q + 1) * ks->NQ_BD * sizeof(double));
+  off = align256(off + (size_t)n * 2 * D * ks->TR_TILE * sizeof(double));
   const size_t o_fn = off;
-  off = align256(off + nface * Q * ks->NQ_BD * sizeof(double));
+  off = align256(off + nface * Q * ks->NM * sizeof(double));
   if (off > kScratchBytes) return ADG_ERR_NOALLOC_CAPACITY;
 
   int dev = 0;

@@ -490,6 +490,36 @@ def build_ops(el):
         check_chain(stages, el.dense_sk_corr(d), f"vol_term{d}")
         ops[f"vol_term{d}"] = (stages, len(pt_keys_st), el.Np_s)
 
+    # ---- vol_eval_slice[k]: st modes -> the spatial GL points of time node k
+    # (one time slice of vol_eval's points, pts_s order).  Together with
+    # vol_term_sp this lets a kernel hold one slice of point values at a time:
+    # the same stages as vol_eval restricted to one time column.
+    sp_keys = [tuple(('q', k) for k in pt) for pt in el.pts_s]
+    for k in range(N):
+        tabs = {p: el.val for p in range(D)}
+        tabs[D] = [[el.val[a][k]] for a in range(P + 1)]
+        stages, keys = ch.eval_chain(list(range(D, -1, -1)), st_keys, tabs, D + 1)
+        stages.append(stage_from_map(keys, sp_keys, lambda ok: [(ok + (('q', 0),), 1.0)]))
+        dense = [el.V[el.pts_st.index(tuple(pt) + (k,))] for pt in el.pts_s]
+        check_chain(stages, dense, f"vol_eval_slice{k}")
+        ops[f"vol_eval_slice{k}"] = (stages, el.Np_st, len(sp_keys))
+
+    # ---- vol_term_sp[d]: the spatial stages of vol_term[d], applied to the
+    # time-integrated flux sum_k w_k F_d(x, t_k) at the spatial points
+    for d in range(D):
+        tabs = {}
+        for p in range(D):
+            base = el.dval if p == d else el.val
+            tabs[p] = [[base[a][k] * el.weights[k] for k in range(N)] for a in range(P + 1)]
+        stages, keys = ch.project_chain(list(range(D)), sp_keys, tabs, degree_ok(P))
+        s_keys = [tuple(('m', a) for a in n) for n in el.mi_s]
+        stages.append(stage_from_map(keys, s_keys, lambda ok: [(ok, 1.0)]))
+        dsk = el.dense_sk_corr(d)
+        dense = [[dsk[r][el.pts_st.index(tuple(pt) + (0,))] / el.weights[0] for pt in el.pts_s]
+                 for r in range(el.Np_s)]
+        check_chain(stages, dense, f"vol_term_sp{d}")
+        ops[f"vol_term_sp{d}"] = (stages, len(sp_keys), el.Np_s)
+
     # ---- face_eval[d][side]: st modes -> face points (free spatial dims, time)
     bd_pt_keys = [tuple(('q', k) for k in pt) for pt in el.pts_bd]
     for d in range(D):
@@ -713,11 +743,148 @@ def add_amr_ops(el, ops):
                                                      for r in rows])], len(el.pts_bd), len(ms))
 
 
+def legendre_monomial(n):
+    """Exact monomial coefficients of P_n (index = power)."""
+    p0, p1 = [Fraction(1)], [Fraction(0), Fraction(1)]
+    if n == 0:
+        return p0
+    for k in range(2, n + 1):
+        xp1 = [Fraction(0)] + p1
+        p2 = [Fraction(0)] * (k + 1)
+        for i, v in enumerate(xp1):
+            p2[i] += Fraction(2 * k - 1, k) * v
+        for i, v in enumerate(p0):
+            p2[i] -= Fraction(k - 1, k) * v
+        p0, p1 = p1, p2
+    return p1
+
+
+def legendre_shift_coeffs(P, upper):
+    """c[n][j]: P_n((x + s) / 2) = sum_j c[n][j] P_j(x), s = +1 (upper half of
+    a coarse interval) or -1 (lower half), exact."""
+    s = Fraction(1 if upper else -1)
+    out = []
+    for n in range(P + 1):
+        a = legendre_monomial(n)
+        # sum_i a_i ((x + s) / 2)^i in monomials of x
+        poly = [Fraction(0)] * (n + 1)
+        for i, ai in enumerate(a):
+            for r in range(i + 1):  # binomial term x^r s^(i-r)
+                poly[r] += ai * Fraction(math.comb(i, r)) * s ** (i - r) / Fraction(2) ** i
+        row = []
+        for j in range(P + 1):
+            pj = legendre_monomial(j)
+            integ = Fraction(0)
+            for r, pr in enumerate(poly):
+                for t, pt in enumerate(pj):
+                    if (r + t) % 2 == 0:
+                        integ += pr * pt * Fraction(2, r + t + 1)
+            row.append(Fraction(2 * j + 1, 2) * integ)
+        out.append(row)
+    return out
+
+
+def add_face_moment_ops(el, ops):
+    """Face moments of the numerical flux.  For a face of direction d the
+    corrector's boundary operators only see the flux through its tangential
+    Legendre moments
+      M[j] = sum_pts w_t prod_a (w_a P_ja(x_a)) fnum(pt),  |j| <= P,
+    (a over the spatial dims != d), because
+      Mkbd{m,p}[d][n] fnum = P_nd(+-1) M[n without d]          (bd_mom)
+      P_flux_fc[k][n] fnum  = P_nd(+-1) sum_j prod_a c[n_a][j_a] M_fine[j]  (pflux_mom)
+    with c the exact Legendre coefficients of P_n((x -+ 1)/2) on a half face.
+    face_mom is the same operator for every direction (the free dims use the
+    same tables)."""
+    D, P, N = el.D, el.P, el.N
+    ch = Chains(el)
+    nfree = D - 1
+    mom = multi_index(P, nfree)
+    mom_keys = [tuple(('m', a) for a in j) for j in mom]
+    bd_pt_keys = [tuple(('q', k) for k in pt) for pt in el.pts_bd]
+    tabs = {i: [[el.val[a][k] * el.weights[k] for k in range(N)] for a in range(P + 1)] for i in range(nfree)}
+    tabs[nfree] = [[el.weights[k] for k in range(N)]]
+    stages, keys = ch.project_chain([nfree] + list(range(nfree)), bd_pt_keys, tabs, degree_ok(P))
+    stages.append(stage_from_map(keys, mom_keys, lambda ok: [(ok + (('m', 0),), 1.0)]))
+    dense_mom = []
+    for j in mom:
+        row = []
+        for pt in el.pts_bd:
+            w = el.weights[pt[nfree]]
+            for i in range(nfree):
+                w *= el.weights[pt[i]] * el.val[j[i]][pt[i]]
+            row.append(w)
+        dense_mom.append(row)
+    check_chain(stages, dense_mom, "face_mom")
+    ops["face_mom"] = (stages, len(bd_pt_keys), len(mom))
+    # face_mom_sp: the tangential stages alone, on the time integral of the
+    # flux at the NQ_BD / N spatial face points (free dims in order)
+    sp_face = list(itertools.product(range(N), repeat=nfree))
+    sp_keys = [tuple(('q', k) for k in pt) for pt in sp_face]
+    tabs_sp = {i: tabs[i] for i in range(nfree)}
+    st_sp, keys_sp = ch.project_chain(list(range(nfree)), sp_keys, tabs_sp, degree_ok(P))
+    st_sp.append(stage_from_map(keys_sp, mom_keys, lambda ok: [(ok, 1.0)]))
+    dense_sp = [[dense_mom[r][el.pts_bd.index(tuple(pt) + (0,))] / el.weights[0] for pt in sp_face]
+                for r in range(len(mom))]
+    check_chain(st_sp, dense_sp, "face_mom_sp")
+    ops["face_mom_sp"] = (st_sp, len(sp_keys), len(mom))
+    pos = {j: i for i, j in enumerate(mom)}
+
+    def composed(rows):
+        """(Np_s x NM) rows times the dense moment operator."""
+        return [[sum(v * dense_mom[c][p] for c, v in r) for p in range(len(el.pts_bd))] for r in rows]
+
+    def dense_of(name):
+        st = ops[name][0]
+        return chain_dense(st)
+
+    for d in range(D):
+        free = [a for a in range(D) if a != d]
+        for side in range(2):
+            rows = [[(pos[tuple(n[a] for a in free)], el.bd[n[d]][side])] for n in el.mi_s]
+            name = f"bd_mom{d}{side}"
+            ref = el.dense_bd_term(d, side)
+            got = composed(rows)
+            scale = max(abs(v) for r in ref for v in r)
+            err = max(abs(got[i][p] - ref[i][p]) for i in range(len(ref)) for p in range(len(ref[0])))
+            if err > 1e-12 * scale:
+                raise SystemExit(f"{name} does not reproduce bd_term{d}{side}: {err / scale}")
+            ops[name] = ([Stage(len(mom), el.Np_s, rows)], len(mom), el.Np_s)
+    c_lo, c_hi = legendre_shift_coeffs(P, False), legendre_shift_coeffs(P, True)
+    nfc = 1 << (D - 1)
+    for d in range(D):
+        free = [a for a in range(D) if a != d]
+        for k in range(nfc):
+            up = {a: (k >> i) & 1 for i, a in enumerate(free)}
+            for side in range(2):
+                rows = []
+                for n in el.mi_s:
+                    terms = []
+                    for j in mom:
+                        v = Fraction(1)
+                        for i, a in enumerate(free):
+                            v *= (c_hi if up[a] else c_lo)[n[a]][j[i]]
+                            if v == 0:
+                                break
+                        if v != 0:
+                            terms.append((pos[j], float(v * Fraction(el.bd[n[d]][side]))))
+                    rows.append(terms)
+                name = f"pflux_mom{d}{side}{k}"
+                ref = dense_of(f"pflux{d}{side}{k}")
+                got = composed(rows)
+                scale = max(abs(v) for r in ref for v in r)
+                err = max(abs(got[i][p] - ref[i][p]) for i in range(len(ref)) for p in range(len(ref[0])))
+                if err > 1e-12 * scale:
+                    raise SystemExit(f"{name} does not reproduce pflux{d}{side}{k}: {err / scale}")
+                ops[name] = ([Stage(len(mom), el.Np_s, rows)], len(mom), el.Np_s)
+    return len(mom)
+
+
 def generate(D, P, out_path):
     el = Element(D, P)
     ops = build_ops(el)
     add_ic_proj(el, ops)
     add_amr_ops(el, ops)
+    n_mom = add_face_moment_ops(el, ops)
     N = P + 1
     qst = N ** (D + 1)
     qbd = N ** D
@@ -730,6 +897,7 @@ def generate(D, P, out_path):
         "__device__ __constant__ const double MDIAG_[] = {" + ", ".join(lit(v) for v in el.Mdiag) + "};",
         "__device__ __constant__ const double MINV_[] = {" + ", ".join(lit(v) for v in el.Minv) + "};",
         "__device__ __constant__ const double NODES_[] = {" + ", ".join(lit(v) for v in el.nodes) + "};",
+        "__device__ __constant__ const double WEIGHTS_[] = {" + ", ".join(lit(v) for v in el.weights) + "};",
         "struct Ops {",
         f"  static constexpr int D = {D};",
         f"  static constexpr int P = {P};",
@@ -741,10 +909,12 @@ def generate(D, P, out_path):
         f"  static constexpr int NQ_BD = {qbd};",
         f"  static constexpr int NQ_S = {N ** D};",
         f"  static constexpr int NQ_INIT = {N ** D};",
+        f"  static constexpr int NM = {n_mom};  // tangential flux moments per face and variable",
         f"  static constexpr double CFL = {lit((1.0 / (2.0 * P + 1.0)) * (1.0 / D))};",
         "  static __device__ __forceinline__ double mdiag(int n) { return MDIAG_[n]; }",
         "  static __device__ __forceinline__ double minv(int n) { return MINV_[n]; }",
         "  static __device__ __forceinline__ double node(int k) { return NODES_[k]; }",
+        "  static __device__ __forceinline__ double weight(int k) { return WEIGHTS_[k]; }",
     ]
     counts = {}
     for name, op in ops.items():
@@ -765,12 +935,17 @@ def generate(D, P, out_path):
     hdr.append(disp("proj", [((d,), f"proj{d}") for d in range(D)], ["d"]))
     hdr.append(disp("proj_init", [((d,), f"proj_init{d}") for d in range(D)], ["d"]))
     hdr.append(disp("vol_term", [((d,), f"vol_term{d}") for d in range(D)], ["d"]))
+    hdr.append(disp("vol_term_sp", [((d,), f"vol_term_sp{d}") for d in range(D)], ["d"]))
+    hdr.append(disp("vol_eval_slice", [((k,), f"vol_eval_slice{k}") for k in range(N)], ["k"]))
     hdr.append(disp("face_eval", [((d, s), f"face_eval{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("bd_term", [((d, s), f"bd_term{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("pcf", [((l,), f"pcf{l}") for l in range(1 << D)], ["l"]))
     hdr.append(disp("pfc", [((l,), f"pfc{l}") for l in range(1 << D)], ["l"]))
     hdr.append(disp("pflux", [((d, s, k), f"pflux{d}{s}{k}") for d in range(D) for s in range(2)
                               for k in range(1 << (D - 1))], ["d", "s", "k"]))
+    hdr.append(disp("bd_mom", [((d, s), f"bd_mom{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
+    hdr.append(disp("pflux_mom", [((d, s, k), f"pflux_mom{d}{s}{k}") for d in range(D) for s in range(2)
+                                  for k in range(1 << (D - 1))], ["d", "s", "k"]))
     # FP64 instruction counts of the linear stages per column and step
     sweeps = P
     per_col = (counts["wu"] + counts["vol_eval_init"] + sum(counts[f"proj_init{d}"] for d in range(D)) + 2 * D * el.Np_st

@@ -291,7 +291,7 @@ int adg_fp64_peak_probe(double* gflops);
  * and the step size; all intermediates live in one fixed device array of
  * ADG_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
  * the process exits.  Problems whose intermediates do not fit return
- * ADG_ERR_NOALLOC_CAPACITY (about 11,000 elements at D=2, P=3).  The first
+ * ADG_ERR_NOALLOC_CAPACITY (about 12,800 elements at D=2, P=3).  The first
  * call on a device looks up the array's device address (make it before any
  * stream capture).  All calls share the array: calls that overlap on the GPU
  * race.  Work is issued on `stream` (NULL: default stream), asynchronously. */

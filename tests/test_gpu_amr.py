@@ -107,3 +107,43 @@ def test_caller_supplied_layout_reproduces_the_run():
     for l in range(a.num_levels()):
         assert np.array_equal(a.get_U_w(l), b.get_U_w(l)), l
     assert a.Dt == b.Dt
+
+
+@pytest.mark.parametrize("case,kw", [("kh_p3_amr", {}),
+                                     ("blast3d_p2_amr", dict(limiter_type="TVB", TVB_M=10.0, t_limit=1))])
+def test_overlapped_regrid_matches_synchronous_regrid(case, kw):
+    """A due regrid overlaps the step (the step runs on the current boxes while
+    the host clusters, and is redone on the new boxes if they differ); the
+    per-stage timing path regrids first.  Both take the same steps bit for
+    bit, also when a forced layout makes the clustering change the boxes
+    (the rollback)."""
+    a = make_gpu_amr(case, **kw)
+    b = make_gpu_amr(case, **kw)
+    dtn = AMR_CASES[case][7]["dtn_regrid"]
+    a.advance(dtn, use_graph=True)
+    b.time_kernels(dtn)
+    # a layout the clustering will not keep: level 0 and one small box per finer level
+    D = a.D
+    for s in (a, b):
+        boxes = [s.boxes(0)]
+        for l in range(1, s.num_levels()):
+            lo = s.boxes(l)[0][:3]
+            hi = lo.copy()
+            hi[:D] = lo[:D] + AMR_CASES[case][7]["blocking_factor"] - 1
+            box = np.concatenate([lo, hi])
+            if l > 1:  # inside the level below with a one-cell margin (its coarse-fine ghosts)
+                prev = boxes[l - 1][0]
+                half = AMR_CASES[case][7]["blocking_factor"] // 2
+                box[:D] = 2 * prev[:D] + half
+                box[3:3 + D] = 2 * prev[:D] + 3 * half - 1
+            boxes.append(box.reshape(1, 6))
+        s.set_layout(boxes)
+    a.advance(2 * dtn, use_graph=True)
+    b.time_kernels(2 * dtn)
+    assert a.num_levels() == b.num_levels()
+    for l in range(a.num_levels()):
+        assert np.array_equal(a.boxes(l), b.boxes(l))
+        assert np.array_equal(a.get_U_w(l), b.get_U_w(l)), l
+    assert a.time == b.time and a.Dt == b.Dt
+    assert a.regrid_count() == b.regrid_count()
+    assert a.status() == 0 and b.status() == 0
