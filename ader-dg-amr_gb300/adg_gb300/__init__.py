@@ -26,6 +26,7 @@ LIB_PATH = os.path.join(_PKG, "_lib", "libadg.so")
 ADG_OK = 0
 ADG_MEM_HOST = 0
 ADG_MEM_DEVICE = 1
+ADG_MEM_HOST_ASYNC = 2
 IC_CODES = {"isentropic_vortex": 0, "vortex": 0, "kh_noise": 1, "kelvin_helmolz_instability": 2,
             "kh_ref": 2, "blast3d": 3, "const": 4}
 
@@ -120,6 +121,7 @@ def lib():
         "adg_level_cell_coords": ([vp, i, ctypes.POINTER(i)], i),
         "adg_tags": ([vp, i, ctypes.POINTER(ctypes.c_uint8)], i),
         "adg_get_step": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_synchronize": ([vp], i),
         "adg_write_plotfile": ([vp, ctypes.c_char_p, i, i, ctypes.POINTER(ctypes.c_char_p)], i),
         "adg_read_plotfile": ([vp, ctypes.c_char_p, i, dp], i),
         "adg_plotfile_info": ([ctypes.c_char_p, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i), dp,
@@ -403,6 +405,23 @@ class AmrDG:
         a = np.ascontiguousarray(arr, dtype=np.float64)
         assert a.size == self.level_cells(lev) * self.Q * self.Np_s
         self._check(self._L.adg_set_state(self.ctx, lev, a.ctypes.data, ADG_MEM_HOST), "adg_set_state")
+
+    def get_U_w_async(self, pinned, lev=0):
+        """Queue the copy of level lev into a PinnedArray of shape
+        (cells, Q, Np_s); valid after synchronize()."""
+        assert pinned.array.shape == (self.level_cells(lev), self.Q, self.Np_s)
+        self._check(self._L.adg_get_state(self.ctx, lev, pinned.array.ctypes.data, ADG_MEM_HOST_ASYNC),
+                    "adg_get_state")
+
+    def set_U_w_async(self, pinned, lev=0):
+        """Queue the copy of a PinnedArray into level lev; the array must not
+        change before synchronize()."""
+        assert pinned.array.shape == (self.level_cells(lev), self.Q, self.Np_s)
+        self._check(self._L.adg_set_state(self.ctx, lev, pinned.array.ctypes.data, ADG_MEM_HOST_ASYNC),
+                    "adg_set_state")
+
+    def synchronize(self):
+        self._check(self._L.adg_synchronize(self.ctx), "adg_synchronize")
 
     def get_U_w_device(self, lev, dev_ptr):
         self._check(self._L.adg_get_state(self.ctx, lev, ctypes.c_void_p(dev_ptr), ADG_MEM_DEVICE), "adg_get_state")

@@ -1120,21 +1120,21 @@ int adg_level_cells(const adg_ctx* ctx, int lev, int64_t* ncells) {
 int adg_get_state(adg_ctx* ctx, int lev, double* dst, int mem) {
   int rc = check_ready(ctx);
   if (rc) return rc;
-  if (!dst || lev < 0 || lev >= ctx->hier.nlevels()) return fail(ctx, ADG_ERR_ARG, "bad level or pointer");
+  if (!dst || lev < 0 || lev >= ctx->hier.nlevels() || mem < 0 || mem > 2) return fail(ctx, ADG_ERR_ARG, "bad level, pointer or memory kind");
   const size_t per = (size_t)ctx->ks->Q * ctx->ks->Np_s;
   const size_t off = ctx->hier.level_valid_offset(lev) * per;
   const size_t cnt = ctx->hier.level_valid_count(lev) * per;
   ADG_CUDA(cudaMemcpyAsync(dst, ctx->Uw.p + off, cnt * sizeof(double),
                            mem == ADG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream),
            "get_state copy");
-  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "get_state sync");
+  if (mem != ADG_MEM_HOST_ASYNC) ADG_CUDA(cudaStreamSynchronize(ctx->stream), "get_state sync");
   return ADG_OK;
 }
 
 int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem) {
   int rc = check_ready(ctx);
   if (rc) return rc;
-  if (!src || lev < 0 || lev >= ctx->hier.nlevels()) return fail(ctx, ADG_ERR_ARG, "bad level or pointer");
+  if (!src || lev < 0 || lev >= ctx->hier.nlevels() || mem < 0 || mem > 2) return fail(ctx, ADG_ERR_ARG, "bad level, pointer or memory kind");
   const size_t per = (size_t)ctx->ks->Q * ctx->ks->Np_s;
   const size_t off = ctx->hier.level_valid_offset(lev) * per;
   const size_t cnt = ctx->hier.level_valid_count(lev) * per;
@@ -1145,7 +1145,13 @@ int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem) {
     rc = launch_ghost_fill(ctx);
     if (rc) return rc;
   }
-  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "set_state sync");
+  if (mem != ADG_MEM_HOST_ASYNC) ADG_CUDA(cudaStreamSynchronize(ctx->stream), "set_state sync");
+  return ADG_OK;
+}
+
+int adg_synchronize(adg_ctx* ctx) {
+  if (!ctx) return ADG_ERR_ARG;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "synchronize");
   return ADG_OK;
 }
 

@@ -504,7 +504,9 @@ def run_ours(args, w):
     value = whole_job_rate(head["dof"], world, ms)
 
     # end to end through the C ABI with host buffers: every step copies the
-    # state of every level in from page-locked host memory and back out
+    # state of every level in from page-locked host memory, runs the step
+    # (graph replay) and copies every level back out; the copies are queued
+    # on the context's stream and the host waits once per step for the result
     s = head["sim"]
     e2e_steps = max(5, min(args.steps, 50))
     nl = s.num_levels()
@@ -522,13 +524,14 @@ def run_ours(args, w):
             for l in range(len(hosts)):
                 hosts[l].array[:] = s.get_U_w(l)
         for l in range(len(hosts)):
-            s.set_U_w(hosts[l].array, l)
+            s.set_U_w_async(hosts[l], l)
             h2d += hosts[l].array.nbytes
-        s.time_integration()
+        s.advance(1, use_graph=True)
         for l in range(s.num_levels()):
             if l < len(hosts) and hosts[l].array.shape[0] == s.level_cells(l):
-                hosts[l].array[:] = s.get_U_w(l)
+                s.get_U_w_async(hosts[l], l)
                 d2h += hosts[l].array.nbytes
+        s.synchronize()
     e2e_s = barrier_max(time.perf_counter() - t0)
     d_after, _ = s.dof_updates()
     e2e_val = (d_after - d_before) * world / e2e_s

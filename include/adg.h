@@ -35,6 +35,8 @@ extern "C" {
 
 #define ADG_MEM_HOST 0
 #define ADG_MEM_DEVICE 1
+#define ADG_MEM_HOST_ASYNC 2 /* page-locked host buffer; the copy is queued on the context's stream and the
+                                call returns at once: adg_synchronize before the buffer is read or reused */
 
 /* Initial conditions (Source/Model/CompressibleEuler/Compressible_Euler.h:120-368). */
 #define ADG_IC_VORTEX 0     /* isentropic vortex, free stream (u_inf, v_inf) */
@@ -100,6 +102,9 @@ int adg_num_levels(const adg_ctx* ctx, int* nlev);
 int adg_level_cells(const adg_ctx* ctx, int lev, int64_t* ncells);
 int adg_get_state(adg_ctx* ctx, int lev, double* dst, int mem);
 int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem);
+/* Waits for everything queued on the context's stream (copies of
+ * ADG_MEM_HOST_ASYNC, steps of adg_advance). */
+int adg_synchronize(adg_ctx* ctx);
 
 /* Time step size: current Dt (device-computed), set an explicit Dt, or
  * recompute it from the state (set_Dt, AmrDG.h:1253-1357). */

@@ -83,3 +83,25 @@ def test_free_stream_is_preserved():
     s.advance(10)
     u1 = s.get_U_w()
     assert np.max(np.abs(u1 - u0)) < 1e-13
+
+
+def test_async_host_copies_match_synchronous_ones():
+    """ADG_MEM_HOST_ASYNC: copies queued on the context's stream into and out
+    of page-locked host memory give the synchronous copies' values once
+    adg_synchronize returns; an unknown memory kind is rejected."""
+    a = make_gpu("kh_p3")
+    a.advance(3)
+    pin = G.PinnedArray((a.level_cells(0), a.Q, a.Np_s))
+    a.get_U_w_async(pin, 0)
+    a.synchronize()
+    assert np.array_equal(pin.array, a.get_U_w(0))
+    b = make_gpu("kh_p3")
+    b.set_U_w_async(pin, 0)
+    b.synchronize()
+    assert np.array_equal(b.get_U_w(0), a.get_U_w(0))
+    b.Dt = a.Dt  # the state alone does not carry the time step
+    b.advance(2)
+    a.advance(2)
+    assert np.array_equal(b.get_U_w(0), a.get_U_w(0))
+    assert a._L.adg_get_state(a.ctx, 0, pin.array.ctypes.data, 7) == 1
+    pin.free()
