@@ -179,45 +179,75 @@ __device__ __forceinline__ void flux_slice_accumulate(const double* sh, double* 
 
 // Volume fluxes of the final H_w, one time slice after the other: shared
 // memory holds (1 + D) NS ld doubles instead of the D NQ_ST ld of all
-// space-time points at once.
+// space-time points at once.  With FACE_FROM_SLICES each column also
+// extrapolates its face values of the slice (face_slice) and writes them to
+// its element's trace tiles (variable q at time node K).
 template <class O, int E, int K>
 __device__ __forceinline__ void final_volume_flux(const double* hw, double* sh, double* fbar, int col, int ld,
-                                                  double gm1) {
+                                                  double gm1, double* tr_elem, int q) {
+  constexpr int D = O::D, NB = O::NQ_BD, NSB = NB / O::N, TT = tr_tile<O>();
   O::template vol_eval_slice<K>(RegIn{hw}, ColOut{sh + col, ld});
+  if constexpr (O::FACE_FROM_SLICES) {
+    if (tr_elem) {
+      double fv[NSB];
+#define ADG_FS(DD, SS)                                                           \
+  {                                                                              \
+    O::template face_slice<DD, SS>(ColIn{sh + col, ld}, RegOut{fv});             \
+    double* t = tr_elem + (2 * DD + SS) * TT + q * NB + K * NSB;                 \
+    _Pragma("unroll") for (int x = 0; x < NSB; ++x) t[x] = fv[x];               \
+  }
+      ADG_FS(0, 0)
+      ADG_FS(0, 1)
+      ADG_FS(1, 0)
+      ADG_FS(1, 1)
+      if constexpr (D == 3) {
+        ADG_FS(2, 0)
+        ADG_FS(2, 1)
+      }
+#undef ADG_FS
+    }
+  }
   __syncthreads();
   flux_slice_accumulate<O, E, K>(sh, fbar, ld, gm1);
   __syncthreads();
-  if constexpr (K + 1 < O::N) final_volume_flux<O, E, K + 1>(hw, sh, fbar, col, ld, gm1);
+  if constexpr (K + 1 < O::N) final_volume_flux<O, E, K + 1>(hw, sh, fbar, col, ld, gm1, tr_elem, q);
 }
 
 // Face traces of direction DIR: H at the points of its two faces
-// (AmrDG.tpp:437-493), then the normal flux and wave speed there
-// (AmrDG.h:1207-1251), written to Tr.
+// (AmrDG.tpp:437-493; from the modes, or already in Tr with
+// FACE_FROM_SLICES), then the normal flux and wave speed there
+// (AmrDG.h:1207-1251), written to Tr in tile order.
 template <class O, int E, int DIR>
 __device__ __forceinline__ void face_traces(const double* hw, double* sm, int col, int ld, const PredictorArgs& a,
                                             int e0, int limit) {
-  constexpr int D = O::D, Q = O::Q, NB = O::NQ_BD, NF = 2 * D, TT = tr_tile<O>();
-  O::template face_eval<DIR, 0>(RegIn{hw}, ColOut{sm + col, ld});
-  O::template face_eval<DIR, 1>(RegIn{hw}, ColOut{sm + NB * ld + col, ld});
-  __syncthreads();
+  constexpr int D = O::D, Q = O::Q, N = O::N, NB = O::NQ_BD, NSB = NB / N, NF = 2 * D, TT = tr_tile<O>();
+  if constexpr (!O::FACE_FROM_SLICES) {
+    O::template face_eval<DIR, 0>(RegIn{hw}, ColOut{sm + col, ld});
+    O::template face_eval<DIR, 1>(RegIn{hw}, ColOut{sm + NB * ld + col, ld});
+    __syncthreads();
+  }
 #pragma unroll 2
   for (int it = threadIdx.x; it < E * 2 * NB; it += blockDim.x) {
-    const int m = it % NB;
+    const int p = it % NB;  // tile position t NSB + x
     const int side = (it / NB) & 1;
     const int ee = it / (2 * NB);
     if (e0 + ee >= limit) continue;
     const int elem = a.elem_list ? a.elem_list[e0 + ee] : e0 + ee;
-    const double* h = sm + (side * NB + m) * ld + ee * Q;
+    double* t = a.Tr + ((size_t)elem * NF + 2 * DIR + side) * TT + p;
     double uu[Q], F[Q];
+    if constexpr (O::FACE_FROM_SLICES) {
 #pragma unroll
-    for (int k = 0; k < Q; ++k) uu[k] = h[k];
+      for (int k = 0; k < Q; ++k) uu[k] = t[k * NB];
+    } else {
+      // face_eval's point m = x N + t (time fastest)
+      const double* h = sm + (side * NB + (p % NSB) * N + p / NSB) * ld + ee * Q;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) uu[k] = h[k];
+    }
     const double df = euler_flux_normal<D>(DIR, uu, a.gamma, F);
-    // face_eval's point m = x N + t (time fastest) goes to t NS_BD + x
-    constexpr int NSB = NB / O::N;
-    double* t = a.Tr + ((size_t)elem * NF + 2 * DIR + side) * TT + (m % O::N) * NSB + m / O::N;
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
-      t[k * NB] = uu[k];
+      if constexpr (!O::FACE_FROM_SLICES) t[k * NB] = uu[k];
       t[(Q + k) * NB] = F[k];
     }
     t[2 * Q * NB] = df;
@@ -390,7 +420,8 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   {
     constexpr int NS = O::NQ_S;
     double* fbar = sm + NS * LD;
-    final_volume_flux<O, E, 0>(hw, sm, fbar, col, LD, gm1);
+    final_volume_flux<O, E, 0>(hw, sm, fbar, col, LD, gm1,
+                               live ? a.Tr + (size_t)e * 2 * D * tr_tile<O>() : nullptr, q);
     double R[NP_S], v[NP_S];
 #pragma unroll
     for (int n = 0; n < NP_S; ++n) R[n] = O::mdiag(n) * u[n];

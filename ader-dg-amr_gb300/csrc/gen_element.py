@@ -504,6 +504,50 @@ def build_ops(el):
         check_chain(stages, dense, f"vol_eval_slice{k}")
         ops[f"vol_eval_slice{k}"] = (stages, el.Np_st, len(sp_keys))
 
+    # ---- face_slice[d][side]: the face values of one time slice from the
+    # slice's spatial point values, by Lagrange extrapolation along d (H is a
+    # polynomial of degree <= P in x_d, so N nodes determine it exactly):
+    # point x of the face (free dims != d in order) <- sum_i l_i(+-1) H(x with x_d = node i)
+    def lagrange_at(xe):
+        out = []
+        for i in range(N):
+            v = Fraction(1)
+            for j in range(N):
+                if j != i:
+                    v *= (Fraction(xe) - Fraction(el.nodes[j])) / (Fraction(el.nodes[i]) - Fraction(el.nodes[j]))
+            out.append(float(v))
+        return out
+    lag = [lagrange_at(-1.0), lagrange_at(1.0)]
+    sp_index = {tuple(pt): i for i, pt in enumerate(el.pts_s)}
+    for d in range(D):
+        free = [a for a in range(D) if a != d]
+        free_pts = list(itertools.product(range(N), repeat=D - 1))
+        for side in range(2):
+            rows = []
+            for fp in free_pts:
+                terms = []
+                for i in range(N):
+                    full = [0] * D
+                    full[d] = i
+                    for a, v in zip(free, fp):
+                        full[a] = v
+                    terms.append((sp_index[tuple(full)], lag[side][i]))
+                rows.append(terms)
+            st_face = Stage(len(el.pts_s), len(free_pts), rows)
+            name = f"face_slice{d}{side}"
+            ref_full = el.dense_face_eval(d, side)
+            for k in range(N):  # face_slice o vol_eval_slice[k] == face_eval at time node k
+                ev = chain_dense(ops[f"vol_eval_slice{k}"][0])
+                got = chain_dense([st_face])
+                comp = [[sum(got[r][c] * ev[c][m] for c in range(len(el.pts_s))) for m in range(el.Np_st)]
+                        for r in range(len(free_pts))]
+                ref = [ref_full[el.pts_bd.index(tuple(fp) + (k,))] for fp in free_pts]
+                scale = max(abs(v) for r in ref for v in r)
+                err = max(abs(comp[i][j] - ref[i][j]) for i in range(len(ref)) for j in range(el.Np_st))
+                if err > 1e-12 * scale:
+                    raise SystemExit(f"{name} does not reproduce face_eval{d}{side} at time node {k}: {err / scale}")
+            ops[name] = ([st_face], len(el.pts_s), len(free_pts))
+
     # ---- vol_term_sp[d]: the spatial stages of vol_term[d], applied to the
     # time-integrated flux sum_k w_k F_d(x, t_k) at the spatial points
     for d in range(D):
@@ -937,6 +981,7 @@ def generate(D, P, out_path):
     hdr.append(disp("vol_term", [((d,), f"vol_term{d}") for d in range(D)], ["d"]))
     hdr.append(disp("vol_term_sp", [((d,), f"vol_term_sp{d}") for d in range(D)], ["d"]))
     hdr.append(disp("vol_eval_slice", [((k,), f"vol_eval_slice{k}") for k in range(N)], ["k"]))
+    hdr.append(disp("face_slice", [((d, s), f"face_slice{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("face_eval", [((d, s), f"face_eval{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("bd_term", [((d, s), f"bd_term{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("pcf", [((l,), f"pcf{l}") for l in range(1 << D)], ["l"]))
@@ -946,14 +991,26 @@ def generate(D, P, out_path):
     hdr.append(disp("bd_mom", [((d, s), f"bd_mom{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("pflux_mom", [((d, s, k), f"pflux_mom{d}{s}{k}") for d in range(D) for s in range(2)
                                   for k in range(1 << (D - 1))], ["d", "s", "k"]))
-    # FP64 instruction counts of the linear stages per column and step
+    # FP64 instruction counts of the linear stages per column and step: the
+    # first sweep from the initial guess, the remaining sweeps, the corrector
+    # volume term, the face values (from the slices or from the modes,
+    # whichever is cheaper), the face moments (once per face, D faces per
+    # element, time integral then face_mom_sp; the boundary terms of the
+    # corrector are sign copies of them) and the update
     sweeps = P
+    slices_cost = N * sum(counts[f"face_slice{d}{s}"] for d in range(D) for s in range(2))
+    modes_cost = sum(counts[f"face_eval{d}{s}"] for d in range(D) for s in range(2))
+    nsb = N ** (D - 1)
     per_col = (counts["wu"] + counts["vol_eval_init"] + sum(counts[f"proj_init{d}"] for d in range(D)) + 2 * D * el.Np_st
                + (sweeps - 1) * (counts["vol_eval"] + sum(counts[f"proj{d}"] for d in range(D)) + 2 * D * el.Np_st)
                + counts["vol_eval"] + sum(counts[f"vol_term{d}"] for d in range(D))
-               + sum(counts[f"face_eval{d}{s}"] for d in range(D) for s in range(2))
-               + sum(counts[f"bd_term{d}{s}"] for d in range(D) for s in range(2)) + 4 * el.Np_s)
+               + min(slices_cost, modes_cost)
+               + D * (counts["face_mom_sp"] + nsb * (N - 1)) + 4 * el.Np_s)
     hdr.append(f"  static constexpr int LINEAR_FP64_PER_COLUMN = {per_col};")
+    # face values: extrapolated from the time slices when that is cheaper
+    # than evaluating the face traces from the modes
+    hdr.append(f"  static constexpr bool FACE_FROM_SLICES = {'true' if slices_cost < modes_cost else 'false'};"
+               f"  // {slices_cost} vs {modes_cost} FP64 per column")
     # spatial mode of degree 1 in direction d and 0 in the others (the TVB
     # limiter's slope modes, lin_mode_idx of AmrDG.tpp:174-183)
     lin = []
