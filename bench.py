@@ -349,7 +349,7 @@ L2_FLUSH_BYTES = 256 << 20  # twice the 129 MB L2: written before every timed st
 # DRAM bytes (read + write) of one plain k_predictor launch, from the ncu
 # capture summarised in the named profile (same workload and code)
 PROFILED_TRAFFIC = {
-    "kh_p3_amr3": (33.52e6, "profiles/k_predictor_kh_p3_amr3.md"),
+    "kh_p3_amr3": (36.00e6, "profiles/k_predictor_kh_p3_amr3.md"),
 }
 
 
