@@ -141,7 +141,7 @@ struct adg_ctx {
   TableView<int8_t> elem_level;
   DevBuf<double> scal;  // scalar block: [0] Dt, [1] t, Dt/dx per level (kScalDtDx)
   DevBuf<unsigned int> dt_done;  // blocks of the Dt reduction that have finished
-  DevBuf<unsigned long long> min_bits;
+  DevBuf<unsigned long long> rate_bits;  // Dt reduction: max of lambda / dx as IEEE bits
   DevBuf<unsigned int> status;
   // AMR tables
   TableView<int> rf_elem, rf_off, rf_face, rf_fine, ad_all, gf_elem, gf_parent, rf_rec_of_elem;
@@ -198,7 +198,7 @@ struct adg_ctx {
     if (graph) cudaGraphDestroy(graph);
     Uw.release(); Rvol.release(); Tr.release(); Fnum.release(); Hw_dbg.release();
     face_left.release(); face_right.release(); elem_face.release(); elem_cell.release();
-    elem_level.release(); scal.release(); dt_done.release(); min_bits.release(); status.release();
+    elem_level.release(); scal.release(); dt_done.release(); rate_bits.release(); status.release();
     rf_elem.release(); rf_off.release(); rf_face.release(); rf_fine.release(); ad_all.release();
     gf_elem.release(); gf_parent.release(); rf_dside.release(); gf_child.release(); tags.release();
     sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); hseed_f.release(); fb_list.release(); fb_count.release();
@@ -478,17 +478,17 @@ int launch_dt(adg_ctx* ctx, int advance_time) {
   for (int l = 0; l < kMaxLevels; ++l) {
     double s = 0.0;
     for (int d = 0; d < ctx->cfg.D; ++d) s += g.dx[l][d];
-    da.dx_avg[l] = s / (double)ctx->cfg.D;
+    da.inv_dx_avg[l] = 1.0 / (s / (double)ctx->cfg.D);
+    for (int d = 0; d < 3; ++d) da.inv_geom.dx[l][d] = 1.0 / g.dx[l][d];
   }
   da.gamma = ctx->cfg.gamma;
-  da.min_bits = ctx->min_bits.p;
+  da.rate_bits = ctx->rate_bits.p;
   da.status = ctx->status.p;
   da.scal = ctx->scal.p;
   da.done = ctx->dt_done.p;
   da.c_dt = ctx->cfg.c_dt;
   da.advance_time = advance_time;
   da.D = ctx->cfg.D;
-  da.geom = g;
   cudaError_t e = ctx->ks->dt_reduce(da, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "dt launch");
   ctx->launches += 1;
@@ -964,19 +964,16 @@ int adg_ctx_create(const adg_config* cfg, adg_ctx** out) {
   }
   if (ctx->scal.ensure(kScalCount) != cudaSuccess || ctx->dt_done.ensure(1) != cudaSuccess ||
       ctx->limited.ensure(1) != cudaSuccess ||
-      ctx->min_bits.ensure(1) != cudaSuccess || ctx->status.ensure(1) != cudaSuccess) {
+      ctx->rate_bits.ensure(1) != cudaSuccess || ctx->status.ensure(1) != cudaSuccess) {
     delete ctx;
     return ADG_ERR_CUDA;
   }
   double z[kScalCount] = {};
-  unsigned long long big = 0;
-  double huge = 1.0e300;
-  std::memcpy(&big, &huge, sizeof(big));
   unsigned int zero = 0;
   if (cudaMemcpy(ctx->scal.p, z, sizeof(z), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemset(ctx->dt_done.p, 0, sizeof(unsigned int)) != cudaSuccess ||
       cudaMemset(ctx->limited.p, 0, sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMemcpy(ctx->min_bits.p, &big, sizeof(big), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(ctx->rate_bits.p, 0, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMemcpy(ctx->status.p, &zero, sizeof(zero), cudaMemcpyHostToDevice) != cudaSuccess) {
     delete ctx;
     return ADG_ERR_CUDA;

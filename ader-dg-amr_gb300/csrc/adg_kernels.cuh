@@ -503,8 +503,9 @@ constexpr int numflux_faces_per_block() {
 // flux (AmrDG_NumericalFlux.tpp:4-41) over each face, the only part of the
 // flux the corrector's boundary operators and the coarse-fine corrections
 // read (Mkbd, P_flux_fc).
-//   Phase 1, thread (face, point): (w_t / 2) (fL + fR - C (uR - uL)).
-//   Phase 2, thread (face, variable, spatial point x): the time integral at x.
+//   Phase 1, thread (face, point): fL + fR - C (uR - uL), twice the flux.
+//   Phase 2, thread (face, variable, spatial point x): the time integral at x
+//   with the weights w_t / 2.
 //   Phase 3, thread (face, variable): the tangential moments (face_mom_sp).
 template <class O>
 __global__ void k_numflux(FaceArgs a) {
@@ -528,12 +529,11 @@ __global__ void k_numflux(FaceArgs a) {
       const double* tl = a.Tr + ((size_t)L * NF + 2 * d + 1) * TT + m;
       const double* tr = a.Tr + ((size_t)R * NF + 2 * d + 0) * TT + m;
       const double C = fmax(fabs(tl[2 * Q * NB]), fabs(tr[2 * Q * NB]));
-      const double hw = 0.5 * O::weight(m / NSB);
 #pragma unroll
       for (int q = 0; q < Q; ++q) {
         const double uL = tl[q * NB], uR = tr[q * NB];
         const double fL = tl[(Q + q) * NB], fR = tr[(Q + q) * NB];
-        h[(lf * Q + q) * LDH + m] = hw * fma(-C, uR - uL, fL + fR);
+        h[(lf * Q + q) * LDH + m] = fma(-C, uR - uL, fL + fR);  // twice the LLF flux
       }
     }
   }
@@ -541,9 +541,9 @@ __global__ void k_numflux(FaceArgs a) {
   for (int i = threadIdx.x; i < nfb * Q * NSB; i += NT) {
     const int x = i % NSB, c = i / NSB;  // c = face * Q + q
     const double* hc = h + c * LDH + x;
-    double sum = hc[0];
+    double sum = (0.5 * O::weight(0)) * hc[0];
 #pragma unroll
-    for (int t = 1; t < N; ++t) sum += hc[t * NSB];
+    for (int t = 1; t < N; ++t) sum = fma(0.5 * O::weight(t), hc[t * NSB], sum);
     g[c * LDG + x] = sum;
   }
   __syncthreads();
@@ -896,24 +896,27 @@ __global__ void k_limit_tvb(LimiterArgs a) {
 #undef ADG_V
 
 // Time step (AmrDG.h:1253-1357): dt_cell = CFL * dx_avg / lambda(U at spatial
-// quadrature point 0); block minimum then a global atomic minimum on the
-// IEEE bit pattern (positive doubles order like their bits).
+// quadrature point 0), Dt = c_dt min over cells.  Reduced as the maximum of
+// the rate lambda / dx_avg (a product with the host's reciprocal instead of
+// a division per cell; Dt = c_dt * CFL / max): block maximum, then a global
+// atomic maximum on the IEEE bit pattern (non-negative doubles order like
+// their bits).
 struct DtArgs {
   const double* Uw;
   int n_valid;
   const int8_t* elem_level;
-  double dx_avg[kMaxLevels];
+  double inv_dx_avg[kMaxLevels];
   double gamma;
-  unsigned long long* min_bits;
+  unsigned long long* rate_bits;  // 0 between reductions
   unsigned int* status;
-  // finalisation by the last block: Dt = c_dt * min, t += old Dt when
-  // advance_time, Dt/dx of every level; min_bits and done reset
+  // finalisation by the last block: Dt, t += old Dt when advance_time,
+  // Dt/dx of every level (products with inv_geom); rate_bits and done reset
   double* scal;
   unsigned int* done;
   double c_dt;
   int advance_time;
   int D;
-  LevelGeom geom;
+  LevelGeom inv_geom;  // 1 / dx per level and direction
 };
 
 // Elements per block of k_dt_reduce (block of 128 threads).
@@ -937,7 +940,7 @@ __global__ void k_dt_reduce(DtArgs a) {
     upt[i / Q][i % Q] = v;
   }
   __syncthreads();
-  double dtc = 1.0e300;
+  double rate = 0.0;
   unsigned int st_bits = 0;
   if ((int)threadIdx.x < ne) {
     const int e = e0 + threadIdx.x;
@@ -945,43 +948,47 @@ __global__ void k_dt_reduce(DtArgs a) {
     double u[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) u[q] = upt[threadIdx.x][q];
-    const double lam = euler_cfl_lambda<D>(u, a.gamma);
-    dtc = O::CFL * (a.dx_avg[lev] / lam);
+    rate = euler_cfl_lambda<D>(u, a.gamma) * a.inv_dx_avg[lev];
     if (!(u[0] > 0.0)) st_bits |= kStatusNonPositiveDensity;
-    if (!(dtc == dtc) || !(lam == lam)) {
+    if (!(rate == rate)) {
       st_bits |= kStatusNaN;
-      dtc = 1.0e300;
+      rate = 0.0;
     }
   }
-  // warp then block minimum
-  for (int o = 16; o > 0; o >>= 1) dtc = fmin(dtc, __shfl_xor_sync(0xffffffffu, dtc, o));
-  __shared__ double wmin[32];
+  // warp then block maximum
+  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+  __shared__ double wmax[32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) wmin[wid] = dtc;
+  if (lane == 0) wmax[wid] = rate;
   __syncthreads();
   if (wid == 0) {
-    double v = (lane < (int)(blockDim.x + 31) / 32) ? wmin[lane] : 1.0e300;
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (lane == 0) atomicMin(a.min_bits, (unsigned long long)__double_as_longlong(v));
+    double v = (lane < (int)(blockDim.x + 31) / 32) ? wmax[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) atomicMax(a.rate_bits, (unsigned long long)__double_as_longlong(v));
   }
   if (st_bits) atomicOr(a.status, st_bits);
   // the last block to finish publishes Dt (threadFenceReduction pattern)
   __shared__ bool last;
+  __shared__ double dt_s;
   if (threadIdx.x == 0) {
     __threadfence();
     last = atomicAdd(a.done, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    const unsigned long long bits = atomicAdd(a.min_bits, 0ull);
-    const double dt = a.c_dt * __longlong_as_double((long long)bits);
-    if (a.advance_time) a.scal[1] += a.scal[0];
-    a.scal[0] = dt;
-    for (int l = 0; l < kMaxLevels; ++l)
-      for (int d = 0; d < 3; ++d) a.scal[kScalDtDx + 3 * l + d] = d < a.D ? dt / a.geom.dx[l][d] : 0.0;
-    *a.min_bits = (unsigned long long)__double_as_longlong(1.0e300);
-    *a.done = 0u;
+  if (last) {  // block-uniform
+    if (threadIdx.x == 0) {
+      __threadfence();
+      const unsigned long long bits = atomicAdd(a.rate_bits, 0ull);
+      const double dt = a.c_dt * (O::CFL / __longlong_as_double((long long)bits));
+      if (a.advance_time) a.scal[1] += a.scal[0];
+      a.scal[0] = dt;
+      dt_s = dt;
+      *a.rate_bits = 0ull;
+      *a.done = 0u;
+    }
+    __syncthreads();
+    const int i = threadIdx.x;
+    if (i < 3 * kMaxLevels) a.scal[kScalDtDx + i] = i % 3 < a.D ? dt_s * a.inv_geom.dx[i / 3][i % 3] : 0.0;
   }
 }
 
