@@ -514,30 +514,42 @@ def run_ours(args, w):
     # (graph replay) and copies every level back out; the copies are queued
     # on the context's stream and the host waits once per step for the result
     s = head["sim"]
+    L, ctx = s._L, s.ctx
     e2e_steps = max(5, min(args.steps, 50))
-    nl = s.num_levels()
-    hosts = [G.PinnedArray((s.level_cells(l), Q, Nps)) for l in range(nl)]
-    for l in range(nl):
-        hosts[l].array[:] = s.get_U_w(l)
+
+    def check(rc, what):
+        if rc != 0:
+            raise G.AdgError(f"{what} failed (status {rc})")
+
+    def level_cells():
+        return [s.level_cells(l) for l in range(s.num_levels())]
+
+    def new_hosts(cells):
+        hs = [G.PinnedArray((n, Q, Nps)) for n in cells]
+        for l, h in enumerate(hs):
+            h.array[:] = s.get_U_w(l)
+        return hs, [h.array.ctypes.data for h in hs]
+
+    cells = level_cells()
+    hosts, ptrs = new_hosts(cells)
     h2d = d2h = 0
     t0 = time.perf_counter()
     d_before, _ = s.dof_updates()
     for _ in range(e2e_steps):
-        if s.num_levels() != len(hosts) or any(s.level_cells(l) != hosts[l].array.shape[0] for l in range(len(hosts))):
+        if cells != [h.array.shape[0] for h in hosts]:  # a regrid changed the layout
             for h in hosts:
                 h.free()
-            hosts = [G.PinnedArray((s.level_cells(l), Q, Nps)) for l in range(s.num_levels())]
-            for l in range(len(hosts)):
-                hosts[l].array[:] = s.get_U_w(l)
-        for l in range(len(hosts)):
-            s.set_U_w_async(hosts[l], l)
+            hosts, ptrs = new_hosts(cells)
+        for l, p in enumerate(ptrs):
+            check(L.adg_set_state(ctx, l, p, G.ADG_MEM_HOST_ASYNC), "adg_set_state")
             h2d += hosts[l].array.nbytes
-        s.advance(1, use_graph=True)
-        for l in range(s.num_levels()):
-            if l < len(hosts) and hosts[l].array.shape[0] == s.level_cells(l):
-                s.get_U_w_async(hosts[l], l)
+        check(L.adg_advance(ctx, 1, 1), "adg_advance")
+        cells = level_cells()
+        for l, p in enumerate(ptrs):
+            if l < len(cells) and hosts[l].array.shape[0] == cells[l]:
+                check(L.adg_get_state(ctx, l, p, G.ADG_MEM_HOST_ASYNC), "adg_get_state")
                 d2h += hosts[l].array.nbytes
-        s.synchronize()
+        check(L.adg_synchronize(ctx), "adg_synchronize")
     e2e_s = barrier_max(time.perf_counter() - t0)
     d_after, _ = s.dof_updates()
     e2e_val = (d_after - d_before) * world / e2e_s
