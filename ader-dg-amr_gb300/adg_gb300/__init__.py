@@ -122,6 +122,10 @@ def lib():
         "adg_tags": ([vp, i, ctypes.POINTER(ctypes.c_uint8)], i),
         "adg_get_step": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
         "adg_synchronize": ([vp], i),
+        "adg_interp_scatter": ([vp, vp, vp, ctypes.c_int64, vp, i], i),
+        "adg_interp_gather": ([vp, vp, ctypes.c_int64, vp, i], i),
+        "adg_average_down": ([vp], i),
+        "adg_fill_ghosts": ([vp], i),
         "adg_write_plotfile": ([vp, ctypes.c_char_p, i, i, ctypes.POINTER(ctypes.c_char_p)], i),
         "adg_read_plotfile": ([vp, ctypes.c_char_p, i, dp], i),
         "adg_plotfile_info": ([ctypes.c_char_p, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i), dp,
@@ -419,6 +423,34 @@ class AmrDG:
         assert pinned.array.shape == (self.level_cells(lev), self.Q, self.Np_s)
         self._check(self._L.adg_set_state(self.ctx, lev, pinned.array.ctypes.data, ADG_MEM_HOST_ASYNC),
                     "adg_set_state")
+
+    # ------------------------------------------------------------ L2ProjInterp
+    def amr_scatter(self, coarse, child):
+        """L2ProjInterp::amr_scatter on a batch: coarse [n, Q, Np_s], child [n]
+        (bit D-1-d: upper half in direction d) -> fine [n, Q, Np_s]."""
+        c = np.ascontiguousarray(coarse, dtype=np.float64).reshape(-1, self.Q, self.Np_s)
+        ch = np.ascontiguousarray(child, dtype=np.int8)
+        assert ch.shape == (c.shape[0],)
+        out = np.empty_like(c)
+        self._check(self._L.adg_interp_scatter(self.ctx, c.ctypes.data, ch.ctypes.data, c.shape[0],
+                                               out.ctypes.data, ADG_MEM_HOST), "adg_interp_scatter")
+        return out
+
+    def amr_gather(self, fine):
+        """L2ProjInterp::amr_gather on a batch: fine [n, 2^D, Q, Np_s] -> coarse [n, Q, Np_s]."""
+        f = np.ascontiguousarray(fine, dtype=np.float64).reshape(-1, 1 << self.D, self.Q, self.Np_s)
+        out = np.empty((f.shape[0], self.Q, self.Np_s))
+        self._check(self._L.adg_interp_gather(self.ctx, f.ctypes.data, f.shape[0], out.ctypes.data, ADG_MEM_HOST),
+                    "adg_interp_gather")
+        return out
+
+    def average_down(self):
+        """Solver::AMR_average_fine_coarse on the context's layout."""
+        self._check(self._L.adg_average_down(self.ctx), "adg_average_down")
+
+    def fill_ghosts(self):
+        """The coarse-interpolated ghost cells of FillPatchTwoLevels on the context's layout."""
+        self._check(self._L.adg_fill_ghosts(self.ctx), "adg_fill_ghosts")
 
     def synchronize(self):
         self._check(self._L.adg_synchronize(self.ctx), "adg_synchronize")

@@ -158,6 +158,8 @@ struct adg_ctx {
   DevBuf<double> ubar_old;   // [elem][q] cell means at the start of the step (TVB limiter)
   DevBuf<unsigned long long> limited;  // elements the limiter modified
   DevBuf<double> Uw_alt;   // regrid target state (swapped with Uw)
+  DevBuf<double> xfer_in, xfer_out;  // host batches of adg_interp_scatter / adg_interp_gather
+  DevBuf<int8_t> xfer_child;
   TableView<int> remap_i;     // regrid remap entries: dst | parent | src_old
   TableView<int8_t> remap_c;  // regrid remap child indices
   double rg_phase_ms[6] = {0, 0, 0, 0, 0, 0};  // regrid host time by phase
@@ -204,6 +206,7 @@ struct adg_ctx {
     sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); hseed_f.release(); fb_list.release(); fb_count.release();
     fb_total.release(); Uw_alt.release(); remap_i.release(); remap_c.release(); l2_flush.release();
     ubar_old.release(); limited.release();
+    xfer_in.release(); xfer_out.release(); xfer_child.release();
     if (tab_ev) cudaEventSynchronize(tab_ev), cudaEventDestroy(tab_ev);
     if (tag_ev) cudaEventSynchronize(tag_ev), cudaEventDestroy(tag_ev);
     if (tags_host) cudaFreeHost(tags_host);
@@ -1421,6 +1424,80 @@ int adg_tags(adg_ctx* ctx, int lev, uint8_t* out) {
   ctx->launches++;
   ADG_CUDA(cudaMemcpyAsync(out, ctx->tags.p, ta.n, cudaMemcpyDeviceToHost, ctx->stream), "tags d2h");
   ADG_CUDA(cudaStreamSynchronize(ctx->stream), "tags sync");
+  return ADG_OK;
+}
+
+// L2ProjInterp::amr_scatter on a caller batch (AmrDG_Interpolater.tpp:344-364).
+int adg_interp_scatter(adg_ctx* ctx, const double* coarse, const int8_t* child, int64_t n, double* fine, int mem) {
+  if (!ctx) return ADG_ERR_ARG;
+  if (n < 0 || (n > 0 && (!coarse || !child || !fine)) || (mem != ADG_MEM_HOST && mem != ADG_MEM_DEVICE))
+    return fail(ctx, ADG_ERR_ARG, "bad interpolation arguments");
+  if (n == 0) return ADG_OK;
+  const KernelSet* ks = ctx->ks;
+  const size_t cnt = (size_t)n * ks->Q * ks->Np_s;
+  cudaError_t e;
+  if (mem == ADG_MEM_HOST) {
+    for (int64_t i = 0; i < n; ++i)
+      if (child[i] < 0 || child[i] >= (1 << ctx->cfg.D)) return fail(ctx, ADG_ERR_ARG, "child index out of range");
+    ADG_CUDA(ctx->xfer_in.ensure(cnt), "alloc");
+    ADG_CUDA(ctx->xfer_out.ensure(cnt), "alloc");
+    ADG_CUDA(ctx->xfer_child.ensure((size_t)n), "alloc");
+    ADG_CUDA(cudaMemcpyAsync(ctx->xfer_in.p, coarse, cnt * 8, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    ADG_CUDA(cudaMemcpyAsync(ctx->xfer_child.p, child, (size_t)n, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    e = ks->interp_scatter(ctx->xfer_in.p, ctx->xfer_child.p, n, ctx->xfer_out.p, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scatter launch");
+    ADG_CUDA(cudaMemcpyAsync(fine, ctx->xfer_out.p, cnt * 8, cudaMemcpyDeviceToHost, ctx->stream), "d2h");
+  } else {
+    e = ks->interp_scatter(coarse, child, n, fine, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scatter launch");
+  }
+  ctx->launches++;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "scatter sync");
+  return ADG_OK;
+}
+
+// L2ProjInterp::amr_gather on a caller batch (AmrDG_Interpolater.tpp:366-398).
+int adg_interp_gather(adg_ctx* ctx, const double* fine, int64_t n, double* coarse, int mem) {
+  if (!ctx) return ADG_ERR_ARG;
+  if (n < 0 || (n > 0 && (!coarse || !fine)) || (mem != ADG_MEM_HOST && mem != ADG_MEM_DEVICE))
+    return fail(ctx, ADG_ERR_ARG, "bad interpolation arguments");
+  if (n == 0) return ADG_OK;
+  const KernelSet* ks = ctx->ks;
+  const size_t cnt = (size_t)n * ks->Q * ks->Np_s, cnt_f = cnt << ctx->cfg.D;
+  cudaError_t e;
+  if (mem == ADG_MEM_HOST) {
+    ADG_CUDA(ctx->xfer_in.ensure(cnt_f), "alloc");
+    ADG_CUDA(ctx->xfer_out.ensure(cnt), "alloc");
+    ADG_CUDA(cudaMemcpyAsync(ctx->xfer_in.p, fine, cnt_f * 8, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+    e = ks->interp_gather(ctx->xfer_in.p, n, ctx->xfer_out.p, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "gather launch");
+    ADG_CUDA(cudaMemcpyAsync(coarse, ctx->xfer_out.p, cnt * 8, cudaMemcpyDeviceToHost, ctx->stream), "d2h");
+  } else {
+    e = ks->interp_gather(fine, n, coarse, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "gather launch");
+  }
+  ctx->launches++;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "gather sync");
+  return ADG_OK;
+}
+
+int adg_average_down(adg_ctx* ctx) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  rc = launch_average_down(ctx);
+  if (rc) return rc;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "average down sync");
+  return ADG_OK;
+}
+
+int adg_fill_ghosts(adg_ctx* ctx) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (ctx->hier.nlevels() > 1) {
+    rc = launch_ghost_fill(ctx);
+    if (rc) return rc;
+  }
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "ghost fill sync");
   return ADG_OK;
 }
 

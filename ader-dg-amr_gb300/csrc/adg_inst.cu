@@ -111,6 +111,19 @@ struct Impl final : KernelSet {
     k_scatter<O><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
     return cudaGetLastError();
   }
+  cudaError_t interp_scatter(const double* coarse, const int8_t* child, long long n, double* fine,
+                             cudaStream_t s) const override {
+    if (n <= 0) return cudaSuccess;
+    const long long t = n * O::Q;
+    k_interp_scatter<O><<<(unsigned)((t + 127) / 128), 128, 0, s>>>(coarse, child, n, fine);
+    return cudaGetLastError();
+  }
+  cudaError_t interp_gather(const double* fine, long long n, double* coarse, cudaStream_t s) const override {
+    if (n <= 0) return cudaSuccess;
+    const long long t = n * O::Q;
+    k_interp_gather<O><<<(unsigned)((t + 127) / 128), 128, 0, s>>>(fine, n, coarse);
+    return cudaGetLastError();
+  }
   cudaError_t tag(const TagArgs& a, cudaStream_t s) const override {
     if (a.n == 0) return cudaSuccess;
     k_tag<O><<<(a.n + 127) / 128, 128, 0, s>>>(a);

@@ -1181,6 +1181,62 @@ __global__ void k_average_down(double* Uw, const int* rec, int nrec) {
   }
 }
 
+// L2ProjInterp on caller batches (AmrDG_Interpolater.tpp:344-398): thread
+// per (cell, variable).  Scatter: fine[i] = Minv P_cf[child[i]] coarse[i];
+// gather: coarse[i] = 2^-D Minv sum_l P_fc[l] fine[i][l], children summed in
+// order as k_average_down does.  Layouts [n][Q][Np_s] and [n][2^D][Q][Np_s].
+template <class O>
+__global__ void k_interp_scatter(const double* coarse, const int8_t* child, long long n, double* fine) {
+  constexpr int Q = O::Q, NP_S = O::NP_S;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * Q) return;
+  const long long i = t / Q;
+  const int q = (int)(t % Q);
+  double out[NP_S];
+  const int l = child[i];
+#pragma unroll
+  for (int k = 0; k < NP_S; ++k) out[k] = __longlong_as_double(0x7ff8000000000000LL);  // NaN: child out of range
+  if (l >= 0 && l < (1 << O::D)) pcf_rt<O>(l, RegIn{coarse + (size_t)t * NP_S}, RegOut{out});
+#pragma unroll
+  for (int k = 0; k < NP_S; ++k) fine[(size_t)t * NP_S + k] = out[k];
+}
+
+template <class O>
+__global__ void k_interp_gather(const double* fine, long long n, double* coarse) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NOV = 1 << D;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * Q) return;
+  const long long i = t / Q;
+  const int q = (int)(t % Q);
+  double part[NOV][NP_S];
+#pragma unroll
+  for (int l = 0; l < NOV; ++l) {
+    const double* uf = fine + (((size_t)i * NOV + l) * Q + q) * NP_S;
+    switch (l) {
+      case 0: O::template pfc<0>(RegIn{uf}, RegOut{part[l]}); break;
+      case 1: O::template pfc<1>(RegIn{uf}, RegOut{part[l]}); break;
+      case 2: O::template pfc<2>(RegIn{uf}, RegOut{part[l]}); break;
+      case 3: O::template pfc<3>(RegIn{uf}, RegOut{part[l]}); break;
+      default:
+        if constexpr (D == 3) {
+          switch (l) {
+            case 4: O::template pfc<4>(RegIn{uf}, RegOut{part[l]}); break;
+            case 5: O::template pfc<5>(RegIn{uf}, RegOut{part[l]}); break;
+            case 6: O::template pfc<6>(RegIn{uf}, RegOut{part[l]}); break;
+            default: O::template pfc<7>(RegIn{uf}, RegOut{part[l]}); break;
+          }
+        }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NP_S; ++k) {
+    double sum = 0.0;
+#pragma unroll
+    for (int l = 0; l < NOV; ++l) sum += part[l][k];
+    coarse[(size_t)t * NP_S + k] = (1.0 / NOV) * (O::minv(k) * sum);
+  }
+}
+
 // Coarse -> fine projection (amr_scatter, AmrDG_Interpolater.tpp:344-364)
 // into ghost elements (FillPatchTwoLevels) or, with src_old, the regrid
 // remap of a level (valid data of the old layout where it existed).

@@ -26,6 +26,9 @@ struct KernelSet {
   virtual cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t average_down(double* Uw, const int* rec, int nrec, cudaStream_t s) const = 0;
   virtual cudaError_t scatter(const ScatterArgs& a, cudaStream_t s) const = 0;
+  virtual cudaError_t interp_scatter(const double* coarse, const int8_t* child, long long n, double* fine,
+                                     cudaStream_t s) const = 0;
+  virtual cudaError_t interp_gather(const double* fine, long long n, double* coarse, cudaStream_t s) const = 0;
   virtual cudaError_t tag(const TagArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t seed_features(const SeedFeatArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t seed_targets(const SeedFeatArgs& a, cudaStream_t s) const = 0;

@@ -168,6 +168,26 @@ int adg_set_layout(adg_ctx* ctx, int nlev, const int* nbox, const int* boxes);
 int adg_level_cell_coords(const adg_ctx* ctx, int lev, int* ijk);
 int adg_tags(adg_ctx* ctx, int lev, uint8_t* out);
 
+/* L2ProjInterp transfer operators (AmrDG_Interpolater.tpp:283-398) for a caller
+ * that keeps its own FillPatch / average-down machinery and wants the
+ * projections on the GPU.  mem: ADG_MEM_HOST or ADG_MEM_DEVICE for every array.
+ * adg_interp_scatter (amr_scatter): fine[i] = Minv P_cf[child[i]] coarse[i] for
+ * i < n; coarse and fine [n][Q][Np_s]; child[i] in [0, 2^D), bit (D-1-d) set
+ * for the upper half in direction d (host children out of range: ADG_ERR_ARG;
+ * device ones give NaN).
+ * adg_interp_gather (amr_gather): coarse[i] = 2^-D Minv sum_l P_fc[l] fine[i][l];
+ * fine [n][2^D][Q][Np_s] with children numbered as above, coarse [n][Q][Np_s].
+ * adg_average_down (Solver::AMR_average_fine_coarse): every covered cell of
+ * the context's layout from its children, finest level first.
+ * adg_fill_ghosts (the coarse-interpolated part of FillPatchTwoLevels): the
+ * context's coarse-fine ghost elements from their coarse parents.
+ * The coarse-fine flux correction (FluxRegister + L2ProjInterp::reflux) has no
+ * entry point of its own: it is part of adg_ader's corrector. */
+int adg_interp_scatter(adg_ctx* ctx, const double* coarse, const int8_t* child, int64_t n, double* fine, int mem);
+int adg_interp_gather(adg_ctx* ctx, const double* fine, int64_t n, double* coarse, int mem);
+int adg_average_down(adg_ctx* ctx);
+int adg_fill_ghosts(adg_ctx* ctx);
+
 /* Completed steps of the evolve loop (the reference's n, AmrDG.h:868-877,
  * 1012); a restart from a plotfile continues its count. */
 int adg_get_step(const adg_ctx* ctx, int64_t* n);
