@@ -16,7 +16,6 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "adg_async.cuh"
 #include "adg_device.cuh"
 
 namespace adg {

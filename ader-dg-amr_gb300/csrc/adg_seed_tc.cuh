@@ -17,8 +17,9 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "adg_kernels.cuh"
+#include "adg_async.cuh"
 #include "adg_gelu.cuh"
+#include "adg_kernels.cuh"
 
 namespace adg {
 namespace tc {
