@@ -110,6 +110,96 @@ __device__ __forceinline__ double euler_flux_normal(int d, const double* u, doub
   return fabs(vd) + c;
 }
 
+// Change of the physical flux F(u + du) - F(u) between a state u and a nearby
+// state u + du, in FP32, written with the algebraic differences of its terms
+// (v' - v = (dm - v drho) / rho', m'.v' - m.v = m.dv + dm.v', ...) so that no
+// two rounded fluxes are subtracted: the rounding error is relative to the
+// change, not to the flux.  The pressure floor of euler_flux_all applies to
+// both states (the change of the floored pressure).
+struct DeltaState {
+  float v1[3], dv[3];  // velocity of u + du, its change
+  float p, dp;         // floored pressure of u, change of the floored pressure
+};
+
+template <int D>
+__device__ __forceinline__ DeltaState euler_delta_state(const float* u, const float* du, float gm1) {
+  DeltaState s;
+  const float r = __frcp_rn(u[0]);
+  const float r1 = __frcp_rn(u[0] + du[0]);
+  float ke = 0.0f, dke = 0.0f;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const float v = u[d + 1] * r;
+    s.dv[d] = fmaf(-v, du[0], du[d + 1]) * r1;
+    s.v1[d] = v + s.dv[d];
+    ke = fmaf(u[d + 1], v, ke);
+    dke = fmaf(du[d + 1], s.v1[d], fmaf(u[d + 1], s.dv[d], dke));
+  }
+  const float L = (float)kPdeLimit;
+  const float p = gm1 * fmaf(-0.5f, ke, u[D + 1]);
+  const float dp = gm1 * fmaf(-0.5f, dke, du[D + 1]);
+  const float p1 = p + dp;
+  if (p < L || p1 < L) {
+    const float pf = p < L ? L : p;
+    const float pf1 = p1 < L ? L : p1;
+    s.p = pf;
+    s.dp = pf1 - pf;
+  } else {
+    s.p = p;
+    s.dp = dp;
+  }
+  return s;
+}
+
+// Change of the flux in every direction; dF[d*Q + q].
+template <int D>
+__device__ __forceinline__ void euler_dflux_all(const float* u, const float* du, float gm1, float* dF) {
+  constexpr int Q = D + 2;
+  const DeltaState s = euler_delta_state<D>(u, du, gm1);
+  const float ep = u[D + 1] + s.p, dep = du[D + 1] + s.dp;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    dF[d * Q] = du[d + 1];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      const float t = fmaf(du[k + 1], s.v1[d], u[k + 1] * s.dv[d]);
+      dF[d * Q + k + 1] = k == d ? t + s.dp : t;
+    }
+    dF[d * Q + D + 1] = fmaf(dep, s.v1[d], ep * s.dv[d]);
+  }
+}
+
+// Change of the normal flux in direction d, and the LLF wave-speed bound of
+// the state u + du (as euler_flux_normal, in FP32).
+template <int D>
+__device__ __forceinline__ float euler_dflux_normal(int d, const float* u, const float* du, float gm1, float gamma,
+                                                    float* dF) {
+  const DeltaState s = euler_delta_state<D>(u, du, gm1);
+  float v1d = s.v1[0], dvd = s.dv[0];
+#pragma unroll
+  for (int k = 1; k < D; ++k)
+    if (k == d) {
+      v1d = s.v1[k];
+      dvd = s.dv[k];
+    }
+  float dmd = du[1];
+#pragma unroll
+  for (int k = 1; k < D; ++k)
+    if (k == d) dmd = du[k + 1];
+  dF[0] = dmd;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const float t = fmaf(du[k + 1], v1d, u[k + 1] * dvd);
+    dF[k + 1] = k == d ? t + s.dp : t;
+  }
+  dF[D + 1] = fmaf(du[D + 1] + s.dp, v1d, (u[D + 1] + s.p) * dvd);
+  const float rho1 = u[0] + du[0];
+  const float L = (float)kPdeLimit;
+  const float rinv_c = rho1 < L ? 1.0f / L : __frcp_rn(rho1);
+  const float c = sqrtf(gamma * ((s.p + s.dp) * rinv_c));
+  return fabsf(v1d) + c;
+}
+
 // CFL speed max_d(|u_d/rho| + c) at one point (Compressible_Euler.cpp:57-70).
 template <int D>
 __device__ __forceinline__ double euler_cfl_lambda(const double* u, double gamma) {

@@ -14,13 +14,15 @@ using O = ADG_NS::Ops;
 //   FP32 sweeps (MODE 2)    D NQ_ST ld floats
 //   final volume slices     (1 + D) NQ_S ld doubles
 //   face traces             2 NQ_BD ld doubles   (one direction at a time)
+//   MODE 2 final stage      split_epilogue_doubles (volume and face phases)
 //   seed residual           2 E Q doubles
 template <int E, int MODE>
 constexpr size_t smem_bytes() {
   constexpr size_t ld = E * O::Q + 1;
   constexpr size_t sweeps = MODE == 2 ? O::D * O::NQ_ST * ld * sizeof(float) : O::D * O::NQ_ST * ld * sizeof(double);
-  constexpr size_t fin = (1 + O::D) * O::NQ_S * ld * sizeof(double);
-  constexpr size_t faces = 2 * O::NQ_BD * ld * sizeof(double);
+  constexpr size_t fin = MODE == 2 ? split_epilogue_doubles<O>(ld) * sizeof(double)
+                                   : (1 + O::D) * O::NQ_S * ld * sizeof(double);
+  constexpr size_t faces = MODE == 2 ? 0 : 2 * O::NQ_BD * ld * sizeof(double);
   constexpr size_t red = 2 * E * O::Q * sizeof(double);
   constexpr size_t m1 = sweeps > fin ? sweeps : fin;
   constexpr size_t m2 = faces > red ? faces : red;

@@ -254,6 +254,272 @@ __device__ __forceinline__ void face_traces(const double* hw, double* sm, int co
   __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
+// Final stage of the seeded FP32 path.  W U is U constant in time, so the
+// final H_w = W U + dlt is H(x, t) = U(x) + delta(x, t) with delta the
+// expansion of dlt, the FP32 sweeps' change.  FP64 work is kept to the
+// time-independent part: U and F(U) at the NS spatial points (whose volume
+// term is taken once, times the sum of the time weights) and at the NSB
+// spatial points of every face.  The time-dependent part is the FP32 change
+// of the flux F(U + delta) - F(U) (euler_dflux_*), whose rounding is
+// relative to the change; it is added to the FP64 part in modal space (the
+// volume term) or point by point (the traces).  The outputs are those of
+// final_volume_flux + face_traces: Rvol and the trace tiles of H, F_n, the
+// wave speed.
+// ---------------------------------------------------------------------------
+
+// Shared memory of split_epilogue (doubles): region A = (1 + D) NS ld doubles
+// (U and F(U) at the spatial points, later the FP32 delta slice and flux
+// change sums, later the face buffers), then NS ld floats of U in FP32.
+template <class O>
+constexpr size_t split_epilogue_doubles(size_t ld) {
+  constexpr size_t NS = O::NQ_S, NB = O::NQ_BD, NSB = NB / O::N;
+  const size_t vol = (1 + O::D) * NS * ld + (NS * ld + 1) / 2;
+  const size_t faces = (4 * NSB + (2 * NSB + 2 * NB + 1) / 2) * ld;
+  return vol > faces ? vol : faces;
+}
+
+// Time slice K: delta at the spatial points of time node K (column), then the
+// flux changes at those points accumulated with the time weights (points).
+template <class O, int E, int K>
+__device__ __forceinline__ void delta_slices(const float* dlt, const float* us32, float* ds32, float* fb32, int col,
+                                             float gm1f) {
+  constexpr int D = O::D, Q = O::Q, NS = O::NQ_S, LD = E * Q + 1;
+  O::template vol_eval_slice<K, float>(RegInT<float>{dlt}, ColOutT<float>{ds32 + col, LD});
+  __syncthreads();
+  const float w = O::weight_f(K);
+#pragma unroll 2
+  for (int it = threadIdx.x; it < E * NS; it += blockDim.x) {
+    const int m = it % NS;
+    const int ee = it / NS;
+    float uu[Q], du[Q], dF[D * Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      uu[k] = us32[m * LD + ee * Q + k];
+      du[k] = ds32[m * LD + ee * Q + k];
+    }
+    euler_dflux_all<D>(uu, du, gm1f, dF);
+    float* f = fb32 + m * LD + ee * Q;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        float& dst = f[d * NS * LD + k];
+        dst = K == 0 ? w * dF[d * Q + k] : fmaf(w, dF[d * Q + k], dst);
+      }
+  }
+  __syncthreads();
+  if constexpr (K + 1 < O::N) delta_slices<O, E, K + 1>(dlt, us32, ds32, fb32, col, gm1f);
+}
+
+// Column part of one face side: U at the face's spatial points (FP64), delta
+// at its space-time points (FP32), both to shared memory, and the trace of
+// H = U + delta to the element's tile.
+template <class O, int E, int DIR, int S>
+__device__ __forceinline__ void split_face_column(const double* u, const float* dlt, double* uface64, float* uf32,
+                                                  float* dface32, int col, int q, double* tr_elem) {
+  constexpr int N = O::N, NB = O::NQ_BD, NSB = NB / N, LD = E * O::Q + 1, TT = tr_tile<O>();
+  double uf[NSB];
+  float df[NB];
+  O::template face_eval_sp<DIR, S>(RegIn{u}, RegOut{uf});
+  O::template face_eval<DIR, S, float>(RegInT<float>{dlt}, RegOutT<float>{df});  // point x N + t
+#pragma unroll
+  for (int x = 0; x < NSB; ++x) {
+    uface64[(S * NSB + x) * LD + col] = uf[x];
+    uf32[(S * NSB + x) * LD + col] = (float)uf[x];
+  }
+  double* t = tr_elem ? tr_elem + (2 * DIR + S) * TT + q * NB : nullptr;
+#pragma unroll
+  for (int tt = 0; tt < N; ++tt)
+#pragma unroll
+    for (int x = 0; x < NSB; ++x) {
+      const int p = tt * NSB + x;  // tile position
+      const float d = df[x * N + tt];
+      dface32[(S * NB + p) * LD + col] = d;
+      if (t) t[p] = uf[x] + (double)d;
+    }
+}
+
+// The two faces of direction DIR: H traces (columns), F_n(U) at the faces'
+// spatial points (FP64, points), then per space-time face point the flux
+// change and the wave speed (FP32), F_n = F_n(U) + change, to the tiles.
+template <class O, int E, int DIR>
+__device__ __forceinline__ void split_faces(const double* u, const float* dlt, double* sm, int col, int q,
+                                            double* tr_elem, const PredictorArgs& a, int e0, int limit) {
+  constexpr int D = O::D, Q = O::Q, N = O::N, NB = O::NQ_BD, NSB = NB / N, NF = 2 * D, TT = tr_tile<O>();
+  constexpr int LD = E * Q + 1;
+  double* uface64 = sm;                                         // [side][x][col]
+  double* fun64 = sm + 2 * NSB * LD;                            // [side][x][col]
+  float* uf32 = reinterpret_cast<float*>(sm + 4 * NSB * LD);    // [side][x][col]
+  float* dface32 = uf32 + 2 * NSB * LD;                         // [side][t NSB + x][col]
+  split_face_column<O, E, DIR, 0>(u, dlt, uface64, uf32, dface32, col, q, tr_elem);
+  split_face_column<O, E, DIR, 1>(u, dlt, uface64, uf32, dface32, col, q, tr_elem);
+  __syncthreads();
+  for (int it = threadIdx.x; it < E * 2 * NSB; it += blockDim.x) {
+    const int x = it % NSB;
+    const int s = (it / NSB) & 1;
+    const int ee = it / (2 * NSB);
+    const double* b = uface64 + (s * NSB + x) * LD + ee * Q;
+    double uu[Q], F[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) uu[k] = b[k];
+    (void)euler_flux_normal<D>(DIR, uu, a.gamma, F);
+    double* f = fun64 + (s * NSB + x) * LD + ee * Q;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[k] = F[k];
+  }
+  __syncthreads();
+  const float gm1f = (float)(a.gamma - 1.0), gf = (float)a.gamma;
+#pragma unroll 2
+  for (int it = threadIdx.x; it < E * 2 * NB; it += blockDim.x) {
+    const int p = it % NB;
+    const int s = (it / NB) & 1;
+    const int ee = it / (2 * NB);
+    if (e0 + ee >= limit) continue;
+    const int elem = a.elem_list ? a.elem_list[e0 + ee] : e0 + ee;
+    const int x = p % NSB;
+    float uu[Q], du[Q], dF[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      uu[k] = uf32[(s * NSB + x) * LD + ee * Q + k];
+      du[k] = dface32[(s * NB + p) * LD + ee * Q + k];
+    }
+    const float ws = euler_dflux_normal<D>(DIR, uu, du, gm1f, gf, dF);
+    const double* f = fun64 + (s * NSB + x) * LD + ee * Q;
+    double* t = a.Tr + ((size_t)elem * NF + 2 * DIR + s) * TT + p;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) t[(Q + k) * NB] = f[k] + (double)dF[k];
+    t[2 * Q * NB] = (double)ws;
+  }
+  __syncthreads();
+}
+
+template <class O, int E>
+__device__ __forceinline__ void split_epilogue(const double* u, const float* dlt, const double* c, double gm1,
+                                               double* sm, int col, int q, bool live, int e, const PredictorArgs& a) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NS = O::NQ_S, NF = 2 * D;
+  constexpr int LD = E * Q + 1;
+  double* us64 = sm;
+  double* fU64 = sm + NS * LD;
+  float* us32 = reinterpret_cast<float*>(sm + (1 + D) * NS * LD);
+
+  // U at the spatial points (FP64, and in FP32 for the flux changes)
+  O::sp_eval(RegIn{u}, ColOut{us64 + col, LD});
+#pragma unroll
+  for (int m = 0; m < NS; ++m) us32[m * LD + col] = (float)us64[m * LD + col];
+  __syncthreads();
+  // F(U) at the spatial points (FP64)
+#pragma unroll 2
+  for (int it = threadIdx.x; it < E * NS; it += blockDim.x) {
+    const int m = it % NS;
+    const int ee = it / NS;
+    const double* b = us64 + m * LD + ee * Q;
+    double uu[Q], F[D * Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) uu[k] = b[k];
+    euler_flux_all<D, double>(uu, gm1, F);
+    double* f = fU64 + m * LD + ee * Q;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+#pragma unroll
+      for (int k = 0; k < Q; ++k) f[d * NS * LD + k] = F[d * Q + k];
+  }
+  __syncthreads();
+  // volume term of the time-constant part (AmrDG.tpp:696-709 with F = F(U)):
+  // M U + sum_d c_d (sum_k w_k) Sk_d F_d(U)
+  double R[NP_S], v[NP_S];
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) R[n] = O::mdiag(n) * u[n];
+  O::template vol_term_sp<0>(ColIn{fU64 + col, LD}, RegOut{v});
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) R[n] = fma(c[0] * O::WEIGHT_SUM, v[n], R[n]);
+  O::template vol_term_sp<1>(ColIn{fU64 + NS * LD + col, LD}, RegOut{v});
+#pragma unroll
+  for (int n = 0; n < NP_S; ++n) R[n] = fma(c[1] * O::WEIGHT_SUM, v[n], R[n]);
+  if constexpr (D == 3) {
+    O::template vol_term_sp<2>(ColIn{fU64 + 2 * NS * LD + col, LD}, RegOut{v});
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[2] * O::WEIGHT_SUM, v[n], R[n]);
+  }
+  __syncthreads();
+  // time-dependent part: the time integrals of the flux changes (FP32)
+  float* ds32 = reinterpret_cast<float*>(sm);
+  float* fb32 = ds32 + NS * LD;
+  delta_slices<O, E, 0>(dlt, us32, ds32, fb32, col, (float)gm1);
+  {
+    float w[NP_S];
+    O::template vol_term_sp<0, float>(ColInT<float>{fb32 + col, LD}, RegOutT<float>{w});
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[0], (double)w[n], R[n]);
+    O::template vol_term_sp<1, float>(ColInT<float>{fb32 + NS * LD + col, LD}, RegOutT<float>{w});
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[1], (double)w[n], R[n]);
+    if constexpr (D == 3) {
+      O::template vol_term_sp<2, float>(ColInT<float>{fb32 + 2 * NS * LD + col, LD}, RegOutT<float>{w});
+#pragma unroll
+      for (int n = 0; n < NP_S; ++n) R[n] = fma(c[2], (double)w[n], R[n]);
+    }
+  }
+  if (live) {
+    double* dst = a.Rvol + ((size_t)e * Q + q) * NP_S;
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) dst[n] = R[n];
+  }
+  __syncthreads();
+  // face traces, one direction at a time
+  const int e0 = blockIdx.x * E;
+  const int limit = a.elem_list ? *a.list_count : a.n_elem;
+  double* tr_elem = live ? a.Tr + (size_t)e * NF * tr_tile<O>() : nullptr;
+  split_faces<O, E, 0>(u, dlt, sm, col, q, tr_elem, a, e0, limit);
+  split_faces<O, E, 1>(u, dlt, sm, col, q, tr_elem, a, e0, limit);
+  if constexpr (D == 3) split_faces<O, E, 2>(u, dlt, sm, col, q, tr_elem, a, e0, limit);
+}
+
+// Final stage of the FP64 paths: the corrector volume term and the face
+// traces of the final H_w.
+template <class O, int E>
+__device__ __forceinline__ void fp64_epilogue(const double* hw, const double* u, const double* c, double gm1,
+                                              double* sm, int col, int q, bool live, int e, const PredictorArgs& a) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NS = O::NQ_S;
+  constexpr int LD = E * Q + 1;
+  // ---- corrector volume term (AmrDG.tpp:696-709): M U + sum_d c_d Sk_corr[d] F_d,
+  // one time slice of points at a time (the slice's H, then its fluxes
+  // accumulated into the time integral of F_d at the spatial points)
+  {
+    double* fbar = sm + NS * LD;
+    final_volume_flux<O, E, 0>(hw, sm, fbar, col, LD, gm1,
+                               live ? a.Tr + (size_t)e * 2 * D * tr_tile<O>() : nullptr, q);
+    double R[NP_S], v[NP_S];
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) R[n] = O::mdiag(n) * u[n];
+    O::template vol_term_sp<0>(ColIn{fbar + col, LD}, RegOut{v});
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[0], v[n], R[n]);
+    O::template vol_term_sp<1>(ColIn{fbar + NS * LD + col, LD}, RegOut{v});
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[1], v[n], R[n]);
+    if constexpr (D == 3) {
+      O::template vol_term_sp<2>(ColIn{fbar + 2 * NS * LD + col, LD}, RegOut{v});
+#pragma unroll
+      for (int n = 0; n < NP_S; ++n) R[n] = fma(c[2], v[n], R[n]);
+    }
+    if (live) {
+      double* dst = a.Rvol + ((size_t)e * Q + q) * NP_S;
+#pragma unroll
+      for (int n = 0; n < NP_S; ++n) dst[n] = R[n];
+    }
+  }
+  __syncthreads();
+
+  // ---- face traces of H (AmrDG.tpp:437-493) and face physics (AmrDG.h:1207-1251),
+  // the two faces of one direction at a time
+  const int e0 = blockIdx.x * E;
+  const int limit = a.elem_list ? *a.list_count : a.n_elem;
+  face_traces<O, E, 0>(hw, sm, col, LD, a, e0, limit);
+  face_traces<O, E, 1>(hw, sm, col, LD, a, e0, limit);
+  if constexpr (D == 3) face_traces<O, E, 2>(hw, sm, col, LD, a, e0, limit);
+}
+
 // MODE 0: plain FP64 Picard (the reference's initial guess, P sweeps);
 // MODE 1 / 2: seeded, `sweeps` sweeps from the learned seed in FP64 / FP32,
 // the first one judging the seed by its residual.
@@ -293,6 +559,7 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   double wu[NP_ST];
   O::wu(RegIn{u}, RegOut{wu});
   double hw[NP_ST];
+  float dlt[NP_ST];  // MODE 2: H_w - W U from the FP32 sweeps
 
   if constexpr (MODE == 0) {
     // ---- sweep 1: the reference's initial guess H_w = [U_w, 0, ...]
@@ -361,8 +628,8 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
         for (int n = 0; n < NP_ST; ++n) hw[n] = nw[n];
       }
     } else {
-      // FP32 sweeps on a float copy; the final H_w = W U + dlt in FP64
-      float hf[NP_ST], wf[NP_ST], dlt[NP_ST], cf[D];
+      // FP32 sweeps on a float copy; the final H_w = W U + dlt
+      float hf[NP_ST], wf[NP_ST], cf[D];
       if (a.Hseed_f) {
 #pragma unroll
         for (int n = 0; n < NP_ST; ++n) hf[n] = a.Hseed_f[hoff + n];
@@ -384,9 +651,9 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
         }
       }
       res = (double)resf;
+      if (a.sweeps == 0)  // the seed itself (a diagnostic setting): its change from W U in FP32
 #pragma unroll
-      for (int n = 0; n < NP_ST; ++n)
-        hw[n] = a.sweeps > 0 ? wu[n] + (double)dlt[n] : (a.Hseed_f ? (double)hf[n] : a.Hseed[hoff + n]);
+        for (int n = 0; n < NP_ST; ++n) dlt[n] = hf[n] - wf[n];
     }
     // per-element reduction over its Q columns through shared memory
     double* red = sm;
@@ -410,46 +677,12 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   if (a.Hw_out && live) {
     double* dst = a.Hw_out + ((size_t)e * Q + q) * NP_ST;
 #pragma unroll
-    for (int n = 0; n < NP_ST; ++n) dst[n] = hw[n];
+    for (int n = 0; n < NP_ST; ++n) dst[n] = MODE == 2 ? wu[n] + (double)dlt[n] : hw[n];
   }
-
-  // ---- corrector volume term (AmrDG.tpp:696-709): M U + sum_d c_d Sk_corr[d] F_d,
-  // one time slice of points at a time (the slice's H, then its fluxes
-  // accumulated into the time integral of F_d at the spatial points)
-  {
-    constexpr int NS = O::NQ_S;
-    double* fbar = sm + NS * LD;
-    final_volume_flux<O, E, 0>(hw, sm, fbar, col, LD, gm1,
-                               live ? a.Tr + (size_t)e * 2 * D * tr_tile<O>() : nullptr, q);
-    double R[NP_S], v[NP_S];
-#pragma unroll
-    for (int n = 0; n < NP_S; ++n) R[n] = O::mdiag(n) * u[n];
-    O::template vol_term_sp<0>(ColIn{fbar + col, LD}, RegOut{v});
-#pragma unroll
-    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[0], v[n], R[n]);
-    O::template vol_term_sp<1>(ColIn{fbar + NS * LD + col, LD}, RegOut{v});
-#pragma unroll
-    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[1], v[n], R[n]);
-    if constexpr (D == 3) {
-      O::template vol_term_sp<2>(ColIn{fbar + 2 * NS * LD + col, LD}, RegOut{v});
-#pragma unroll
-      for (int n = 0; n < NP_S; ++n) R[n] = fma(c[2], v[n], R[n]);
-    }
-    if (live) {
-      double* dst = a.Rvol + ((size_t)e * Q + q) * NP_S;
-#pragma unroll
-      for (int n = 0; n < NP_S; ++n) dst[n] = R[n];
-    }
-  }
-  __syncthreads();
-
-  // ---- face traces of H (AmrDG.tpp:437-493) and face physics (AmrDG.h:1207-1251),
-  // the two faces of one direction at a time
-  const int e0 = blockIdx.x * E;
-  const int limit = a.elem_list ? *a.list_count : a.n_elem;
-  face_traces<O, E, 0>(hw, sm, col, LD, a, e0, limit);
-  face_traces<O, E, 1>(hw, sm, col, LD, a, e0, limit);
-  if constexpr (D == 3) face_traces<O, E, 2>(hw, sm, col, LD, a, e0, limit);
+  if constexpr (MODE == 2)
+    split_epilogue<O, E>(u, dlt, c, gm1, sm, col, q, live, e, a);
+  else
+    fp64_epilogue<O, E>(hw, u, c, gm1, sm, col, q, live, e, a);
 }
 
 // N consecutive doubles to registers (and back): 16-byte accesses when every

@@ -618,6 +618,51 @@ def build_ops(el):
             phi *= el.val[n[d]][0]
         row.append(phi)
     ops["u_pt0"] = ([Stage(el.Np_s, 1, [[(c, row[c]) for c in range(el.Np_s) if row[c] != 0.0]])], el.Np_s, 1)
+
+    # ---- sp_eval: spatial modes -> the spatial GL points (pts_s order).
+    # W U, the space-time expansion the Picard update starts from, is U
+    # constant in time (checked below), so a predictor H_w = W U + dlt is
+    # U(x) + dlt(x, t) at the space-time points: the seeded path evaluates
+    # the first term with this operator and the second one in its own
+    # precision.
+    s_keys = [tuple(('m', a) for a in n) for n in el.mi_s]
+
+    def phi_s(n, coord):  # coord: dim -> table row (val at a node, or bd at a face)
+        v = 1.0
+        for a in range(D):
+            v *= coord[a][n[a]]
+        return v
+
+    stages, keys = ch.eval_chain(list(range(D - 1, -1, -1)), s_keys, {p: el.val for p in range(D)}, D)
+    stages.append(stage_from_map(keys, sp_keys, lambda ok: [(ok, 1.0)]))
+    dense_sp = [[phi_s(n, {a: [el.val[m][pt[a]] for m in range(P + 1)] for a in range(D)}) for n in el.mi_s]
+                for pt in el.pts_s]
+    check_chain(stages, dense_sp, "sp_eval")
+    ops["sp_eval"] = (stages, el.Np_s, len(sp_keys))
+    VW = [[sum(el.V[i][k] * el.W[k][j] for k in range(el.Np_st)) for j in range(el.Np_s)]
+          for i in range(len(el.pts_st))]
+    for i, pt in enumerate(el.pts_st):
+        want = dense_sp[el.pts_s.index(tuple(pt[:D]))]
+        if max(abs(VW[i][j] - want[j]) for j in range(el.Np_s)) > 1e-12:
+            raise SystemExit("W U is not U constant in time")
+
+    # ---- face_eval_sp[d][side]: spatial modes -> the face's spatial points
+    # (free dims != d in order, face_slice's point order)
+    for d in range(D):
+        free = [a for a in range(D) if a != d]
+        free_pts = list(itertools.product(range(N), repeat=D - 1))
+        fkeys = [tuple(('q', 0) if a == d else ('q', fp[free.index(a)]) for a in range(D)) for fp in free_pts]
+        for side in range(2):
+            tabs = {p: el.val for p in range(D)}
+            tabs[d] = [[el.bd[a][side]] for a in range(P + 1)]
+            order = [d] + [p for p in range(D - 1, -1, -1) if p != d]
+            stages, keys = ch.eval_chain(order, s_keys, tabs, D)
+            stages.append(stage_from_map(keys, fkeys, lambda ok: [(ok, 1.0)]))
+            dense = [[phi_s(n, {a: ([el.bd[m][side] for m in range(P + 1)] if a == d else
+                                    [el.val[m][fp[free.index(a)]] for m in range(P + 1)]) for a in range(D)})
+                      for n in el.mi_s] for fp in free_pts]
+            check_chain(stages, dense, f"face_eval_sp{d}{side}")
+            ops[f"face_eval_sp{d}{side}"] = (stages, el.Np_s, len(free_pts))
     return ops
 
 
@@ -942,6 +987,7 @@ def generate(D, P, out_path):
         "__device__ __constant__ const double MINV_[] = {" + ", ".join(lit(v) for v in el.Minv) + "};",
         "__device__ __constant__ const double NODES_[] = {" + ", ".join(lit(v) for v in el.nodes) + "};",
         "__device__ __constant__ const double WEIGHTS_[] = {" + ", ".join(lit(v) for v in el.weights) + "};",
+        "__device__ __constant__ const float WEIGHTS_F_[] = {" + ", ".join(lit(v) for v in el.weights) + "};",
         "struct Ops {",
         f"  static constexpr int D = {D};",
         f"  static constexpr int P = {P};",
@@ -959,6 +1005,8 @@ def generate(D, P, out_path):
         "  static __device__ __forceinline__ double minv(int n) { return MINV_[n]; }",
         "  static __device__ __forceinline__ double node(int k) { return NODES_[k]; }",
         "  static __device__ __forceinline__ double weight(int k) { return WEIGHTS_[k]; }",
+        "  static __device__ __forceinline__ float weight_f(int k) { return WEIGHTS_F_[k]; }",
+        f"  static constexpr double WEIGHT_SUM = {lit(sum(el.weights))};  // sum of the GL weights",
     ]
     counts = {}
     for name, op in ops.items():
@@ -983,6 +1031,8 @@ def generate(D, P, out_path):
     hdr.append(disp("vol_eval_slice", [((k,), f"vol_eval_slice{k}") for k in range(N)], ["k"]))
     hdr.append(disp("face_slice", [((d, s), f"face_slice{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("face_eval", [((d, s), f"face_eval{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
+    hdr.append(disp("face_eval_sp", [((d, s), f"face_eval_sp{d}{s}") for d in range(D) for s in range(2)],
+                    ["d", "s"]))
     hdr.append(disp("bd_term", [((d, s), f"bd_term{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("pcf", [((l,), f"pcf{l}") for l in range(1 << D)], ["l"]))
     hdr.append(disp("pfc", [((l,), f"pfc{l}") for l in range(1 << D)], ["l"]))
