@@ -400,7 +400,8 @@ int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
   fa.face_right = ctx->face_right.p;
   for (int d = 0; d <= 3; ++d) fa.face_off[d] = (d <= D) ? H.face_off[d] : H.face_off[D];
   fa.Fnum = ctx->Fnum.p;
-  e = ks->numflux(fa, (long long)H.face_left.size(), ctx->stream);
+  const bool split_tiles = ctx->seed_mode == 2 && ctx->seed;  // predictor modes 2 and 3
+  e = ks->numflux(fa, (long long)H.face_left.size(), ctx->stream, split_tiles);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "numflux launch");
   ctx->launches++;
   if (ev) cudaEventRecord(ev[2], ctx->stream);
@@ -2052,11 +2053,13 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base, cudaEvent_t
   pa.sweeps = ctx->seed_sweeps;
   e = ks->predictor(pa, ctx->E, st, ctx->seed_mode);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "seeded predictor");
-  PredictorArgs fb = base;  // full FP64 Picard for the rejected elements
+  // full FP64 Picard for the rejected elements; in a mode-2 step with the
+  // seeded elements' final stage (mode 3), so that every trace tile is a split tile
+  PredictorArgs fb = base;
   fb.elem_list = ctx->fb_list.p;
   fb.list_count = ctx->fb_count.p;
   fb.count_total = ctx->fb_total.p;
-  e = ks->predictor(fb, ctx->E, st, 0);
+  e = ks->predictor(fb, ctx->E, st, ctx->seed_mode == 2 ? 3 : 0);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "fallback predictor");
   ctx->launches += 2;
   return ADG_OK;

@@ -14,15 +14,16 @@ using O = ADG_NS::Ops;
 //   FP32 sweeps (MODE 2)    D NQ_ST ld floats
 //   final volume slices     (1 + D) NQ_S ld doubles
 //   face traces             2 NQ_BD ld doubles   (one direction at a time)
-//   MODE 2 final stage      split_epilogue_doubles (volume and face phases)
+//   MODE 2, 3 final stage   split_epilogue_doubles (volume and face phases)
 //   seed residual           2 E Q doubles
 template <int E, int MODE>
 constexpr size_t smem_bytes() {
   constexpr size_t ld = E * O::Q + 1;
+  constexpr bool split = MODE == 2 || MODE == 3;
   constexpr size_t sweeps = MODE == 2 ? O::D * O::NQ_ST * ld * sizeof(float) : O::D * O::NQ_ST * ld * sizeof(double);
-  constexpr size_t fin = MODE == 2 ? split_epilogue_doubles<O>(ld) * sizeof(double)
-                                   : (1 + O::D) * O::NQ_S * ld * sizeof(double);
-  constexpr size_t faces = MODE == 2 ? 0 : 2 * O::NQ_BD * ld * sizeof(double);
+  constexpr size_t fin = split ? split_epilogue_doubles<O>(ld) * sizeof(double)
+                               : (1 + O::D) * O::NQ_S * ld * sizeof(double);
+  constexpr size_t faces = split ? 0 : 2 * O::NQ_BD * ld * sizeof(double);
   constexpr size_t red = 2 * E * O::Q * sizeof(double);
   constexpr size_t m1 = sweeps > fin ? sweeps : fin;
   constexpr size_t m2 = faces > red ? faces : red;
@@ -47,6 +48,7 @@ template <int E>
 cudaError_t launch_predictor(const PredictorArgs& a, cudaStream_t s, int mode) {
   if (mode == 1) return launch_predictor_mode<E, 1>(a, s);
   if (mode == 2) return launch_predictor_mode<E, 2>(a, s);
+  if (mode == 3) return launch_predictor_mode<E, 3>(a, s);
   return launch_predictor_mode<E, 0>(a, s);
 }
 
@@ -85,10 +87,14 @@ struct Impl final : KernelSet {
     return launch_predictor<16>(a, s, mode);
   }
 #endif
-  cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s) const override {
+  cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s, bool split) const override {
     if (nface <= 0) return cudaSuccess;
     constexpr int FB = numflux_faces_per_block<O>();
-    k_numflux<O><<<(unsigned)((nface + FB - 1) / FB), FB * O::NQ_BD, 0, s>>>(a);
+    const unsigned grid = (unsigned)((nface + FB - 1) / FB);
+    if (split)
+      k_numflux_split<O><<<grid, FB * O::NQ_BD, 0, s>>>(a);
+    else
+      k_numflux<O><<<grid, FB * O::NQ_BD, 0, s>>>(a);
     return cudaGetLastError();
   }
   cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const override {

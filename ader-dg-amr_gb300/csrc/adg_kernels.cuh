@@ -5,7 +5,10 @@
 //   Rvol  [elem][q][n]                 M U + sum_d (Dt/dx_d) Sk_corr[d] F_d
 //   Tr    [elem][face 2d+s][tile]      tile = field * NQ_BD + t * NS_BD + x (time node t,
 //                                      spatial face point x < NS_BD = NQ_BD / N), field: u_q (Q),
-//                                      f_q (Q), |un|+c (1); tiles padded to an even count of doubles
+//                                      f_q (Q), |un|+c (1); tiles padded to an even count of doubles.
+//                                      Seeded FP32 path (split tiles, same size): u_q and f_q at
+//                                      the NS_BD spatial points in FP64, then the FP32 changes
+//                                      of u_q and f_q over time and |un|+c at the NQ_BD points
 //   Fnum  [face][q][j]                 tangential moments (j < NM) of the local
 //                                      Lax-Friedrichs flux over the face
 // Element-level work is organised in "columns": one thread owns one
@@ -38,6 +41,20 @@ constexpr int kScalCount = kScalDtDx + 3 * kMaxLevels;
 template <class O>
 constexpr int tr_tile() {
   return ((2 * O::Q + 1) * O::NQ_BD + 1) & ~1;
+}
+
+// Split trace tile of the seeded FP32 path, in the same TT doubles:
+//   doubles [0, Q NSB)         u_q at the face's spatial points x        [q][x]
+//   doubles [Q NSB, 2 Q NSB)   the normal flux f_q(u) there              [q][x]
+//   floats from split_tr_float_off: the changes of u_q and f_q at the
+//   space-time face points p = t NSB + x ([q][p] each), then |un|+c [p].
+template <class O>
+constexpr int split_tr_float_off() {
+  return 2 * 2 * O::Q * (O::NQ_BD / O::N);
+}
+template <class O>
+constexpr bool split_tr_fits() {
+  return split_tr_float_off<O>() + (2 * O::Q + 1) * O::NQ_BD <= 2 * tr_tile<O>();
 }
 
 struct PredictorArgs {
@@ -275,7 +292,7 @@ template <class O>
 constexpr size_t split_epilogue_doubles(size_t ld) {
   constexpr size_t NS = O::NQ_S, NB = O::NQ_BD, NSB = NB / O::N;
   const size_t vol = (1 + O::D) * NS * ld + (NS * ld + 1) / 2;
-  const size_t faces = (4 * NSB + (2 * NSB + 2 * NB + 1) / 2) * ld;
+  const size_t faces = (2 * NSB + (2 * NSB + 2 * NB + 1) / 2) * ld;
   return vol > faces ? vol : faces;
 }
 
@@ -312,9 +329,9 @@ __device__ __forceinline__ void delta_slices(const float* dlt, const float* us32
   if constexpr (K + 1 < O::N) delta_slices<O, E, K + 1>(dlt, us32, ds32, fb32, col, gm1f);
 }
 
-// Column part of one face side: U at the face's spatial points (FP64), delta
-// at its space-time points (FP32), both to shared memory, and the trace of
-// H = U + delta to the element's tile.
+// Column part of one face side: U at the face's spatial points (FP64) and
+// delta at its space-time points (FP32), to shared memory and to the split
+// trace tile (u_q and its change).
 template <class O, int E, int DIR, int S>
 __device__ __forceinline__ void split_face_column(const double* u, const float* dlt, double* uface64, float* uf32,
                                                   float* dface32, int col, int q, double* tr_elem) {
@@ -323,12 +340,14 @@ __device__ __forceinline__ void split_face_column(const double* u, const float* 
   float df[NB];
   O::template face_eval_sp<DIR, S>(RegIn{u}, RegOut{uf});
   O::template face_eval<DIR, S, float>(RegInT<float>{dlt}, RegOutT<float>{df});  // point x N + t
+  double* t = tr_elem ? tr_elem + (2 * DIR + S) * TT : nullptr;
 #pragma unroll
   for (int x = 0; x < NSB; ++x) {
     uface64[(S * NSB + x) * LD + col] = uf[x];
     uf32[(S * NSB + x) * LD + col] = (float)uf[x];
+    if (t) t[q * NSB + x] = uf[x];
   }
-  double* t = tr_elem ? tr_elem + (2 * DIR + S) * TT + q * NB : nullptr;
+  float* tf = t ? reinterpret_cast<float*>(t) + split_tr_float_off<O>() + q * NB : nullptr;
 #pragma unroll
   for (int tt = 0; tt < N; ++tt)
 #pragma unroll
@@ -336,21 +355,21 @@ __device__ __forceinline__ void split_face_column(const double* u, const float* 
       const int p = tt * NSB + x;  // tile position
       const float d = df[x * N + tt];
       dface32[(S * NB + p) * LD + col] = d;
-      if (t) t[p] = uf[x] + (double)d;
+      if (tf) tf[p] = d;
     }
 }
 
-// The two faces of direction DIR: H traces (columns), F_n(U) at the faces'
-// spatial points (FP64, points), then per space-time face point the flux
-// change and the wave speed (FP32), F_n = F_n(U) + change, to the tiles.
+// The two faces of direction DIR as split trace tiles: u and its change
+// (columns), then f_n(u) at the faces' spatial points (FP64) and, per
+// space-time face point, the change of f_n and the wave speed (FP32).
 template <class O, int E, int DIR>
 __device__ __forceinline__ void split_faces(const double* u, const float* dlt, double* sm, int col, int q,
                                             double* tr_elem, const PredictorArgs& a, int e0, int limit) {
   constexpr int D = O::D, Q = O::Q, N = O::N, NB = O::NQ_BD, NSB = NB / N, NF = 2 * D, TT = tr_tile<O>();
-  constexpr int LD = E * Q + 1;
+  constexpr int LD = E * Q + 1, FO = split_tr_float_off<O>();
+  static_assert(split_tr_fits<O>(), "split trace tile larger than the FP64 tile");
   double* uface64 = sm;                                         // [side][x][col]
-  double* fun64 = sm + 2 * NSB * LD;                            // [side][x][col]
-  float* uf32 = reinterpret_cast<float*>(sm + 4 * NSB * LD);    // [side][x][col]
+  float* uf32 = reinterpret_cast<float*>(sm + 2 * NSB * LD);    // [side][x][col]
   float* dface32 = uf32 + 2 * NSB * LD;                         // [side][t NSB + x][col]
   split_face_column<O, E, DIR, 0>(u, dlt, uface64, uf32, dface32, col, q, tr_elem);
   split_face_column<O, E, DIR, 1>(u, dlt, uface64, uf32, dface32, col, q, tr_elem);
@@ -359,16 +378,17 @@ __device__ __forceinline__ void split_faces(const double* u, const float* dlt, d
     const int x = it % NSB;
     const int s = (it / NSB) & 1;
     const int ee = it / (2 * NSB);
+    if (e0 + ee >= limit) continue;
+    const int elem = a.elem_list ? a.elem_list[e0 + ee] : e0 + ee;
     const double* b = uface64 + (s * NSB + x) * LD + ee * Q;
     double uu[Q], F[Q];
 #pragma unroll
     for (int k = 0; k < Q; ++k) uu[k] = b[k];
     (void)euler_flux_normal<D>(DIR, uu, a.gamma, F);
-    double* f = fun64 + (s * NSB + x) * LD + ee * Q;
+    double* t = a.Tr + ((size_t)elem * NF + 2 * DIR + s) * TT + Q * NSB + x;
 #pragma unroll
-    for (int k = 0; k < Q; ++k) f[k] = F[k];
+    for (int k = 0; k < Q; ++k) t[k * NSB] = F[k];
   }
-  __syncthreads();
   const float gm1f = (float)(a.gamma - 1.0), gf = (float)a.gamma;
 #pragma unroll 2
   for (int it = threadIdx.x; it < E * 2 * NB; it += blockDim.x) {
@@ -385,11 +405,10 @@ __device__ __forceinline__ void split_faces(const double* u, const float* dlt, d
       du[k] = dface32[(s * NB + p) * LD + ee * Q + k];
     }
     const float ws = euler_dflux_normal<D>(DIR, uu, du, gm1f, gf, dF);
-    const double* f = fun64 + (s * NSB + x) * LD + ee * Q;
-    double* t = a.Tr + ((size_t)elem * NF + 2 * DIR + s) * TT + p;
+    float* t = reinterpret_cast<float*>(a.Tr + ((size_t)elem * NF + 2 * DIR + s) * TT) + FO + p;
 #pragma unroll
-    for (int k = 0; k < Q; ++k) t[(Q + k) * NB] = f[k] + (double)dF[k];
-    t[2 * Q * NB] = (double)ws;
+    for (int k = 0; k < Q; ++k) t[(Q + k) * NB] = dF[k];
+    t[2 * Q * NB] = ws;
   }
   __syncthreads();
 }
@@ -522,7 +541,9 @@ __device__ __forceinline__ void fp64_epilogue(const double* hw, const double* u,
 
 // MODE 0: plain FP64 Picard (the reference's initial guess, P sweeps);
 // MODE 1 / 2: seeded, `sweeps` sweeps from the learned seed in FP64 / FP32,
-// the first one judging the seed by its residual.
+// the first one judging the seed by its residual;
+// MODE 3: the FP64 Picard of MODE 0 with the final stage and split trace
+// tiles of MODE 2 (the fallback elements of a MODE 2 step).
 template <class O, int E, int MODE = 0>
 __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NP_ST = O::NP_ST;
@@ -559,9 +580,9 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
   double wu[NP_ST];
   O::wu(RegIn{u}, RegOut{wu});
   double hw[NP_ST];
-  float dlt[NP_ST];  // MODE 2: H_w - W U from the FP32 sweeps
+  float dlt[NP_ST];  // MODES 2, 3: H_w - W U in FP32
 
-  if constexpr (MODE == 0) {
+  if constexpr (MODE == 0 || MODE == 3) {
     // ---- sweep 1: the reference's initial guess H_w = [U_w, 0, ...]
     // (AmrDG.tpp:520-533) does not depend on x_0; evaluate on the (x_1.., t) grid.
     O::vol_eval_init(RegIn{u}, ColOut{sm + col, LD});
@@ -679,10 +700,14 @@ __global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
 #pragma unroll
     for (int n = 0; n < NP_ST; ++n) dst[n] = MODE == 2 ? wu[n] + (double)dlt[n] : hw[n];
   }
-  if constexpr (MODE == 2)
+  if constexpr (MODE == 2 || MODE == 3) {
+    if constexpr (MODE == 3)
+#pragma unroll
+      for (int n = 0; n < NP_ST; ++n) dlt[n] = (float)(hw[n] - wu[n]);
     split_epilogue<O, E>(u, dlt, c, gm1, sm, col, q, live, e, a);
-  else
+  } else {
     fp64_epilogue<O, E>(hw, u, c, gm1, sm, col, q, live, e, a);
+  }
 }
 
 // N consecutive doubles to registers (and back): 16-byte accesses when every
@@ -777,6 +802,75 @@ __global__ void k_numflux(FaceArgs a) {
 #pragma unroll
     for (int t = 1; t < N; ++t) sum = fma(0.5 * O::weight(t), hc[t * NSB], sum);
     g[c * LDG + x] = sum;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < nfb * Q; c += NT) {
+    double mom[NM];
+    O::face_mom_sp(ColIn{g + c * LDG, 1}, RegOut{mom});
+    store_run<NM>(a.Fnum + ((size_t)fbase * Q + c) * NM, mom);
+  }
+}
+
+// k_numflux on split trace tiles (the seeded FP32 path).  With u = U + du and
+// f = F + df on each side (U, F time-independent, FP64), twice the LLF flux
+// integrated over time with the weights w_t / 2 is
+//   (sum_t w_t / 2) (F_L + F_R) + A - S (U_R - U_L),
+//   A = sum_t (w_t / 2) (df_L + df_R - C_t (du_R - du_L)),  S = sum_t (w_t / 2) C_t,
+// so the time-dependent part (A, S) runs in FP32 and FP64 is spent once per
+// spatial face point.
+//   Phase 1, thread (face, point): C_t and the FP32 terms of A.
+//   Phase 2, thread (face, variable, x): A, S and the FP64 sum.
+//   Phase 3, thread (face, variable): the tangential moments (face_mom_sp).
+template <class O>
+__global__ void k_numflux_split(FaceArgs a) {
+  constexpr int D = O::D, Q = O::Q, N = O::N, NB = O::NQ_BD, NSB = NB / N, NF = 2 * D, NM = O::NM;
+  constexpr int TT = tr_tile<O>(), FB = numflux_faces_per_block<O>(), NT = FB * NB, FO = split_tr_float_off<O>();
+  constexpr int LDH = NB + 1, LDG = NSB + 1;
+  __shared__ float h[FB * Q * LDH];
+  __shared__ float cs[FB * LDH];
+  __shared__ double g[FB * Q * LDG];
+  const int64_t nface = a.face_off[D];
+  const int64_t fbase = (int64_t)blockIdx.x * FB;
+  const int nfb = (int)(nface - fbase < FB ? nface - fbase : FB);
+  {
+    const int lf = threadIdx.x / NB, m = threadIdx.x % NB;  // m = t NSB + x
+    if (lf < nfb) {
+      const int64_t f = fbase + lf;
+      int d = 0;
+#pragma unroll
+      for (int k = 1; k < D; ++k)
+        if (f >= a.face_off[k]) d = k;
+      const int L = a.face_left[f], R = a.face_right[f];
+      const float* tl = reinterpret_cast<const float*>(a.Tr + ((size_t)L * NF + 2 * d + 1) * TT) + FO + m;
+      const float* tr = reinterpret_cast<const float*>(a.Tr + ((size_t)R * NF + 2 * d + 0) * TT) + FO + m;
+      const float C = fmaxf(fabsf(tl[2 * Q * NB]), fabsf(tr[2 * Q * NB]));
+      cs[lf * LDH + m] = C;
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+        h[(lf * Q + q) * LDH + m] = fmaf(-C, tr[q * NB] - tl[q * NB], tl[(Q + q) * NB] + tr[(Q + q) * NB]);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nfb * Q * NSB; i += NT) {
+    const int x = i % NSB, c = i / NSB;  // c = face * Q + q
+    const int lf = c / Q, q = c % Q;
+    const int64_t f = fbase + lf;
+    int d = 0;
+#pragma unroll
+    for (int k = 1; k < D; ++k)
+      if (f >= a.face_off[k]) d = k;
+    const double* tl = a.Tr + ((size_t)a.face_left[f] * NF + 2 * d + 1) * TT + q * NSB + x;
+    const double* tr = a.Tr + ((size_t)a.face_right[f] * NF + 2 * d + 0) * TT + q * NSB + x;
+    const float* hc = h + c * LDH + x;
+    const float* cc = cs + lf * LDH + x;
+    float A = (0.5f * O::weight_f(0)) * hc[0], S = (0.5f * O::weight_f(0)) * cc[0];
+#pragma unroll
+    for (int t = 1; t < N; ++t) {
+      A = fmaf(0.5f * O::weight_f(t), hc[t * NSB], A);
+      S = fmaf(0.5f * O::weight_f(t), cc[t * NSB], S);
+    }
+    const double fsum = tl[Q * NSB] + tr[Q * NSB], jump = tr[0] - tl[0];
+    g[c * LDG + x] = fma(-(double)S, jump, fma(0.5 * O::WEIGHT_SUM, fsum, (double)A));
   }
   __syncthreads();
   for (int c = threadIdx.x; c < nfb * Q; c += NT) {

@@ -20,7 +20,8 @@ struct KernelSet {
   virtual std::vector<int> elems_per_block_choices() const = 0;
   virtual size_t predictor_smem(int E) const = 0;
   virtual cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s, int mode = 0) const = 0;
-  virtual cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s) const = 0;
+  // split: the trace tiles are split tiles (predictor modes 2 and 3)
+  virtual cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s, bool split = false) const = 0;
   virtual cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t dt_reduce(const DtArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t init_ic(const ICArgs& a, cudaStream_t s) const = 0;

@@ -140,6 +140,55 @@ def test_zero_tolerance_falls_back_everywhere_to_the_plain_path():
     assert fb == n == 3 * 32 * 32
 
 
+def test_fp32_path_fallback_is_the_fp64_picard_with_split_traces():
+    """Mode 2 with a zero tolerance: every element takes the FP64 Picard
+    fallback, whose final stage (volume term and split face traces, H = U +
+    FP32 change) is the seeded path's; against the plain FP64 path it
+    differs only by the FP32 rounding of the change of H."""
+    seed, _, _ = _trained_seed()
+    a = _kh(n=32, seed=9)
+    b = _kh(n=32, seed=9)
+    seed.attach(b, mode=2, sweeps=2, tol=1e-300)
+    for _ in range(3):
+        a.time_integration()
+        b.time_integration()
+    fb, n = G.seed_stats(b)
+    assert fb == n == 3 * 32 * 32
+    assert b.status() == 0
+    ua, ub = a.get_U_w(), b.get_U_w()
+    # relative to each variable's largest cell mean (the y momentum of this
+    # flow is only its 1e-3 noise, so its bound is the loosest)
+    scale = np.max(np.abs(ua[:, :, 0]), axis=0)
+    err = np.max(np.abs(ua - ub), axis=(0, 2)) / scale
+    assert np.all(err < 1e-7), err
+    assert np.any(ua != ub)  # the split path ran (not bitwise the plain one)
+
+
+def test_fp32_path_conserves_mass_and_tracks_the_plain_path():
+    """Mode 2 with its working tolerance on a periodic domain: the mean
+    density is conserved to rounding (the split numerical flux is one value
+    per face, shared by both sides), and the state stays closer to the plain
+    FP64 path (three sweeps) than two FP64 sweeps without the seed do."""
+    seed, _, _ = _trained_seed()
+    a = _kh(seed=5)
+    b = _kh(seed=5)
+    c = _kh(seed=5, picard_sweeps=2)
+    seed.attach(b, mode=2, sweeps=2, tol=1e-3)
+    m0 = b.get_U_w()[:, 0, 0].sum()
+    for _ in range(10):
+        for s in (a, b, c):
+            s.time_integration()
+    ub = b.get_U_w()
+    assert abs(ub[:, 0, 0].sum() - m0) < 1e-12 * abs(m0)
+    ua = a.get_U_w()
+    scale = np.max(np.abs(ua[:, :, 0]), axis=0)
+
+    def dist(u):
+        return float(np.max(np.max(np.abs(u - ua), axis=(0, 2)) / scale))
+
+    assert dist(ub) < 0.1 * dist(c.get_U_w()), (dist(ub), dist(c.get_U_w()))
+
+
 def _seed_correction(H, U, s, seed):
     """(H - W U) / (rho_mean Dt/dx): the network's share of the seed."""
     import oracle_ffi as O
