@@ -11,7 +11,7 @@ using O = ADG_NS::Ops;
 
 // Dynamic shared memory of k_predictor per phase (ld = E Q + 1 slots per point):
 //   FP64 sweeps             D NQ_ST ld doubles   (MODE 0 first sweep: D NQ_INIT)
-//   FP32 sweeps (MODE 2)    D NQ_ST ld floats
+//   FP32 sweeps (MODE 2)    D NQ_S ld floats     (one time slice at a time)
 //   final volume slices     (1 + D) NQ_S ld doubles
 //   face traces             2 NQ_BD ld doubles   (one direction at a time)
 //   MODE 2, 3 final stage   split_epilogue_doubles (volume and face phases)
@@ -20,7 +20,7 @@ template <int E, int MODE>
 constexpr size_t smem_bytes() {
   constexpr size_t ld = E * O::Q + 1;
   constexpr bool split = MODE == 2 || MODE == 3;
-  constexpr size_t sweeps = MODE == 2 ? O::D * O::NQ_ST * ld * sizeof(float) : O::D * O::NQ_ST * ld * sizeof(double);
+  constexpr size_t sweeps = MODE == 2 ? O::D * O::NQ_S * ld * sizeof(float) : O::D * O::NQ_ST * ld * sizeof(double);
   constexpr size_t fin = split ? split_epilogue_doubles<O>(ld) * sizeof(double)
                                : (1 + O::D) * O::NQ_S * ld * sizeof(double);
   constexpr size_t faces = split ? 0 : 2 * O::NQ_BD * ld * sizeof(double);

@@ -137,27 +137,52 @@ __device__ __forceinline__ void picard_sweep(const double* hw, const double* wu,
   __syncthreads();
 }
 
-// One Picard sweep entirely in FP32 (the seeded path's sweeps): H = V hw,
-// F_d = f_d(H), and only the change dlt = -sum_d c_d A_d F_d is returned, so
-// that the caller forms H_w' = W U + dlt in the precision it needs.
+// Time slice K of an FP32 Picard sweep: H at the spatial points of time node
+// K (vol_eval_slice), its fluxes (F_0 over H, F_d in slab d), and their
+// projections accumulated into the space-time modes with the sliced form of
+// proj<d>: A_d F = C_d sum_k T_k V_s^T F(., t_k), acc[d] = sum_k T_k V_s^T F_d.
+// A column reads and writes only its own entries of the slabs, so the slice
+// needs two barriers (columns -> points -> columns).
+template <class O, int E, int K>
+__device__ __forceinline__ void sweep_slice_f32(const float* hw, float* sm, int col, float gm1,
+                                                float (&acc)[O::D][O::NP_ST]) {
+  constexpr int D = O::D, Q = O::Q, NS = O::NQ_S, NP_S = O::NP_S, NP_ST = O::NP_ST, LD = E * Q + 1;
+  O::template vol_eval_slice<K, float>(RegInT<float>{hw}, ColOutT<float>{sm + col, LD});
+  __syncthreads();
+  flux_stage<O, E, NS, float>(sm, LD, gm1);
+  __syncthreads();
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    float v[NP_S];
+    O::template vt_sp<float>(ColInT<float>{sm + d * NS * LD + col, LD}, RegOutT<float>{v});
+#pragma unroll
+    for (int n = 0; n < NP_ST; ++n) {
+      const float tv = O::time_val_f(O::st_time(n), K);
+      acc[d][n] = K == 0 ? tv * v[O::st_space(n)] : fmaf(tv, v[O::st_space(n)], acc[d][n]);
+    }
+  }
+  if constexpr (K + 1 < O::N) sweep_slice_f32<O, E, K + 1>(hw, sm, col, gm1, acc);
+}
+
+// One Picard sweep entirely in FP32 (the seeded path's sweeps), one time
+// slice at a time (D NS ld floats of shared memory): H = V hw, F_d = f_d(H),
+// and only the change dlt = -sum_d c_d A_d F_d is returned, so that the
+// caller forms H_w' = W U + dlt in the precision it needs.
 template <class O, int E>
 __device__ __forceinline__ void picard_sweep_f32(const float* hw, const float* c, float* sm, int col, float gm1,
                                                  float* dlt) {
-  constexpr int D = O::D, NP_ST = O::NP_ST, NQ = O::NQ_ST;
-  constexpr int LD = E * O::Q + 1;
-  O::template vol_eval<float>(RegInT<float>{hw}, ColOutT<float>{sm + col, LD});
-  __syncthreads();
-  flux_stage<O, E, NQ, float>(sm, LD, gm1);
-  __syncthreads();
+  constexpr int D = O::D, NP_ST = O::NP_ST;
+  float acc[D][NP_ST];
+  sweep_slice_f32<O, E, 0>(hw, sm, col, gm1, acc);
   float y[NP_ST];
-  O::template proj<0, float>(ColInT<float>{sm + col, LD}, RegOutT<float>{y});
+  O::template cproj<0, float>(RegInT<float>{acc[0]}, RegOutT<float>{y});
 #pragma unroll
   for (int n = 0; n < NP_ST; ++n) dlt[n] = -c[0] * y[n];
-  O::template proj<1, float>(ColInT<float>{sm + NQ * LD + col, LD}, RegOutT<float>{y});
+  O::template cproj<1, float>(RegInT<float>{acc[1]}, RegOutT<float>{y});
 #pragma unroll
   for (int n = 0; n < NP_ST; ++n) dlt[n] = fmaf(-c[1], y[n], dlt[n]);
   if constexpr (D == 3) {
-    O::template proj<2, float>(ColInT<float>{sm + 2 * NQ * LD + col, LD}, RegOutT<float>{y});
+    O::template cproj<2, float>(RegInT<float>{acc[2]}, RegOutT<float>{y});
 #pragma unroll
     for (int n = 0; n < NP_ST; ++n) dlt[n] = fmaf(-c[2], y[n], dlt[n]);
   }
@@ -285,13 +310,13 @@ __device__ __forceinline__ void face_traces(const double* hw, double* sm, int co
 // wave speed.
 // ---------------------------------------------------------------------------
 
-// Shared memory of split_epilogue (doubles): region A = (1 + D) NS ld doubles
-// (U and F(U) at the spatial points, later the FP32 delta slice and flux
-// change sums, later the face buffers), then NS ld floats of U in FP32.
+// Shared memory of split_epilogue (doubles): region A = D NS ld doubles (U,
+// then F(U) at the spatial points; later the FP32 delta slice and flux
+// change sums; later the face buffers), then NS ld floats of U in FP32.
 template <class O>
 constexpr size_t split_epilogue_doubles(size_t ld) {
   constexpr size_t NS = O::NQ_S, NB = O::NQ_BD, NSB = NB / O::N;
-  const size_t vol = (1 + O::D) * NS * ld + (NS * ld + 1) / 2;
+  const size_t vol = O::D * NS * ld + (NS * ld + 1) / 2;
   const size_t faces = (2 * NSB + (2 * NSB + 2 * NB + 1) / 2) * ld;
   return vol > faces ? vol : faces;
 }
@@ -418,9 +443,9 @@ __device__ __forceinline__ void split_epilogue(const double* u, const float* dlt
                                                double* sm, int col, int q, bool live, int e, const PredictorArgs& a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NS = O::NQ_S, NF = 2 * D;
   constexpr int LD = E * Q + 1;
-  double* us64 = sm;
-  double* fU64 = sm + NS * LD;
-  float* us32 = reinterpret_cast<float*>(sm + (1 + D) * NS * LD);
+  double* us64 = sm;  // U, then F_0(U) in place
+  double* fU64 = sm;  // F_d(U) in slab d
+  float* us32 = reinterpret_cast<float*>(sm + D * NS * LD);
 
   // U at the spatial points (FP64, and in FP32 for the flux changes)
   O::sp_eval(RegIn{u}, ColOut{us64 + col, LD});
@@ -428,21 +453,7 @@ __device__ __forceinline__ void split_epilogue(const double* u, const float* dlt
   for (int m = 0; m < NS; ++m) us32[m * LD + col] = (float)us64[m * LD + col];
   __syncthreads();
   // F(U) at the spatial points (FP64)
-#pragma unroll 2
-  for (int it = threadIdx.x; it < E * NS; it += blockDim.x) {
-    const int m = it % NS;
-    const int ee = it / NS;
-    const double* b = us64 + m * LD + ee * Q;
-    double uu[Q], F[D * Q];
-#pragma unroll
-    for (int k = 0; k < Q; ++k) uu[k] = b[k];
-    euler_flux_all<D, double>(uu, gm1, F);
-    double* f = fU64 + m * LD + ee * Q;
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-#pragma unroll
-      for (int k = 0; k < Q; ++k) f[d * NS * LD + k] = F[d * Q + k];
-  }
+  flux_stage<O, E, NS, double>(us64, LD, gm1);
   __syncthreads();
   // volume term of the time-constant part (AmrDG.tpp:696-709 with F = F(U)):
   // M U + sum_d c_d (sum_k w_k) Sk_d F_d(U)
@@ -544,8 +555,17 @@ __device__ __forceinline__ void fp64_epilogue(const double* hw, const double* u,
 // the first one judging the seed by its residual;
 // MODE 3: the FP64 Picard of MODE 0 with the final stage and split trace
 // tiles of MODE 2 (the fallback elements of a MODE 2 step).
+// Resident blocks per SM that MODE 2 asks for: 16 warps (at most 128
+// registers a thread); its sliced sweeps leave the shared memory for them.
+template <int E, int Q, int MODE>
+constexpr int predictor_min_blocks() {
+  constexpr int warps = (E * Q + 31) / 32;
+  return MODE == 2 && 16 / warps > 0 ? 16 / warps : 1;
+}
+
 template <class O, int E, int MODE = 0>
-__global__ void __launch_bounds__(E * O::Q) k_predictor(PredictorArgs a) {
+__global__ void __launch_bounds__(E * O::Q, (predictor_min_blocks<E, O::Q, MODE>()))
+    k_predictor(PredictorArgs a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NP_ST = O::NP_ST;
   constexpr int NQ = O::NQ_ST, NI = O::NQ_INIT;
   constexpr int NCOL = E * Q;

@@ -646,6 +646,31 @@ def build_ops(el):
         if max(abs(VW[i][j] - want[j]) for j in range(el.Np_s)) > 1e-12:
             raise SystemExit("W U is not U constant in time")
 
+    # ---- the projections A_d = C_d V^T one time slice at a time:
+    #   A_d F = C_d sum_k T_k vt_sp(F(., t_k)),
+    # vt_sp = V_s^T (spatial points -> spatial modes, no weights), T_k the
+    # expansion of spatial mode b to the space-time modes (b, a_t) with the
+    # factor val[a_t][k] (st_time / st_space / time_val tables), cproj_d = C_d.
+    stages, keys = ch.project_chain(list(range(D)), sp_keys, {p: el.val for p in range(D)}, degree_ok(P))
+    stages.append(stage_from_map(keys, s_keys, lambda ok: [(ok, 1.0)]))
+    dense_vts = [[dense_sp[m][b] for m in range(len(el.pts_s))] for b in range(el.Np_s)]
+    check_chain(stages, dense_vts, "vt_sp")
+    ops["vt_sp"] = (stages, len(sp_keys), el.Np_s)
+    st_space = [el.mi_s.index(tuple(n[:D])) for n in el.mi_st]
+    st_time = [n[D] for n in el.mi_st]
+    for d in range(D):
+        Cd = el.C[d]
+        ops[f"cproj{d}"] = ([Stage(el.Np_st, el.Np_st, [[(c, Cd[r][c]) for c in range(el.Np_st) if Cd[r][c] != 0.0]
+                                                      for r in range(el.Np_st)])], el.Np_st, el.Np_st)
+        # the sliced form against A_d
+        for r in range(el.Np_st):
+            for i, pt in enumerate(el.pts_st):
+                k, m = pt[D], el.pts_s.index(tuple(pt[:D]))
+                v = sum(Cd[r][n] * el.val[st_time[n]][k] * dense_vts[st_space[n]][m] for n in range(el.Np_st))
+                if abs(v - el.A[d][r][i]) > 1e-11 * max(1.0, abs(el.A[d][r][i])):
+                    raise SystemExit(f"sliced projection {d} does not reproduce A_{d}")
+    el.st_space, el.st_time = st_space, st_time
+
     # ---- face_eval_sp[d][side]: spatial modes -> the face's spatial points
     # (free dims != d in order, face_slice's point order)
     for d in range(D):
@@ -1033,6 +1058,23 @@ def generate(D, P, out_path):
     hdr.append(disp("face_eval", [((d, s), f"face_eval{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("face_eval_sp", [((d, s), f"face_eval_sp{d}{s}") for d in range(D) for s in range(2)],
                     ["d", "s"]))
+    hdr.append(disp("cproj", [((d,), f"cproj{d}") for d in range(D)], ["d"]))
+    # space-time mode n = (spatial mode st_space(n), time degree st_time(n));
+    # time_val(a, k) = P_a(t_k)
+    # (constexpr selections rather than arrays, which device code cannot
+    # read; called with compile-time arguments inside unrolled loops)
+    def select(var, vals, fmt):
+        expr = fmt(vals[-1])
+        for i in range(len(vals) - 2, -1, -1):
+            expr = f"{var} == {i} ? {fmt(vals[i])} : ({expr})"
+        return expr
+    hdr.append("  static constexpr __host__ __device__ int st_space(int n) { return "
+               + select("n", el.st_space, str) + "; }")
+    hdr.append("  static constexpr __host__ __device__ int st_time(int n) { return "
+               + select("n", el.st_time, str) + "; }")
+    tv = [el.val[a][k] for a in range(P + 1) for k in range(N)]
+    hdr.append(f"  static constexpr __host__ __device__ float time_val_f(int a, int k) {{ return "
+               + select(f"(a * {N} + k)", tv, lambda v: lit(v) + "f") + "; }")
     hdr.append(disp("bd_term", [((d, s), f"bd_term{d}{s}") for d in range(D) for s in range(2)], ["d", "s"]))
     hdr.append(disp("pcf", [((l,), f"pcf{l}") for l in range(1 << D)], ["l"]))
     hdr.append(disp("pfc", [((l,), f"pfc{l}") for l in range(1 << D)], ["l"]))
