@@ -126,7 +126,7 @@ __host__ __device__ __forceinline__ int kmajor_off(int row, int k, int K) {
 // to a multiple of 8 (the TF32 MMA's K), output to a multiple of 16 (N of an
 // M = 128 MMA).
 constexpr int kSeedTcHidden = 128;
-constexpr int kSeedTcThreads = 256;
+constexpr int kSeedTcThreads = 512;  // four threads per row and layer column quarter
 constexpr int kSeedTcRows = 128;
 constexpr size_t kSeedTcBuf = 65536;                     // one operand buffer
 constexpr int kSeedTcUfLd = 52;                           // row stride of the FP32 copy of the states
@@ -220,9 +220,11 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
   const bool u_ok = tc::mbar_wait(&bars[3], 0);
   if (!u_ok && t == 0) atomicOr(a.status, kStatusSeedWait);
 
-  // ---- features of row r (two threads per row, half the columns each)
+  // ---- features of row r (four threads per row, groups of four columns
+  // dealt round robin)
   {
-    const int r = t & (kSeedTcRows - 1), half = t >> 7;
+    constexpr int TPR = kSeedTcThreads / kSeedTcRows;
+    const int r = t & (kSeedTcRows - 1), part = t >> 7;
     const int e = row0 + r;
     const bool live = r < rows && u_ok;
     float rinv = 1.0f;
@@ -233,21 +235,21 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
       rinv = (float)(1.0 / rho);
       const int lev = a.elem_level ? a.elem_level[e] : 0;
       cdt = a.dt[kScalDtDx + 3 * lev];
-      if (half == 0) {
+      if (part == 0) {
         rowscale[r] = rho * cdt;
         rowscale_f[r] = (float)(rho * cdt);
       }
-    } else if (half == 0) {
+    } else if (part == 0) {
       rowscale[r] = 0.0;
       rowscale_f[r] = 0.0f;
     }
-    constexpr int HK = K1 / 2;
 #pragma unroll
-    for (int k0 = 0; k0 < HK; k0 += 4) {
+    for (int g = part; g < K1 / 4; g += TPR) {
+      const int k0 = 4 * g;
       float v[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const int f = half * HK + k0 + i;
+        const int f = k0 + i;
         float x = 0.0f;
         if (live && f < NIN) {
           if (f < Q * NP_S) {
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
         }
         v[i] = tc::to_tf32(x);
       }
-      *reinterpret_cast<float4*>(act + tc::kmajor_off(r, half * HK + k0, K1)) = make_float4(v[0], v[1], v[2], v[3]);
+      *reinterpret_cast<float4*>(act + tc::kmajor_off(r, k0, K1)) = make_float4(v[0], v[1], v[2], v[3]);
     }
   }
   tc::fence_proxy_async();  // generic reads of buffer 1 and writes of act before the async proxy
@@ -276,7 +278,7 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
   bool ok = all_u;
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
   const int r = (warp & 3) * 32 + (t & 31);  // this thread's row in the epilogues
-  const int chalf = warp >> 2;                // and its half of the columns
+  const int cq = warp >> 2;                   // and its quarter of the columns
 #pragma unroll 1
   for (int L = 0; L < 4 && ok; ++L) {
     const int wb = L & 1;
@@ -323,9 +325,8 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
     if (L < 3) {
       // hidden epilogue: bias + GELU, back to shared memory as the next A operand
       const float* b = a.bias[L];
-#pragma unroll 1
-      for (int c = 0; c < 2; ++c) {
-        const int col0 = chalf * 64 + c * 32;
+      {
+        const int col0 = cq * 32;
         float v[32];
         tc::tmem_ld32(tmem + lane_base + (uint32_t)col0, v);
 #pragma unroll
@@ -344,10 +345,9 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
     } else {
       // output layer: stage Y + b (rows x N4, padded stride) in the free act buffer
       const float* b = a.bias[3];
-      constexpr int HN = N4 / 2;  // a multiple of 8
-#pragma unroll
-      for (int c = 0; c < HN; c += 8) {
-        const int col0 = chalf * HN + c;
+#pragma unroll 1
+      for (int g = cq; g < N4 / 8; g += 4) {  // groups of 8 columns dealt round robin
+        const int col0 = 8 * g;
         float v[8];
         tc::tmem_ld8(tmem + lane_base + (uint32_t)col0, v);
 #pragma unroll
