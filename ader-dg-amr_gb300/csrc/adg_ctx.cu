@@ -2051,7 +2051,10 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base, cudaEvent_t
   pa.fb_list = ctx->fb_list.p;
   pa.fb_count = ctx->fb_count.p;
   pa.sweeps = ctx->seed_sweeps;
-  e = ks->predictor(pa, ctx->E, st, ctx->seed_mode);
+  // the FP32 predictor at D = 2 runs one-warp blocks (8 elements): 16 of them
+  // per SM, so the element groups spread evenly over the SMs
+  const int Es = ctx->seed_mode == 2 && ctx->cfg.D == 2 ? 8 : ctx->E;
+  e = ks->predictor(pa, Es, st, ctx->seed_mode);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "seeded predictor");
   // full FP64 Picard for the rejected elements; in a mode-2 step with the
   // seeded elements' final stage (mode 3), so that every trace tile is a split tile

@@ -33,15 +33,42 @@ constexpr size_t smem_bytes() {
 template <int E, int MODE>
 cudaError_t launch_predictor_mode(const PredictorArgs& a, cudaStream_t s) {
   constexpr size_t smem = smem_bytes<E, MODE>();
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_predictor<O, E, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
+  if (a.elem_list) {  // fallback pass (modes 0 and 3): two blocks per SM stride over the list
+    if constexpr (MODE == 0 || MODE == 3) {
+      static bool attr = false;
+      if (!attr) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k_predictor_list<O, E, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+      }
+      int dev = 0, sms = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        sms = 152;
+      int grid = (a.n_elem + E - 1) / E;
+      if (grid > 2 * sms) grid = 2 * sms;
+      if (grid <= 0) return cudaSuccess;
+      k_predictor_list<O, E, MODE><<<grid, E * O::Q, smem, s>>>(a);
+      return cudaGetLastError();
+    } else {
+      return cudaErrorInvalidValue;
+    }
   }
-  const int grid = (a.n_elem + E - 1) / E;
-  k_predictor<O, E, MODE><<<grid, E * O::Q, smem, s>>>(a);
-  return cudaGetLastError();
+  if constexpr (MODE == 3) {
+    return cudaErrorInvalidValue;  // mode 3 runs on element lists only
+  } else {
+    static bool attr = false;
+    if (!attr) {
+      cudaError_t e = cudaFuncSetAttribute(k_predictor<O, E, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+    const int grid = (a.n_elem + E - 1) / E;
+    if (grid <= 0) return cudaSuccess;
+    k_predictor<O, E, MODE><<<grid, E * O::Q, smem, s>>>(a);
+    return cudaGetLastError();
+  }
 }
 
 template <int E>

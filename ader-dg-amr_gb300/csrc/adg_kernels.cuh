@@ -440,7 +440,8 @@ __device__ __forceinline__ void split_faces(const double* u, const float* dlt, d
 
 template <class O, int E>
 __device__ __forceinline__ void split_epilogue(const double* u, const float* dlt, const double* c, double gm1,
-                                               double* sm, int col, int q, bool live, int e, const PredictorArgs& a) {
+                                               double* sm, int col, int q, bool live, int e, int e0, int limit,
+                                               const PredictorArgs& a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NS = O::NQ_S, NF = 2 * D;
   constexpr int LD = E * Q + 1;
   double* us64 = sm;  // U, then F_0(U) in place
@@ -476,19 +477,21 @@ __device__ __forceinline__ void split_epilogue(const double* u, const float* dlt
   float* ds32 = reinterpret_cast<float*>(sm);
   float* fb32 = ds32 + NS * LD;
   delta_slices<O, E, 0>(dlt, us32, ds32, fb32, col, (float)gm1);
-  {
-    float w[NP_S];
+  {  // summed over the directions in FP32, one conversion per mode
+    float w[NP_S], ws[NP_S];
     O::template vol_term_sp<0, float>(ColInT<float>{fb32 + col, LD}, RegOutT<float>{w});
 #pragma unroll
-    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[0], (double)w[n], R[n]);
+    for (int n = 0; n < NP_S; ++n) ws[n] = (float)c[0] * w[n];
     O::template vol_term_sp<1, float>(ColInT<float>{fb32 + NS * LD + col, LD}, RegOutT<float>{w});
 #pragma unroll
-    for (int n = 0; n < NP_S; ++n) R[n] = fma(c[1], (double)w[n], R[n]);
+    for (int n = 0; n < NP_S; ++n) ws[n] = fmaf((float)c[1], w[n], ws[n]);
     if constexpr (D == 3) {
       O::template vol_term_sp<2, float>(ColInT<float>{fb32 + 2 * NS * LD + col, LD}, RegOutT<float>{w});
 #pragma unroll
-      for (int n = 0; n < NP_S; ++n) R[n] = fma(c[2], (double)w[n], R[n]);
+      for (int n = 0; n < NP_S; ++n) ws[n] = fmaf((float)c[2], w[n], ws[n]);
     }
+#pragma unroll
+    for (int n = 0; n < NP_S; ++n) R[n] += (double)ws[n];
   }
   if (live) {
     double* dst = a.Rvol + ((size_t)e * Q + q) * NP_S;
@@ -497,8 +500,6 @@ __device__ __forceinline__ void split_epilogue(const double* u, const float* dlt
   }
   __syncthreads();
   // face traces, one direction at a time
-  const int e0 = blockIdx.x * E;
-  const int limit = a.elem_list ? *a.list_count : a.n_elem;
   double* tr_elem = live ? a.Tr + (size_t)e * NF * tr_tile<O>() : nullptr;
   split_faces<O, E, 0>(u, dlt, sm, col, q, tr_elem, a, e0, limit);
   split_faces<O, E, 1>(u, dlt, sm, col, q, tr_elem, a, e0, limit);
@@ -509,7 +510,8 @@ __device__ __forceinline__ void split_epilogue(const double* u, const float* dlt
 // traces of the final H_w.
 template <class O, int E>
 __device__ __forceinline__ void fp64_epilogue(const double* hw, const double* u, const double* c, double gm1,
-                                              double* sm, int col, int q, bool live, int e, const PredictorArgs& a) {
+                                              double* sm, int col, int q, bool live, int e, int e0, int limit,
+                                              const PredictorArgs& a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NS = O::NQ_S;
   constexpr int LD = E * Q + 1;
   // ---- corrector volume term (AmrDG.tpp:696-709): M U + sum_d c_d Sk_corr[d] F_d,
@@ -543,8 +545,6 @@ __device__ __forceinline__ void fp64_epilogue(const double* hw, const double* u,
 
   // ---- face traces of H (AmrDG.tpp:437-493) and face physics (AmrDG.h:1207-1251),
   // the two faces of one direction at a time
-  const int e0 = blockIdx.x * E;
-  const int limit = a.elem_list ? *a.list_count : a.n_elem;
   face_traces<O, E, 0>(hw, sm, col, LD, a, e0, limit);
   face_traces<O, E, 1>(hw, sm, col, LD, a, e0, limit);
   if constexpr (D == 3) face_traces<O, E, 2>(hw, sm, col, LD, a, e0, limit);
@@ -563,28 +563,23 @@ constexpr int predictor_min_blocks() {
   return MODE == 2 && 16 / warps > 0 ? 16 / warps : 1;
 }
 
-template <class O, int E, int MODE = 0>
-__global__ void __launch_bounds__(E * O::Q, (predictor_min_blocks<E, O::Q, MODE>()))
-    k_predictor(PredictorArgs a) {
+// One group of E elements (positions chunk E .. chunk E + E - 1 of the
+// element range or list, limit = its length).
+template <class O, int E, int MODE>
+__device__ __forceinline__ void predictor_chunk(const PredictorArgs& a, double* sm, int chunk, int limit) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NP_ST = O::NP_ST;
   constexpr int NQ = O::NQ_ST, NI = O::NQ_INIT;
   constexpr int NCOL = E * Q;
   constexpr int LD = NCOL + 1;  // odd stride: conflict-free point-major access
-  extern __shared__ double sm[];
 
   const int col = threadIdx.x;
   const int el = col / Q;
   const int q = col % Q;
-  int e_raw = blockIdx.x * E + el;
-  bool live = e_raw < a.n_elem;
-  if (a.elem_list) {
-    const int cnt = *a.list_count;
-    if (a.count_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.count_total, (unsigned long long)cnt);
-    if ((int)(blockIdx.x * E) >= cnt) return;  // whole block idle
-    live = e_raw < cnt;
-    e_raw = live ? a.elem_list[e_raw] : a.elem_list[cnt - 1];
-  }
-  const int e = live ? e_raw : (a.elem_list ? e_raw : (a.n_elem - 1));
+  const int e0 = chunk * E;
+  int e_raw = e0 + el;
+  const bool live = e_raw < limit;
+  if (a.elem_list) e_raw = a.elem_list[live ? e_raw : limit - 1];
+  const int e = live || a.elem_list ? e_raw : limit - 1;
   const int lev = a.elem_level ? a.elem_level[e] : 0;
   double c[D];
 #pragma unroll
@@ -724,10 +719,31 @@ __global__ void __launch_bounds__(E * O::Q, (predictor_min_blocks<E, O::Q, MODE>
     if constexpr (MODE == 3)
 #pragma unroll
       for (int n = 0; n < NP_ST; ++n) dlt[n] = (float)(hw[n] - wu[n]);
-    split_epilogue<O, E>(u, dlt, c, gm1, sm, col, q, live, e, a);
+    split_epilogue<O, E>(u, dlt, c, gm1, sm, col, q, live, e, e0, limit, a);
   } else {
-    fp64_epilogue<O, E>(hw, u, c, gm1, sm, col, q, live, e, a);
+    fp64_epilogue<O, E>(hw, u, c, gm1, sm, col, q, live, e, e0, limit, a);
   }
+}
+
+// The kernels: one element group per block over the element range
+// (k_predictor), or a short grid striding over the groups of an element
+// list whose length is known only on the device (k_predictor_list, the
+// fallback pass).  Every phase of a group ends with a barrier, so the next
+// group may reuse the shared memory.
+template <class O, int E, int MODE = 0>
+__global__ void __launch_bounds__(E * O::Q, (predictor_min_blocks<E, O::Q, MODE>()))
+    k_predictor(PredictorArgs a) {
+  extern __shared__ double sm[];
+  predictor_chunk<O, E, MODE>(a, sm, blockIdx.x, a.n_elem);
+}
+
+template <class O, int E, int MODE>
+__global__ void __launch_bounds__(E * O::Q) k_predictor_list(PredictorArgs a) {
+  extern __shared__ double sm[];
+  const int limit = *a.list_count;
+  if (a.count_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.count_total, (unsigned long long)limit);
+#pragma unroll 1
+  for (int chunk = blockIdx.x; chunk * E < limit; chunk += gridDim.x) predictor_chunk<O, E, MODE>(a, sm, chunk, limit);
 }
 
 // N consecutive doubles to registers (and back): 16-byte accesses when every
