@@ -131,6 +131,7 @@ struct adg_ctx {
   long long dof_updates = 0;  // sum over steps of valid elements * Q * Np_s
   long long leaf_dof_updates = 0;  // the same over leaf (uncovered) elements
   size_t n_leaf = 0;               // leaf elements of the current layout
+  bool ghosts_stale = false;       // a coarse level's state was set since the last ghost fill
   double regrid_ms = 0.0;     // host wall time spent in regrids
   bool first_step = true;
   int n_regrids = 0;
@@ -366,7 +367,11 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base, cudaEvent_t
 namespace {
 
 // ADER of every level with the current device Dt (AmrDG.h:1071-1165).
+int flush_ghosts(adg_ctx* ctx);
+
 int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
+  int rc0 = flush_ghosts(ctx);
+  if (rc0) return rc0;
   const Hierarchy& H = ctx->hier;
   const KernelSet* ks = ctx->ks;
   const int D = ctx->cfg.D;
@@ -451,6 +456,15 @@ int launch_ghost_fill(adg_ctx* ctx) {
   return ADG_OK;
 }
 
+// The coarse-fine ghosts after adg_set_state: filled once, before the next
+// kernel that reads them (predictor, limiter, tags), however many levels were
+// set in between.
+int flush_ghosts(adg_ctx* ctx) {
+  if (!ctx->ghosts_stale) return ADG_OK;
+  ctx->ghosts_stale = false;
+  return ctx->hier.nlevels() > 1 ? launch_ghost_fill(ctx) : ADG_OK;
+}
+
 int launch_average_down(adg_ctx* ctx) {
   const Hierarchy& H = ctx->hier;
   if (H.nlevels() <= 1) return ADG_OK;
@@ -471,8 +485,8 @@ int launch_amr_sync(adg_ctx* ctx) {
   return ctx->hier.nlevels() > 1 ? launch_ghost_fill(ctx) : ADG_OK;
 }
 
-// Dt from the current state; advance_time adds the old Dt to t first.
-int launch_dt(adg_ctx* ctx, int advance_time) {
+// Arguments of the Dt reduction; advance_time adds the old Dt to t first.
+DtArgs dt_args(adg_ctx* ctx, int advance_time) {
   const Hierarchy& H = ctx->hier;
   DtArgs da{};
   da.Uw = ctx->Uw.p;
@@ -493,14 +507,22 @@ int launch_dt(adg_ctx* ctx, int advance_time) {
   da.c_dt = ctx->cfg.c_dt;
   da.advance_time = advance_time;
   da.D = ctx->cfg.D;
-  cudaError_t e = ctx->ks->dt_reduce(da, ctx->stream);
+  return da;
+}
+
+// Dt from the current state; advance_time adds the old Dt to t first.
+int launch_dt(adg_ctx* ctx, int advance_time) {
+  cudaError_t e = ctx->ks->dt_reduce(dt_args(ctx, advance_time), ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "dt launch");
   ctx->launches += 1;
   return ADG_OK;
 }
 
+
 // TVB limiter of the finest level (AmrDG.h:990-997, 1657-1855).
 int launch_limiter(adg_ctx* ctx) {
+  int rc0 = flush_ghosts(ctx);
+  if (rc0) return rc0;
   const Hierarchy& H = ctx->hier;
   const int F = H.nlevels() - 1;
   const LevelGeom g = level_geom(ctx);
@@ -805,6 +827,8 @@ int capture_graph(adg_ctx* ctx) {
 // The step's kernels on the current layout: the captured graph (updated or
 // re-captured after a layout change) or direct launches.
 int launch_one_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
+  int rc0 = flush_ghosts(ctx);  // outside the graph
+  if (rc0) return rc0;
   if (use_graph && !ev) {
     if (!ctx->graph_exec || ctx->graph_stale) {
       auto t0 = std::chrono::steady_clock::now();
@@ -833,7 +857,8 @@ void count_step(adg_ctx* ctx) {
 // timing path regrid synchronously.
 int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
   if (ctx->cfg.limiter_t > 1) use_graph = false;  // the step's kernels then differ from step to step
-  int rc = ADG_OK;
+  int rc = flush_ghosts(ctx);  // the regrid's tags read them
+  if (rc) return rc;
   if (regrid_due(ctx) && !ctx->first_step && !ev) {
     auto t0 = std::chrono::steady_clock::now();
     size_t nt = 0;
@@ -1142,10 +1167,7 @@ int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem) {
   ADG_CUDA(cudaMemcpyAsync(ctx->Uw.p + off, src, cnt * sizeof(double),
                            mem == ADG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream),
            "set_state copy");
-  if (lev + 1 < ctx->hier.nlevels()) {  // the finer level's ghosts project from this level
-    rc = launch_ghost_fill(ctx);
-    if (rc) return rc;
-  }
+  if (lev + 1 < ctx->hier.nlevels()) ctx->ghosts_stale = true;  // the finer level's ghosts project from this level
   if (mem != ADG_MEM_HOST_ASYNC) ADG_CUDA(cudaStreamSynchronize(ctx->stream), "set_state sync");
   return ADG_OK;
 }
@@ -1408,6 +1430,8 @@ int adg_tags(adg_ctx* ctx, int lev, uint8_t* out) {
   if (rc) return rc;
   const Hierarchy& H = ctx->hier;
   if (!out || lev < 0 || lev >= H.nlevels()) return fail(ctx, ADG_ERR_ARG, "bad level");
+  rc = flush_ghosts(ctx);
+  if (rc) return rc;
   ADG_CUDA(ctx->tags.ensure(H.n_valid()), "alloc tags");
   TagArgs ta{};
   ta.Uw = ctx->Uw.p;
@@ -1494,6 +1518,7 @@ int adg_average_down(adg_ctx* ctx) {
 int adg_fill_ghosts(adg_ctx* ctx) {
   int rc = check_ready(ctx);
   if (rc) return rc;
+  ctx->ghosts_stale = false;
   if (ctx->hier.nlevels() > 1) {
     rc = launch_ghost_fill(ctx);
     if (rc) return rc;

@@ -126,7 +126,9 @@ struct Impl final : KernelSet {
   }
   cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const override {
     const long long n = ((long long)a.n_valid + (a.rec_of_elem ? a.nrec : 0)) * O::Q;
-    const int bs = 128;
+    // one-warp blocks: at its ~130 registers an SM holds 15 of them, so the
+    // columns of ~16k elements run in one wave instead of 1.2
+    const int bs = 32;
     k_corrector<O><<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(a);
     return cudaGetLastError();
   }

@@ -1552,8 +1552,7 @@ __global__ void k_interp_scatter(const double* coarse, const int8_t* child, long
   constexpr int Q = O::Q, NP_S = O::NP_S;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * Q) return;
-  const long long i = t / Q;
-  const int q = (int)(t % Q);
+  const long long i = t / Q;  // cell; variable t % Q
   double out[NP_S];
   const int l = child[i];
 #pragma unroll
