@@ -97,7 +97,10 @@ int adg_set_stream(adg_ctx* ctx, void* cuda_stream);
 int adg_init(adg_ctx* ctx);
 
 /* Level state in/out: n_cells * Q * Np_s doubles, element-major, cells in
- * x-fastest order over the level's valid cells. */
+ * x-fastest order over the level's valid cells.  Setting a level that has a
+ * finer level makes that level's coarse-fine ghosts stale; they are projected
+ * again once, before the next kernel that reads them (a step, adg_ader,
+ * adg_predictor, adg_tags) or by adg_fill_ghosts. */
 int adg_num_levels(const adg_ctx* ctx, int* nlev);
 int adg_level_cells(const adg_ctx* ctx, int lev, int64_t* ncells);
 int adg_get_state(adg_ctx* ctx, int lev, double* dst, int mem);
