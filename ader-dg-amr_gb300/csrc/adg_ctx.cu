@@ -2077,7 +2077,8 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base, cudaEvent_t
   pa.fb_count = ctx->fb_count.p;
   pa.sweeps = ctx->seed_sweeps;
   // the FP32 predictor at D = 2 runs one-warp blocks (8 elements): 16 of them
-  // per SM, so the element groups spread evenly over the SMs
+  // per SM, so the element groups spread evenly over the SMs (at D = 3 the
+  // 40-thread blocks of 8 elements idle 3/8 of their lanes: the tuned E stays)
   const int Es = ctx->seed_mode == 2 && ctx->cfg.D == 2 ? 8 : ctx->E;
   e = ks->predictor(pa, Es, st, ctx->seed_mode);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "seeded predictor");

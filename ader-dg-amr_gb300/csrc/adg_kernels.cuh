@@ -439,7 +439,8 @@ __device__ __forceinline__ void split_faces(const double* u, const float* dlt, d
 }
 
 template <class O, int E>
-__device__ __forceinline__ void split_epilogue(const double* u, const float* dlt, const double* c, double gm1,
+__device__ __forceinline__ void split_epilogue(const double* u, const float* uf, const float* dlt, const double* c,
+                                               double gm1,
                                                double* sm, int col, int q, bool live, int e, int e0, int limit,
                                                const PredictorArgs& a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NS = O::NQ_S, NF = 2 * D;
@@ -448,10 +449,10 @@ __device__ __forceinline__ void split_epilogue(const double* u, const float* dlt
   double* fU64 = sm;  // F_d(U) in slab d
   float* us32 = reinterpret_cast<float*>(sm + D * NS * LD);
 
-  // U at the spatial points (FP64, and in FP32 for the flux changes)
+  // U at the spatial points (FP64, and in FP32 from the FP32 modes uf for
+  // the flux changes)
   O::sp_eval(RegIn{u}, ColOut{us64 + col, LD});
-#pragma unroll
-  for (int m = 0; m < NS; ++m) us32[m * LD + col] = (float)us64[m * LD + col];
+  O::template sp_eval<float>(RegInT<float>{uf}, ColOutT<float>{us32 + col, LD});
   __syncthreads();
   // F(U) at the spatial points (FP64)
   flux_stage<O, E, NS, double>(us64, LD, gm1);
@@ -596,6 +597,7 @@ __device__ __forceinline__ void predictor_chunk(const PredictorArgs& a, double* 
   O::wu(RegIn{u}, RegOut{wu});
   double hw[NP_ST];
   float dlt[NP_ST];  // MODES 2, 3: H_w - W U in FP32
+  float uf[NP_S];    // MODES 2, 3: U_w in FP32
 
   if constexpr (MODE == 0 || MODE == 3) {
     // ---- sweep 1: the reference's initial guess H_w = [U_w, 0, ...]
@@ -673,7 +675,9 @@ __device__ __forceinline__ void predictor_chunk(const PredictorArgs& a, double* 
 #pragma unroll
         for (int n = 0; n < NP_ST; ++n) hf[n] = (float)a.Hseed[hoff + n];
       }
-      O::template wu<float>(RegIn{u}, RegOutT<float>{wf});
+#pragma unroll
+      for (int n = 0; n < NP_S; ++n) uf[n] = (float)u[n];
+      O::template wu<float>(RegInT<float>{uf}, RegOutT<float>{wf});
 #pragma unroll
       for (int d = 0; d < D; ++d) cf[d] = (float)c[d];
       float resf = 0.0f;
@@ -716,10 +720,13 @@ __device__ __forceinline__ void predictor_chunk(const PredictorArgs& a, double* 
     for (int n = 0; n < NP_ST; ++n) dst[n] = MODE == 2 ? wu[n] + (double)dlt[n] : hw[n];
   }
   if constexpr (MODE == 2 || MODE == 3) {
-    if constexpr (MODE == 3)
+    if constexpr (MODE == 3) {
 #pragma unroll
       for (int n = 0; n < NP_ST; ++n) dlt[n] = (float)(hw[n] - wu[n]);
-    split_epilogue<O, E>(u, dlt, c, gm1, sm, col, q, live, e, e0, limit, a);
+#pragma unroll
+      for (int n = 0; n < NP_S; ++n) uf[n] = (float)u[n];
+    }
+    split_epilogue<O, E>(u, uf, dlt, c, gm1, sm, col, q, live, e, e0, limit, a);
   } else {
     fp64_epilogue<O, E>(hw, u, c, gm1, sm, col, q, live, e, e0, limit, a);
   }
