@@ -2026,6 +2026,8 @@ int seed_infer(adg_ctx* ctx, double* dst, int path, float* dst_f = nullptr) {
     for (int L = 0; L < 4; ++L) {
       ta.w_off[L] = sd->w_off[L];
       ta.bias[L] = sd->params.p + sd->off[2 * L + 1];
+      if (L < 3 && (reinterpret_cast<uintptr_t>(ta.bias[L]) & 15u))  // read as float4 by the epilogues
+        return fail(ctx, ADG_ERR_ARG, "seed biases not 16-byte aligned");
     }
     ta.x_mean = sd->x_mean.p;
     ta.x_istd = sd->x_istd.p;

@@ -104,14 +104,14 @@ __device__ __forceinline__ float to_tf32(float x) {
   return __uint_as_float(r);
 }
 
-// GELU with tanh(y) = 1 - 2 / (exp(2y) + 1) on the fast exponential and
-// reciprocal; |y| clamped to 15 where tanh is 1 in FP32.  Its error (~1e-7)
-// is far below the TF32 rounding of the activations that follows.
+// GELU in its logistic form 0.5 z (1 + tanh y) = z / (1 + exp(-2y)) on the
+// fast exponential and reciprocal; |y| clamped to 15, where tanh is 1 in
+// FP32.  Its error (~1e-7) is far below the TF32 rounding of the
+// activations that follows.
 __device__ __forceinline__ float gelu_fast(float z) {
-  float y = mlp::kGeluK * (z + mlp::kGeluA * z * z * z);
+  float y = mlp::kGeluK * fmaf(mlp::kGeluA * z, z * z, z);
   y = fminf(fmaxf(y, -15.0f), 15.0f);
-  const float th = 1.0f - __fdividef(2.0f, __expf(2.0f * y) + 1.0f);
-  return 0.5f * z * (1.0f + th);
+  return __fdividef(z, 1.0f + __expf(-2.0f * y));
 }
 
 // Float offset of (row, k) in the canonical K-major layout of a matrix with K
@@ -331,11 +331,14 @@ __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs 
         tc::tmem_ld32(tmem + lane_base + (uint32_t)col0, v);
 #pragma unroll
         for (int i = 0; i < 32; i += 4) {
+          // biases 16-byte aligned (their offsets in the packed parameters are
+          // multiples of 4 floats at hidden width 128; checked by the launcher)
+          const float4 bb = __ldg(reinterpret_cast<const float4*>(b + col0 + i));
           float4 o;
-          o.x = tc::to_tf32(tc::gelu_fast(v[i + 0] + __ldg(b + col0 + i + 0)));
-          o.y = tc::to_tf32(tc::gelu_fast(v[i + 1] + __ldg(b + col0 + i + 1)));
-          o.z = tc::to_tf32(tc::gelu_fast(v[i + 2] + __ldg(b + col0 + i + 2)));
-          o.w = tc::to_tf32(tc::gelu_fast(v[i + 3] + __ldg(b + col0 + i + 3)));
+          o.x = tc::to_tf32(tc::gelu_fast(v[i + 0] + bb.x));
+          o.y = tc::to_tf32(tc::gelu_fast(v[i + 1] + bb.y));
+          o.z = tc::to_tf32(tc::gelu_fast(v[i + 2] + bb.z));
+          o.w = tc::to_tf32(tc::gelu_fast(v[i + 3] + bb.w));
           *reinterpret_cast<float4*>(act + tc::kmajor_off(r, col0 + i, H)) = o;
         }
       }
