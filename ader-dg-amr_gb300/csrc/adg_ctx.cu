@@ -598,18 +598,18 @@ int regrid_tags(adg_ctx* ctx, size_t* nt_out) {
   const int max_crse = std::min(F, ctx->cfg.max_level - 1);
   const size_t nt = H.level_valid_offset(max_crse) + H.level_valid_count(max_crse);
   ADG_CUDA(ctx->tags.ensure(nt), "alloc tags");
-  for (int l = 0; l <= max_crse; ++l) {
+  {  // the valid elements of levels 0 .. max_crse are contiguous: one launch
     TagArgs ta{};
     ta.Uw = ctx->Uw.p;
     ta.elem_face = ctx->elem_face.p;
     ta.face_left = ctx->face_left.p;
     ta.face_right = ctx->face_right.p;
-    ta.e0 = (int)H.level_valid_offset(l);
-    ta.n = (int)H.level_valid_count(l);
+    ta.e0 = 0;
+    ta.n = (int)nt;
     ta.kind = ctx->cfg.tag_kind;
     ta.threshold = ctx->cfg.tag_threshold;
     ta.gamma = ctx->cfg.gamma;
-    ta.tags = ctx->tags.p + H.level_valid_offset(l);
+    ta.tags = ctx->tags.p;
     cudaError_t e = ks->tag(ta, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "tag launch");
     ctx->launches++;
