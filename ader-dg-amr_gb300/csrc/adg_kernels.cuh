@@ -608,15 +608,19 @@ __device__ __forceinline__ void predictor_chunk(const PredictorArgs& a, double* 
     __syncthreads();
   #pragma unroll
     for (int n = 0; n < NP_ST; ++n) hw[n] = wu[n];
-    {
+    {  // (A_0 F = 0 here: the initial guess, and so its flux, does not depend on x_0)
       double y[NP_ST];
-      O::template proj_init<0>(ColIn{sm + col, LD}, RegOut{y});
+      if constexpr (!O::proj_init_zero(0)) {
+        O::template proj_init<0>(ColIn{sm + col, LD}, RegOut{y});
   #pragma unroll
-      for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[0], y[n], hw[n]);
-      O::template proj_init<1>(ColIn{sm + NI * LD + col, LD}, RegOut{y});
+        for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[0], y[n], hw[n]);
+      }
+      if constexpr (!O::proj_init_zero(1)) {
+        O::template proj_init<1>(ColIn{sm + NI * LD + col, LD}, RegOut{y});
   #pragma unroll
-      for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[1], y[n], hw[n]);
-      if constexpr (D == 3) {
+        for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[1], y[n], hw[n]);
+      }
+      if constexpr (D == 3 && !O::proj_init_zero(2)) {
         O::template proj_init<2>(ColIn{sm + 2 * NI * LD + col, LD}, RegOut{y});
   #pragma unroll
         for (int n = 0; n < NP_ST; ++n) hw[n] = fma(-c[2], y[n], hw[n]);
@@ -1538,7 +1542,7 @@ __global__ void k_average_down(double* Uw, const int* rec, int nrec) {
     for (int n = 0; n < NP_S; ++n) {
       double sum = 0.0;
 #pragma unroll
-      for (int l = 0; l < NOV; ++l) sum += part[l][n][x];
+      for (int l = 0; l < NOV; ++l) sum = __dadd_rn(sum, part[l][n][x]);  // as k_interp_gather
       out[r * EL + q * NP_S + n] = (1.0 / NOV) * (O::minv(n) * sum);
     }
   }
@@ -1600,7 +1604,7 @@ __global__ void k_interp_gather(const double* fine, long long n, double* coarse)
   for (int k = 0; k < NP_S; ++k) {
     double sum = 0.0;
 #pragma unroll
-    for (int l = 0; l < NOV; ++l) sum += part[l][k];
+    for (int l = 0; l < NOV; ++l) sum = __dadd_rn(sum, part[l][k]);  // never fused with a child's last product
     coarse[(size_t)t * NP_S + k] = (1.0 / NOV) * (O::minv(k) * sum);
   }
 }

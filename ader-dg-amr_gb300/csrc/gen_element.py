@@ -993,12 +993,54 @@ def add_face_moment_ops(el, ops):
     return len(mom)
 
 
+# Coefficients below DENOISE_REL of a stage's largest are the rounding residue
+# of exact zeros: the matrices built by quadrature on the double-valued node
+# and weight tables (P_cf, P_fc, the Gram inverse inside C_d) carry entries of
+# 1e-17 .. 1e-34 where the exact projections between Legendre bases are zero
+# (their true entries are rationals of order 1e-3 .. 1e2).  They are dropped,
+# and an operator whose whole product is below DENOISE_REL of its norm bound
+# (the product of its stages' largest row sums) is zero: it is emitted with no
+# arithmetic and reported in ZERO_OPS.  Every operator is checked against its
+# dense matrix again, to DENOISE_REL of the norm bound.
+DENOISE_REL = 1e-13
+
+
+def norm_bound(stages):
+    b = 1.0
+    for st in stages:
+        b *= max((sum(abs(v) for _, v in r) for r in st.rows), default=0.0)
+    return b
+
+
+def denoise(ops):
+    zero = set()
+    for name, (stages, n_in, n_out) in list(ops.items()):
+        before = chain_dense(stages)
+        bound = norm_bound(stages)
+        if bound > 0 and max(abs(x) for r in before for x in r) < DENOISE_REL * bound:
+            ops[name] = ([Stage(n_in, n_out, [[] for _ in range(n_out)])], n_in, n_out)
+            zero.add(name)
+            continue
+        clean = []
+        for st in stages:
+            mx = max((abs(v) for r in st.rows for _, v in r), default=0.0)
+            clean.append(Stage(st.n_in, st.n_out, [[(c, v) for c, v in r if abs(v) >= DENOISE_REL * mx]
+                                                   for r in st.rows]))
+        after = chain_dense(clean)
+        err = max(abs(after[i][j] - before[i][j]) for i in range(len(before)) for j in range(len(before[0])))
+        if err > DENOISE_REL * bound:
+            raise SystemExit(f"denoised {name} moved by {err} (bound {bound})")
+        ops[name] = (clean, n_in, n_out)
+    return zero
+
+
 def generate(D, P, out_path):
     el = Element(D, P)
     ops = build_ops(el)
     add_ic_proj(el, ops)
     add_amr_ops(el, ops)
     n_mom = add_face_moment_ops(el, ops)
+    zero_ops = denoise(ops)
     N = P + 1
     qst = N ** (D + 1)
     qbd = N ** D
@@ -1059,6 +1101,10 @@ def generate(D, P, out_path):
     hdr.append(disp("face_eval_sp", [((d, s), f"face_eval_sp{d}{s}") for d in range(D) for s in range(2)],
                     ["d", "s"]))
     hdr.append(disp("cproj", [((d,), f"cproj{d}") for d in range(D)], ["d"]))
+    # proj_init[d] is zero when the flux of the first sweep's initial guess
+    # (independent of x_0) is projected with the x_0 derivative: A_0 F = 0
+    hdr.append("  static constexpr __host__ __device__ bool proj_init_zero(int d) { return "
+               + " || ".join([f"d == {d}" for d in range(D) if f"proj_init{d}" in zero_ops] or ["false"]) + "; }")
     # space-time mode n = (spatial mode st_space(n), time degree st_time(n));
     # time_val(a, k) = P_a(t_k)
     # (constexpr selections rather than arrays, which device code cannot
@@ -1093,7 +1139,9 @@ def generate(D, P, out_path):
     slices_cost = N * sum(counts[f"face_slice{d}{s}"] for d in range(D) for s in range(2))
     modes_cost = sum(counts[f"face_eval{d}{s}"] for d in range(D) for s in range(2))
     nsb = N ** (D - 1)
-    per_col = (counts["wu"] + counts["vol_eval_init"] + sum(counts[f"proj_init{d}"] for d in range(D)) + 2 * D * el.Np_st
+    nz_init = sum(1 for d in range(D) if f"proj_init{d}" not in zero_ops)  # projections the first sweep runs
+    per_col = (counts["wu"] + counts["vol_eval_init"] + sum(counts[f"proj_init{d}"] for d in range(D))
+               + 2 * nz_init * el.Np_st
                + (sweeps - 1) * (counts["vol_eval"] + sum(counts[f"proj{d}"] for d in range(D)) + 2 * D * el.Np_st)
                + counts["vol_eval"] + sum(counts[f"vol_term{d}"] for d in range(D))
                + min(slices_cost, modes_cost)
