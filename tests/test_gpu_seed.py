@@ -224,6 +224,32 @@ def test_fp32_path_on_amr_conserves_mass_and_tracks_the_plain_path(quirk):
     assert dist(b) < 0.1 * dist(c), (dist(b), dist(c))
 
 
+@pytest.mark.parametrize("case", ["vortex_p1", "vortex_p2", "kh_p3", "vortex_p3_outflow", "blast3d_p1_per",
+                                  "blast3d_p2"])
+def test_fp32_path_runs_on_every_configuration(case):
+    """Mode 2 on every compiled (D, P), with an untrained network (its
+    corrections stay near W U, so the three FP32 sweeps carry the predictor):
+    the split final stage, split traces and split numerical flux give a
+    finite state, conserve mass on periodic domains, and track the plain
+    FP64 run to the Picard truncation of three sweeps."""
+    from parity import CASES
+    per = CASES[case][5]
+    a = make_gpu(case)
+    b = make_gpu(case)
+    seed = G.PredictorSeed(b.D, b.P, hidden=128, rng_seed=3)
+    seed.attach(b, mode=2, sweeps=3, tol=1e9)
+    m0 = b.get_U_w()[:, 0, 0].sum()
+    for _ in range(3):
+        a.time_integration()
+        b.time_integration()
+    ua, ub = a.get_U_w(), b.get_U_w()
+    assert np.all(np.isfinite(ub)) and b.status() == 0
+    if all(per[:b.D]):
+        assert abs(ub[:, 0, 0].sum() - m0) < 1e-12 * abs(m0)
+    scale = np.max(np.abs(ua[:, :, 0]))  # largest cell mean of any variable
+    assert np.max(np.abs(ub - ua)) < 1e-3 * scale, np.max(np.abs(ub - ua)) / scale
+
+
 def _seed_correction(H, U, s, seed):
     """(H - W U) / (rho_mean Dt/dx): the network's share of the seed."""
     import oracle_ffi as O
