@@ -230,24 +230,28 @@ def test_fp32_path_runs_on_every_configuration(case):
     """Mode 2 on every compiled (D, P), with an untrained network (its
     corrections stay near W U, so the three FP32 sweeps carry the predictor):
     the split final stage, split traces and split numerical flux give a
-    finite state, conserve mass on periodic domains, and track the plain
-    FP64 run to the Picard truncation of three sweeps."""
+    finite state, conserve mass on periodic domains, and stay as close to a
+    converged Picard run (8 FP64 sweeps) as the plain path's P sweeps from
+    the reference's initial guess do (closer where P < 3)."""
     from parity import CASES
     per = CASES[case][5]
-    a = make_gpu(case)
+    a = make_gpu(case)                   # plain: P sweeps
+    c = make_gpu(case, picard_sweeps=8)  # converged predictor
     b = make_gpu(case)
     seed = G.PredictorSeed(b.D, b.P, hidden=128, rng_seed=3)
     seed.attach(b, mode=2, sweeps=3, tol=1e9)
     m0 = b.get_U_w()[:, 0, 0].sum()
     for _ in range(3):
-        a.time_integration()
-        b.time_integration()
-    ua, ub = a.get_U_w(), b.get_U_w()
+        for s in (a, b, c):
+            s.time_integration()
+    ua, ub, uc = a.get_U_w(), b.get_U_w(), c.get_U_w()
     assert np.all(np.isfinite(ub)) and b.status() == 0
     if all(per[:b.D]):
         assert abs(ub[:, 0, 0].sum() - m0) < 1e-12 * abs(m0)
-    scale = np.max(np.abs(ua[:, :, 0]))  # largest cell mean of any variable
-    assert np.max(np.abs(ub - ua)) < 1e-3 * scale, np.max(np.abs(ub - ua)) / scale
+    scale = np.max(np.abs(uc[:, :, 0]))  # largest cell mean of any variable
+    d_seed = np.max(np.abs(ub - uc)) / scale
+    d_plain = np.max(np.abs(ua - uc)) / scale
+    assert d_seed <= 2.0 * d_plain + 1e-9, (d_seed, d_plain)
 
 
 def _seed_correction(H, U, s, seed):
