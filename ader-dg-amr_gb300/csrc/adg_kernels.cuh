@@ -304,10 +304,10 @@ __device__ __forceinline__ void face_traces(const double* hw, double* sm, int co
 // term is taken once, times the sum of the time weights) and at the NSB
 // spatial points of every face.  The time-dependent part is the FP32 change
 // of the flux F(U + delta) - F(U) (euler_dflux_*), whose rounding is
-// relative to the change; it is added to the FP64 part in modal space (the
-// volume term) or point by point (the traces).  The outputs are those of
-// final_volume_flux + face_traces: Rvol and the trace tiles of H, F_n, the
-// wave speed.
+// relative to the change; it is added to the FP64 part in modal space for
+// the volume term (Rvol), and kept apart in the split trace tiles (U and
+// f_n(U) in FP64, the changes of u and f_n and the wave speed in FP32) that
+// k_numflux_split reads.
 // ---------------------------------------------------------------------------
 
 // Shared memory of split_epilogue (doubles): region A = D NS ld doubles (U,
@@ -440,9 +440,8 @@ __device__ __forceinline__ void split_faces(const double* u, const float* dlt, d
 
 template <class O, int E>
 __device__ __forceinline__ void split_epilogue(const double* u, const float* uf, const float* dlt, const double* c,
-                                               double gm1,
-                                               double* sm, int col, int q, bool live, int e, int e0, int limit,
-                                               const PredictorArgs& a) {
+                                               double gm1, double* sm, int col, int q, bool live, int e, int e0,
+                                               int limit, const PredictorArgs& a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S, NS = O::NQ_S, NF = 2 * D;
   constexpr int LD = E * Q + 1;
   double* us64 = sm;  // U, then F_0(U) in place
