@@ -19,6 +19,9 @@ struct KernelSet {
   virtual ~KernelSet() = default;
   virtual std::vector<int> elems_per_block_choices() const = 0;
   virtual size_t predictor_smem(int E) const = 0;
+  // mode 0: FP64 Picard; 1 / 2: seeded, FP64 / FP32 sweeps; 3: FP64 Picard with
+  // mode 2's final stage (element lists only: the fallback of a mode-2 step).
+  // With a.elem_list set (modes 0 and 3) a short grid strides over the list.
   virtual cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s, int mode = 0) const = 0;
   // split: the trace tiles are split tiles (predictor modes 2 and 3)
   virtual cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s, bool split = false) const = 0;
