@@ -604,7 +604,11 @@ def run_ours(args, w):
     line = {
         "metric": METRIC, "value": value, "unit": "DOF-updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64" if head_name == "plain_fp64" else "f64+f32",
+        "dtype_detail": (None if head_name == "plain_fp64" else
+                         "FP64 state, corrector, numerical-flux moments and the time-independent part of the "
+                         "predictor; FP32 Picard sweeps and flux changes; TF32 tensor-core seed network"),
+        "data": "synthetic",
         "config": {**base_config(args, w, world), "path": head_name, "elems_per_block": E, "cuda_graph": True,
                    "l2": f"flushed before every timed step ({L2_FLUSH_BYTES >> 20} MiB device memset, outside "
                          "the per-step CUDA-event intervals that are summed)"},
