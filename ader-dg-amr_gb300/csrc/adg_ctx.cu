@@ -146,6 +146,9 @@ struct adg_ctx {
   DevBuf<unsigned int> status;
   // AMR tables
   TableView<int> rf_elem, rf_off, rf_face, rf_fine, ad_all, gf_elem, gf_parent, rf_rec_of_elem;
+  // the work of a step on an AMR layout (empty: every element, face, valid element)
+  TableView<int> pred_list, face_list, corr_list;
+  size_t n_pred = 0, n_face_list = 0, n_corr = 0;
   TableView<int8_t> rf_dside, gf_child;
   // all layout tables packed in one device buffer, uploaded by one copy from
   // a pinned staging buffer (tab_ev: that copy has completed)
@@ -203,6 +206,7 @@ struct adg_ctx {
     face_left.release(); face_right.release(); elem_face.release(); elem_cell.release();
     elem_level.release(); scal.release(); dt_done.release(); rate_bits.release(); status.release();
     rf_elem.release(); rf_off.release(); rf_face.release(); rf_fine.release(); ad_all.release();
+    pred_list.release(); face_list.release(); corr_list.release();
     gf_elem.release(); gf_parent.release(); rf_dside.release(); gf_child.release(); tags.release();
     sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); hseed_f.release(); fb_list.release(); fb_count.release();
     fb_total.release(); Uw_alt.release(); remap_i.release(); remap_c.release(); l2_flush.release();
@@ -315,6 +319,47 @@ int upload_tables(adg_ctx* ctx, const RemapTable* rm = nullptr) {
   for (size_t r = 0; r < H.rf_elem.size(); ++r) roe[H.rf_elem[r]] = (int)r;
   add(ctx->rf_rec_of_elem, roe);
   add(ctx->ad_all, ad);
+  // A covered element's state is replaced by the average down, so the step
+  // needs its predictor only for the faces it shares with an uncovered
+  // element, and its corrector not at all: the faces of the step are those
+  // with an uncovered valid side (and those the coarse-fine corrections
+  // read), its predictor elements the sides of those faces and every
+  // uncovered element, its corrector elements the uncovered ones (record
+  // elements are updated by the record threads).  The state after the step
+  // is the one of computing everything.
+  std::vector<int> pred_l, face_l, corr_l;
+  {
+    const size_t nv = H.n_valid(), ne = H.n_elem(), nf = H.face_left.size();
+    const size_t nov1 = ((size_t)1 << D) + 1;
+    std::vector<uint8_t> covered(ne, 0);
+    for (size_t r = 0; r + nov1 <= ad.size(); r += nov1) covered[ad[r]] = 1;
+    if (ad.size() >= nov1) {
+      std::vector<uint8_t> fneed(nf, 0), eneed(ne, 0);
+      auto uncovered = [&](int e) { return (size_t)e < nv && !covered[e]; };
+      for (size_t f = 0; f < nf; ++f)
+        if (uncovered(H.face_left[f]) || uncovered(H.face_right[f])) fneed[f] = 1;
+      for (int f : H.rf_face) fneed[f] = 1;
+      for (int f : H.rf_fine) fneed[f] = 1;
+      for (size_t f = 0; f < nf; ++f)
+        if (fneed[f]) {
+          face_l.push_back((int)f);
+          eneed[H.face_left[f]] = eneed[H.face_right[f]] = 1;
+        }
+      for (size_t e = 0; e < nv; ++e)
+        if (!covered[e]) {
+          eneed[e] = 1;
+          if (roe[e] < 0) corr_l.push_back((int)e);
+        }
+      for (size_t e = 0; e < ne; ++e)
+        if (eneed[e]) pred_l.push_back((int)e);
+    }
+  }
+  ctx->n_pred = pred_l.size();
+  ctx->n_face_list = face_l.size();
+  ctx->n_corr = corr_l.size();
+  add(ctx->pred_list, pred_l);
+  add(ctx->face_list, face_l);
+  add(ctx->corr_list, corr_l);
   // ghost fills grouped by child index: the warps of the fill kernel then
   // mostly run a single coarse-to-fine operator
   std::vector<size_t> gperm(H.gf_elem.size());
@@ -366,10 +411,12 @@ int upload_tables(adg_ctx* ctx, const RemapTable* rm = nullptr) {
 int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base, cudaEvent_t* ev);
 namespace {
 
-// ADER of every level with the current device Dt (AmrDG.h:1071-1165).
 int flush_ghosts(adg_ctx* ctx);
 
-int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
+// ADER of every level with the current device Dt (AmrDG.h:1071-1165).
+// in_step: the average down follows (a step), so the work lists of the
+// layout apply; alone (adg_ader) every valid element is updated.
+int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr, bool in_step = false) {
   int rc0 = flush_ghosts(ctx);
   if (rc0) return rc0;
   const Hierarchy& H = ctx->hier;
@@ -387,6 +434,11 @@ int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
   pa.Tr = ctx->Tr.p;
   pa.Hw_out = hw_out;
   pa.ubar_old = ctx->cfg.limiter_t > 0 ? ctx->ubar_old.p : nullptr;
+  const bool lists = in_step && ctx->n_pred > 0 && !hw_out;
+  if (lists) {
+    pa.elem_list = ctx->pred_list.p;
+    pa.n_elem = (int)ctx->n_pred;
+  }
   if (ev) cudaEventRecord(ev[0], ctx->stream);
   cudaError_t e = cudaSuccess;
   if (ctx->seed_mode && ctx->seed) {
@@ -405,8 +457,12 @@ int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
   fa.face_right = ctx->face_right.p;
   for (int d = 0; d <= 3; ++d) fa.face_off[d] = (d <= D) ? H.face_off[d] : H.face_off[D];
   fa.Fnum = ctx->Fnum.p;
+  if (lists) {
+    fa.face_list = ctx->face_list.p;
+    fa.n_list = (long long)ctx->n_face_list;
+  }
   const bool split_tiles = ctx->seed_mode == 2 && ctx->seed;  // predictor modes 2 and 3
-  e = ks->numflux(fa, (long long)H.face_left.size(), ctx->stream, split_tiles);
+  e = ks->numflux(fa, lists ? (long long)ctx->n_face_list : (long long)H.face_left.size(), ctx->stream, split_tiles);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "numflux launch");
   ctx->launches++;
   if (ev) cudaEventRecord(ev[2], ctx->stream);
@@ -417,6 +473,10 @@ int launch_ader(adg_ctx* ctx, double* hw_out, cudaEvent_t* ev = nullptr) {
   ca.Fnum = ctx->Fnum.p;
   ca.elem_face = ctx->elem_face.p;
   ca.n_valid = (int)H.n_valid();
+  if (lists) {
+    ca.elem_list = ctx->corr_list.p;
+    ca.n_list = (int)ctx->n_corr;
+  }
   ca.elem_level = pa.elem_level;
   ca.geom = pa.geom;
   ca.dt = ctx->scal.p;
@@ -547,7 +607,7 @@ int launch_limiter(adg_ctx* ctx) {
 }
 
 int launch_step(adg_ctx* ctx, cudaEvent_t* ev = nullptr) {
-  int rc = launch_ader(ctx, nullptr, ev);
+  int rc = launch_ader(ctx, nullptr, ev, true);
   if (rc) return rc;
   if (ctx->cfg.limiter_t > 0 && ctx->nstep % ctx->cfg.limiter_t == 0) {
     rc = launch_limiter(ctx);

@@ -33,7 +33,7 @@ constexpr size_t smem_bytes() {
 template <int E, int MODE>
 cudaError_t launch_predictor_mode(const PredictorArgs& a, cudaStream_t s) {
   constexpr size_t smem = smem_bytes<E, MODE>();
-  if (a.elem_list) {  // fallback pass (modes 0 and 3): two blocks per SM stride over the list
+  if (a.elem_list && a.list_count) {  // fallback pass (modes 0 and 3): two blocks per SM stride over the list
     if constexpr (MODE == 0 || MODE == 3) {
       static bool attr = false;
       if (!attr) {
@@ -125,7 +125,7 @@ struct Impl final : KernelSet {
     return cudaGetLastError();
   }
   cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const override {
-    const long long n = ((long long)a.n_valid + (a.rec_of_elem ? a.nrec : 0)) * O::Q;
+    const long long n = ((long long)(a.elem_list ? a.n_list : a.n_valid) + (a.rec_of_elem ? a.nrec : 0)) * O::Q;
     // one-warp blocks: at its ~130 registers an SM holds 15 of them, so the
     // columns of ~16k elements run in one wave instead of 1.2
     const int bs = 32;

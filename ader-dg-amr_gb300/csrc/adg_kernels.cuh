@@ -794,6 +794,10 @@ struct FaceArgs {
   const int* face_right;
   int face_off[4];  // faces of direction d: [face_off[d], face_off[d+1])
   double* Fnum;
+  // optional: only the faces face_list[0 .. n_list) (those whose flux an
+  // update reads); nullptr: every face
+  const int* face_list;
+  long long n_list;
 };
 
 // Faces per block of k_numflux: one thread per (face, point), about 256.
@@ -817,13 +821,13 @@ __global__ void k_numflux(FaceArgs a) {
   constexpr int LDH = NB + 1, LDG = NSB + 1;  // padded column strides
   __shared__ double h[FB * Q * LDH];
   __shared__ double g[FB * Q * LDG];
-  const int64_t nface = a.face_off[D];
+  const int64_t npos = a.face_list ? a.n_list : a.face_off[D];
   const int64_t fbase = (int64_t)blockIdx.x * FB;
-  const int nfb = (int)(nface - fbase < FB ? nface - fbase : FB);
+  const int nfb = (int)(npos - fbase < FB ? npos - fbase : FB);
   {
     const int lf = threadIdx.x / NB, m = threadIdx.x % NB;  // m = t NSB + x
     if (lf < nfb) {
-      const int64_t f = fbase + lf;
+      const int64_t f = a.face_list ? a.face_list[fbase + lf] : fbase + lf;
       int d = 0;
 #pragma unroll
       for (int k = 1; k < D; ++k)
@@ -853,7 +857,8 @@ __global__ void k_numflux(FaceArgs a) {
   for (int c = threadIdx.x; c < nfb * Q; c += NT) {
     double mom[NM];
     O::face_mom_sp(ColIn{g + c * LDG, 1}, RegOut{mom});
-    store_run<NM>(a.Fnum + ((size_t)fbase * Q + c) * NM, mom);
+    const int64_t f = a.face_list ? a.face_list[fbase + c / Q] : fbase + c / Q;
+    store_run<NM>(a.Fnum + ((size_t)f * Q + c % Q) * NM, mom);
   }
 }
 
@@ -875,13 +880,13 @@ __global__ void k_numflux_split(FaceArgs a) {
   __shared__ float h[FB * Q * LDH];
   __shared__ float cs[FB * LDH];
   __shared__ double g[FB * Q * LDG];
-  const int64_t nface = a.face_off[D];
+  const int64_t npos = a.face_list ? a.n_list : a.face_off[D];
   const int64_t fbase = (int64_t)blockIdx.x * FB;
-  const int nfb = (int)(nface - fbase < FB ? nface - fbase : FB);
+  const int nfb = (int)(npos - fbase < FB ? npos - fbase : FB);
   {
     const int lf = threadIdx.x / NB, m = threadIdx.x % NB;  // m = t NSB + x
     if (lf < nfb) {
-      const int64_t f = fbase + lf;
+      const int64_t f = a.face_list ? a.face_list[fbase + lf] : fbase + lf;
       int d = 0;
 #pragma unroll
       for (int k = 1; k < D; ++k)
@@ -900,7 +905,7 @@ __global__ void k_numflux_split(FaceArgs a) {
   for (int i = threadIdx.x; i < nfb * Q * NSB; i += NT) {
     const int x = i % NSB, c = i / NSB;  // c = face * Q + q
     const int lf = c / Q, q = c % Q;
-    const int64_t f = fbase + lf;
+    const int64_t f = a.face_list ? a.face_list[fbase + lf] : fbase + lf;
     int d = 0;
 #pragma unroll
     for (int k = 1; k < D; ++k)
@@ -922,7 +927,8 @@ __global__ void k_numflux_split(FaceArgs a) {
   for (int c = threadIdx.x; c < nfb * Q; c += NT) {
     double mom[NM];
     O::face_mom_sp(ColIn{g + c * LDG, 1}, RegOut{mom});
-    store_run<NM>(a.Fnum + ((size_t)fbase * Q + c) * NM, mom);
+    const int64_t f = a.face_list ? a.face_list[fbase + c / Q] : fbase + c / Q;
+    store_run<NM>(a.Fnum + ((size_t)f * Q + c % Q) * NM, mom);
   }
 }
 
@@ -970,6 +976,11 @@ struct CorrectorArgs {
   const double* Fnum;
   const int* elem_face;  // [elem][2D]: face index of (d, side)
   int n_valid;
+  // optional: the elements the non-record threads update (elem_list[0 ..
+  // n_list), the valid elements whose state no average down replaces);
+  // nullptr: every valid element
+  const int* elem_list;
+  int n_list;
   const int8_t* elem_level;
   LevelGeom geom;
   const double* dt;
@@ -1054,8 +1065,8 @@ __global__ void k_corrector(CorrectorArgs a) {
     e = a.rec_elem[r];
   } else {
     const int64_t t2 = t - nrq;
-    if (t2 >= (int64_t)a.n_valid * Q) return;
-    e = (int)(t2 / Q);
+    if (t2 >= (int64_t)(a.elem_list ? a.n_list : a.n_valid) * Q) return;
+    e = a.elem_list ? a.elem_list[t2 / Q] : (int)(t2 / Q);
     q = (int)(t2 % Q);
     if (nrq && a.rec_of_elem[e] >= 0) return;  // updated by a record thread
   }

@@ -21,9 +21,12 @@ struct KernelSet {
   virtual size_t predictor_smem(int E) const = 0;
   // mode 0: FP64 Picard; 1 / 2: seeded, FP64 / FP32 sweeps; 3: FP64 Picard with
   // mode 2's final stage (element lists only: the fallback of a mode-2 step).
-  // With a.elem_list set (modes 0 and 3) a short grid strides over the list.
+  // An element list counted on the device (a.list_count, modes 0 and 3: the
+  // fallback) is strided over by a short grid; one counted on the host
+  // (a.list_count == nullptr, a.n_elem entries) runs one group per block.
   virtual cudaError_t predictor(const PredictorArgs& a, int E, cudaStream_t s, int mode = 0) const = 0;
-  // split: the trace tiles are split tiles (predictor modes 2 and 3)
+  // split: the trace tiles are split tiles (predictor modes 2 and 3);
+  // nface: the faces computed (a.n_list with a face list)
   virtual cudaError_t numflux(const FaceArgs& a, long long nface, cudaStream_t s, bool split = false) const = 0;
   virtual cudaError_t corrector(const CorrectorArgs& a, cudaStream_t s) const = 0;
   virtual cudaError_t dt_reduce(const DtArgs& a, cudaStream_t s) const = 0;
