@@ -620,7 +620,8 @@ def run_ours(args, w):
                      "seed_path": seed_roof,
                      "kernel": "k_predictor (plain FP64 path of this workload)", "kernel_ms": km_plain["predictor"],
                      "algorithmic_flops_per_element": alg_pred, "elements_per_launch": el_per_step,
-                     "elements_note": "valid elements of all levels (the launch also runs the coarse-fine ghosts)",
+                     "elements_note": ("valid elements of all levels (on AMR layouts the launch runs the uncovered "
+                                       "ones, the covered ones that border them and the coarse-fine ghosts)"),
                      "issued_linear_fp64_per_element": issued,
                      "fp64_pipe_active_ncu": PROFILED_FP64_ACTIVE.get(args.workload),
                      "note": ("frac counts the reference's dense matrix-form flops per element (the per-unit "
