@@ -349,12 +349,12 @@ L2_FLUSH_BYTES = 256 << 20  # twice the 129 MB L2: written before every timed st
 # DRAM bytes (read + write) of one plain k_predictor launch, from the ncu
 # capture summarised in the named profile (same workload and code)
 PROFILED_TRAFFIC = {
-    "kh_p3_amr3": (35.81e6, "profiles/k_predictor_kh_p3_amr3.md"),
+    "kh_p3_amr3": (24.68e6, "profiles/k_predictor_kh_p3_amr3.md"),
     "kh_p3_256": (285.34e6, "profiles/k_predictor_kh_p3_256.md"),
 }
 # FP64 pipe activity of the predictor kernels (ncu, sm__pipe_fp64_cycles_active of peak, same files)
 PROFILED_FP64_ACTIVE = {
-    "kh_p3_amr3": {"plain_predictor": 0.787, "seeded_predictor": 0.671},
+    "kh_p3_amr3": {"plain_predictor": 0.757, "seeded_predictor": 0.637},
     "kh_p3_256": {"plain_predictor": 0.839},
 }
 
