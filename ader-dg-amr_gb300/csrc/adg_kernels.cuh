@@ -869,31 +869,58 @@ __global__ void k_numflux(FaceArgs a) {
 //   A = sum_t (w_t / 2) (df_L + df_R - C_t (du_R - du_L)),  S = sum_t (w_t / 2) C_t,
 // so the time-dependent part (A, S) runs in FP32 and FP64 is spent once per
 // spatial face point.
-//   Phase 1, thread (face, point): C_t and the FP32 terms of A.
+//   Phase 0, thread (face): the face's two tile addresses into shared memory.
+//   Phase 1, thread (face, point): C_t and the FP32 terms of A; the same
+//     thread loads the FP64 values of its phase-2 items beside them.
 //   Phase 2, thread (face, variable, x): A, S and the FP64 sum.
 //   Phase 3, thread (face, variable): the tangential moments (face_mom_sp).
 template <class O>
 __global__ void k_numflux_split(FaceArgs a) {
   constexpr int D = O::D, Q = O::Q, N = O::N, NB = O::NQ_BD, NSB = NB / N, NF = 2 * D, NM = O::NM;
   constexpr int TT = tr_tile<O>(), FB = numflux_faces_per_block<O>(), NT = FB * NB, FO = split_tr_float_off<O>();
-  constexpr int LDH = NB + 1, LDG = NSB + 1;
+  constexpr int LDH = NB + 1, LDG = NSB + 1, IT = (FB * Q * NSB + NT - 1) / NT;
   __shared__ float h[FB * Q * LDH];
   __shared__ float cs[FB * LDH];
   __shared__ double g[FB * Q * LDG];
+  __shared__ const double* tile[FB][2];  // the left element's high-side and the right one's low-side tile
+  __shared__ int64_t fid[FB];
   const int64_t npos = a.face_list ? a.n_list : a.face_off[D];
   const int64_t fbase = (int64_t)blockIdx.x * FB;
   const int nfb = (int)(npos - fbase < FB ? npos - fbase : FB);
+  // the block's face indices once, so that every tile load below is issued
+  // in one round
+  if ((int)threadIdx.x < nfb) {
+    const int lf = threadIdx.x;
+    const int64_t f = a.face_list ? a.face_list[fbase + lf] : fbase + lf;
+    int d = 0;
+#pragma unroll
+    for (int k = 1; k < D; ++k)
+      if (f >= a.face_off[k]) d = k;
+    fid[lf] = f;
+    tile[lf][0] = a.Tr + ((size_t)a.face_left[f] * NF + 2 * d + 1) * TT;
+    tile[lf][1] = a.Tr + ((size_t)a.face_right[f] * NF + 2 * d + 0) * TT;
+  }
+  __syncthreads();
+  // the FP64 U and F_n(U) values of this thread's (face, variable, point)
+  // items, loaded together with the FP32 changes of phase 1
+  double fsum[IT], jump[IT];
+#pragma unroll
+  for (int k = 0; k < IT; ++k) {
+    const int i = threadIdx.x + k * NT;
+    fsum[k] = jump[k] = 0.0;
+    if (i < nfb * Q * NSB) {
+      const int x = i % NSB, c = i / NSB, lf = c / Q, q = c % Q;
+      const double* tl = tile[lf][0] + q * NSB + x;
+      const double* tr = tile[lf][1] + q * NSB + x;
+      fsum[k] = tl[Q * NSB] + tr[Q * NSB];
+      jump[k] = tr[0] - tl[0];
+    }
+  }
   {
     const int lf = threadIdx.x / NB, m = threadIdx.x % NB;  // m = t NSB + x
     if (lf < nfb) {
-      const int64_t f = a.face_list ? a.face_list[fbase + lf] : fbase + lf;
-      int d = 0;
-#pragma unroll
-      for (int k = 1; k < D; ++k)
-        if (f >= a.face_off[k]) d = k;
-      const int L = a.face_left[f], R = a.face_right[f];
-      const float* tl = reinterpret_cast<const float*>(a.Tr + ((size_t)L * NF + 2 * d + 1) * TT) + FO + m;
-      const float* tr = reinterpret_cast<const float*>(a.Tr + ((size_t)R * NF + 2 * d + 0) * TT) + FO + m;
+      const float* tl = reinterpret_cast<const float*>(tile[lf][0]) + FO + m;
+      const float* tr = reinterpret_cast<const float*>(tile[lf][1]) + FO + m;
       const float C = fmaxf(fabsf(tl[2 * Q * NB]), fabsf(tr[2 * Q * NB]));
       cs[lf * LDH + m] = C;
 #pragma unroll
@@ -902,33 +929,27 @@ __global__ void k_numflux_split(FaceArgs a) {
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < nfb * Q * NSB; i += NT) {
-    const int x = i % NSB, c = i / NSB;  // c = face * Q + q
-    const int lf = c / Q, q = c % Q;
-    const int64_t f = a.face_list ? a.face_list[fbase + lf] : fbase + lf;
-    int d = 0;
 #pragma unroll
-    for (int k = 1; k < D; ++k)
-      if (f >= a.face_off[k]) d = k;
-    const double* tl = a.Tr + ((size_t)a.face_left[f] * NF + 2 * d + 1) * TT + q * NSB + x;
-    const double* tr = a.Tr + ((size_t)a.face_right[f] * NF + 2 * d + 0) * TT + q * NSB + x;
-    const float* hc = h + c * LDH + x;
-    const float* cc = cs + lf * LDH + x;
-    float A = (0.5f * O::weight_f(0)) * hc[0], S = (0.5f * O::weight_f(0)) * cc[0];
+  for (int k = 0; k < IT; ++k) {
+    const int i = threadIdx.x + k * NT;
+    if (i < nfb * Q * NSB) {
+      const int x = i % NSB, c = i / NSB;  // c = face * Q + q
+      const float* hc = h + c * LDH + x;
+      const float* cc = cs + (c / Q) * LDH + x;
+      float A = (0.5f * O::weight_f(0)) * hc[0], S = (0.5f * O::weight_f(0)) * cc[0];
 #pragma unroll
-    for (int t = 1; t < N; ++t) {
-      A = fmaf(0.5f * O::weight_f(t), hc[t * NSB], A);
-      S = fmaf(0.5f * O::weight_f(t), cc[t * NSB], S);
+      for (int t = 1; t < N; ++t) {
+        A = fmaf(0.5f * O::weight_f(t), hc[t * NSB], A);
+        S = fmaf(0.5f * O::weight_f(t), cc[t * NSB], S);
+      }
+      g[c * LDG + x] = fma(-(double)S, jump[k], fma(0.5 * O::WEIGHT_SUM, fsum[k], (double)A));
     }
-    const double fsum = tl[Q * NSB] + tr[Q * NSB], jump = tr[0] - tl[0];
-    g[c * LDG + x] = fma(-(double)S, jump, fma(0.5 * O::WEIGHT_SUM, fsum, (double)A));
   }
   __syncthreads();
   for (int c = threadIdx.x; c < nfb * Q; c += NT) {
     double mom[NM];
     O::face_mom_sp(ColIn{g + c * LDG, 1}, RegOut{mom});
-    const int64_t f = a.face_list ? a.face_list[fbase + c / Q] : fbase + c / Q;
-    store_run<NM>(a.Fnum + ((size_t)f * Q + c % Q) * NM, mom);
+    store_run<NM>(a.Fnum + ((size_t)fid[c / Q] * Q + c % Q) * NM, mom);
   }
 }
 
