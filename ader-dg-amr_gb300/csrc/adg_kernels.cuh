@@ -998,8 +998,8 @@ struct CorrectorArgs {
   const int* elem_face;  // [elem][2D]: face index of (d, side)
   int n_valid;
   // optional: the elements the non-record threads update (elem_list[0 ..
-  // n_list), the valid elements whose state no average down replaces);
-  // nullptr: every valid element
+  // n_list), the valid elements whose state no average down replaces and
+  // that have no reflux record); nullptr: every valid element
   const int* elem_list;
   int n_list;
   const int8_t* elem_level;
@@ -1089,7 +1089,8 @@ __global__ void k_corrector(CorrectorArgs a) {
     if (t2 >= (int64_t)(a.elem_list ? a.n_list : a.n_valid) * Q) return;
     e = a.elem_list ? a.elem_list[t2 / Q] : (int)(t2 / Q);
     q = (int)(t2 % Q);
-    if (nrq && a.rec_of_elem[e] >= 0) return;  // updated by a record thread
+    // updated by a record thread (a list holds no such element)
+    if (nrq && !a.elem_list && a.rec_of_elem[e] >= 0) return;
   }
   const int lev = a.elem_level ? a.elem_level[e] : 0;
   double R[NP_S];
@@ -1335,6 +1336,8 @@ __global__ void k_dt_reduce(DtArgs a) {
   __shared__ double upt[EB][Q + 1];
   const int e0 = blockIdx.x * EB;
   const int ne = a.n_valid - e0 < EB ? a.n_valid - e0 : EB;
+  // the level of this thread's element, loaded beside the states
+  const int lev = a.elem_level && (int)threadIdx.x < ne ? a.elem_level[e0 + threadIdx.x] : 0;
   for (int i = threadIdx.x; i < ne * (EL / 2); i += blockDim.x)
     reinterpret_cast<double2*>(st)[i] = __ldg(reinterpret_cast<const double2*>(a.Uw + (size_t)e0 * EL) + i);
   __syncthreads();
@@ -1347,8 +1350,6 @@ __global__ void k_dt_reduce(DtArgs a) {
   double rate = 0.0;
   unsigned int st_bits = 0;
   if ((int)threadIdx.x < ne) {
-    const int e = e0 + threadIdx.x;
-    const int lev = a.elem_level ? a.elem_level[e] : 0;
     double u[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) u[q] = upt[threadIdx.x][q];
