@@ -48,7 +48,16 @@ class AdgConfig(ctypes.Structure):
         ("n_error_buf", ctypes.c_int), ("reflux_box_quirk", ctypes.c_int),
         ("picard_sweeps", ctypes.c_int), ("elems_per_block", ctypes.c_int),
         ("limiter_t", ctypes.c_int), ("tvb_M", ctypes.c_double), ("tvb_c", ctypes.c_double * 8),
+        ("dt_regrid", ctypes.c_double), ("amr_c", ctypes.c_double * 8), ("tag_advect", ctypes.c_int),
+        ("validation_mode", ctypes.c_int), ("no_reflux", ctypes.c_int),
     ]
+
+
+# Refinement criteria (ADG_TAG_* of include/adg.h): this library's two
+# indicators and the reference's own pde_tag_cell_refinement variants
+# (Compressible_Euler.h:606-685).
+TAG_KINDS = {"density_gradient": 0, "pressure_jump": 1, "isentropic_vortex": 2, "vortex": 2,
+             "kelvin_helmolz_instability": 3, "kh_tvb": 3}
 
 
 class AdgError(RuntimeError):
@@ -224,9 +233,15 @@ class AmrDG:
                              amr_tvb_c=amr_tvb_c, t_limit=t_limit)
 
     def setGeometrySettings(self, prob_lo, prob_hi, n_cell, max_level=0, periodic=None, max_grid=32,
-                            blocking_factor=8, dtn_regrid=4):
-        """Simulation::setGeometrySettings (Simulation.h:120-140)."""
+                            blocking_factor=8, dtn_regrid=4, amr_c=None, dt_regrid=0.0):
+        """Simulation::setGeometrySettings (Simulation.h:120-140): amr_c is
+        the per-level coefficient of the reference's tagging criteria,
+        dtn_regrid / dt_regrid the step and time cadence of the regrid
+        (<= 0: off)."""
         c = self.cfg
+        for l in range(8):
+            c.amr_c[l] = 1.0 if amr_c is None or l >= len(amr_c) else float(amr_c[l])
+        c.dt_regrid = float(dt_regrid)
         for d in range(3):
             if d < self.D:
                 c.prob_lo[d], c.prob_hi[d] = float(prob_lo[d]), float(prob_hi[d])
@@ -248,10 +263,26 @@ class AmrDG:
         self.data_dir, self.restart_tstep = str(data_dir), int(restart_tstep)
         return self
 
-    def setAmrSettings(self, tag_kind=0, tag_threshold=0.1, grid_eff=0.7, n_error_buf=1, reflux_box_quirk=1):
+    def setAmrSettings(self, tag_kind=0, tag_threshold=0.1, grid_eff=0.7, n_error_buf=1, reflux_box_quirk=1,
+                       tag_advect=0, reflux=True):
+        """Refinement criterion (a TAG_KINDS name or code) and the AMReX
+        clustering parameters; tag_advect moves the vortex criterion's centre
+        with the free stream; reflux=False drops the coarse-fine flux
+        correction."""
         c = self.cfg
-        c.tag_kind, c.tag_threshold, c.grid_eff = int(tag_kind), float(tag_threshold), float(grid_eff)
+        c.tag_kind = TAG_KINDS[tag_kind] if isinstance(tag_kind, str) else int(tag_kind)
+        c.tag_threshold, c.grid_eff = float(tag_threshold), float(grid_eff)
         c.n_error_buf, c.reflux_box_quirk = int(n_error_buf), int(reflux_box_quirk)
+        c.tag_advect, c.no_reflux = int(tag_advect), 0 if reflux else 1
+        return self
+
+    def setValidationMode(self, mode):
+        """Simulation::setValidationMode (Simulation.h:51-53, Solver.h:711-734):
+        False/0 projects the finer levels' initial state from the coarser
+        level; True/1 takes the analytic IC on every level (then average down
+        and ghost fill); 2 as 1 with the finer levels' coarse-fine ghosts left
+        at the analytic IC until the first step."""
+        self.cfg.validation_mode = int(mode)
         return self
 
     # ------------------------------------------------------------ lifecycle

@@ -135,6 +135,7 @@ struct adg_ctx {
   double regrid_ms = 0.0;     // host wall time spent in regrids
   bool first_step = true;
   int n_regrids = 0;
+  double t_last_regrid = 0.0;  // time of the last regrid (dt_regrid cadence)
 
   // device state
   DevBuf<double> Uw, Rvol, Tr, Fnum, Hw_dbg;
@@ -241,6 +242,13 @@ int cuda_fail(adg_ctx* c, cudaError_t e, const char* where) {
     cudaError_t _e = (call);                   \
     if (_e != cudaSuccess) return cuda_fail(ctx, _e, where); \
   } while (0)
+
+// Per-level coefficient of the reference's tagging criteria (1.0 when unset,
+// the reference's default, Source/main.cpp:125).
+double amr_coeff(const adg_config& c, int l) {
+  const double v = c.amr_c[l < 8 ? l : 7];
+  return v > 0.0 ? v : 1.0;
+}
 
 LevelGeom level_geom(const adg_ctx* ctx) {
   LevelGeom g{};
@@ -649,6 +657,43 @@ double ms_between(std::chrono::steady_clock::time_point a, std::chrono::steady_c
 int apply_layout(adg_ctx* ctx, const std::vector<std::vector<amr::IBox>>& ng,
                  std::chrono::steady_clock::time_point t2);
 
+// Arguments of the refinement indicator for elements e0 .. e0+n-1.
+TagArgs tag_args(const adg_ctx* ctx, int e0, int n) {
+  const adg_config& c = ctx->cfg;
+  TagArgs ta{};
+  ta.Uw = ctx->Uw.p;
+  ta.elem_face = ctx->elem_face.p;
+  ta.face_left = ctx->face_left.p;
+  ta.face_right = ctx->face_right.p;
+  ta.e0 = e0;
+  ta.n = n;
+  ta.kind = c.tag_kind;
+  ta.threshold = c.tag_threshold;
+  ta.gamma = c.gamma;
+  ta.tags = ctx->tags.p;
+  ta.elem_cell = ctx->elem_cell.p;
+  ta.elem_level = ctx->elem_level.p;
+  ta.scal = ctx->scal.p;
+  ta.geom = level_geom(ctx);
+  for (int d = 0; d < 2; ++d) {
+    ta.prob_lo[d] = c.prob_lo[d];
+    ta.extent[d] = c.prob_hi[d] - c.prob_lo[d];
+  }
+  ta.xc = c.xc;
+  ta.yc = c.yc;
+  ta.u_inf = c.u_inf;
+  ta.v_inf = c.v_inf;
+  ta.advect = c.tag_advect;
+  for (int l = 0; l < kMaxLevels; ++l) {
+    const double ac = amr_coeff(c, l);
+    ta.r_max[l] = ac * ac;
+    double h = ta.geom.dx[l][0];
+    for (int d = 1; d < c.D; ++d) h = std::min(h, ta.geom.dx[l][d]);
+    ta.tvb_thr[l] = c.tvb_c[l < 8 ? l : 7] * ac * std::pow(h, 2.0);
+  }
+  return ta;
+}
+
 // Regrid, device half: the refinement indicator of every level that may be
 // refined, its tags copied into pinned host memory (tag_ev marks the copy).
 int regrid_tags(adg_ctx* ctx, size_t* nt_out) {
@@ -659,17 +704,7 @@ int regrid_tags(adg_ctx* ctx, size_t* nt_out) {
   const size_t nt = H.level_valid_offset(max_crse) + H.level_valid_count(max_crse);
   ADG_CUDA(ctx->tags.ensure(nt), "alloc tags");
   {  // the valid elements of levels 0 .. max_crse are contiguous: one launch
-    TagArgs ta{};
-    ta.Uw = ctx->Uw.p;
-    ta.elem_face = ctx->elem_face.p;
-    ta.face_left = ctx->face_left.p;
-    ta.face_right = ctx->face_right.p;
-    ta.e0 = 0;
-    ta.n = (int)nt;
-    ta.kind = ctx->cfg.tag_kind;
-    ta.threshold = ctx->cfg.tag_threshold;
-    ta.gamma = ctx->cfg.gamma;
-    ta.tags = ctx->tags.p;
+    TagArgs ta = tag_args(ctx, 0, (int)nt);
     cudaError_t e = ks->tag(ta, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "tag launch");
     ctx->launches++;
@@ -776,7 +811,8 @@ int apply_layout(adg_ctx* ctx, const std::vector<std::vector<amr::IBox>>& ng,
   const KernelSet* ks = ctx->ks;
   Hierarchy NH;
   std::string msg;
-  if (!NH.build(ctx->gp, ng, ctx->cfg.reflux_box_quirk, &msg)) return fail(ctx, ADG_ERR_LAYOUT, "layout: " + msg);
+  if (!NH.build(ctx->gp, ng, ctx->cfg.reflux_box_quirk, &msg, !ctx->cfg.no_reflux))
+    return fail(ctx, ADG_ERR_LAYOUT, "layout: " + msg);
   // remap: level 0 is unchanged; level l from the old level l where a cell
   // was valid there, else from the new level l-1 (levels in order on the stream).
   const int Q = ks->Q, Ns = ks->Np_s;
@@ -836,9 +872,29 @@ int apply_layout(adg_ctx* ctx, const std::vector<std::vector<amr::IBox>>& ng,
   return ADG_OK;
 }
 
-bool regrid_due(const adg_ctx* ctx) {
+// AmrDG.h:936-941: at the first step, every dtn_regrid steps, or once
+// dt_regrid of time has passed since the last regrid (the time is read from
+// the device only while dt_regrid is on).
+bool regrid_due(adg_ctx* ctx) {
   if (ctx->cfg.max_level <= 0) return false;
-  return ctx->first_step || (ctx->cfg.dtn_regrid > 0 && ctx->nstep % ctx->cfg.dtn_regrid == 0);
+  if (ctx->first_step || (ctx->cfg.dtn_regrid > 0 && ctx->nstep % ctx->cfg.dtn_regrid == 0)) return true;
+  if (ctx->cfg.dt_regrid > 0.0) {
+    double t = 0.0;
+    if (cudaMemcpyAsync(&t, ctx->scal.p + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      return false;  // the step's own launches report the error
+    return t - ctx->t_last_regrid >= ctx->cfg.dt_regrid - 1e-12;
+  }
+  return false;
+}
+
+// Time of the step about to run, recorded as the last regrid's (dt_regrid).
+void note_regrid_time(adg_ctx* ctx) {
+  if (ctx->cfg.dt_regrid <= 0.0) return;
+  double t = 0.0;
+  if (cudaMemcpyAsync(&t, ctx->scal.p + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess &&
+      cudaStreamSynchronize(ctx->stream) == cudaSuccess)
+    ctx->t_last_regrid = t;
 }
 
 // One evolve-loop body: regrid when due (host), then the step kernels.
@@ -919,7 +975,9 @@ int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
   if (ctx->cfg.limiter_t > 1) use_graph = false;  // the step's kernels then differ from step to step
   int rc = flush_ghosts(ctx);  // the regrid's tags read them
   if (rc) return rc;
-  if (regrid_due(ctx) && !ctx->first_step && !ev) {
+  const bool due = regrid_due(ctx);
+  if (due) note_regrid_time(ctx);
+  if (due && !ctx->first_step && !ev) {
     auto t0 = std::chrono::steady_clock::now();
     size_t nt = 0;
     rc = regrid_tags(ctx, &nt);
@@ -939,7 +997,7 @@ int host_step(adg_ctx* ctx, bool use_graph, cudaEvent_t* ev) {
     ctx->nstep++;
     return ADG_OK;
   }
-  if (regrid_due(ctx)) {
+  if (due) {
     auto t0 = std::chrono::steady_clock::now();
     rc = regrid(ctx);
     if (rc) return rc;
@@ -1101,15 +1159,22 @@ int adg_init(adg_ctx* ctx) {
   const KernelSet* ks = ctx->ks;
   std::string msg;
   ctx->gp = Hierarchy::params(c);
-  // Single level: one box over the domain.  AMR: level 0 chopped to
-  // max_grid, every finer level a full-domain grid to start with (the
-  // reference's initial hierarchy, Source/Core/Solver.h:571-573); the first
+  if (c.validation_mode < 0 || c.validation_mode > 2) return fail(ctx, ADG_ERR_ARG, "validation_mode must be 0, 1 or 2");
+  if (c.tag_kind < 0 || c.tag_kind > 3) return fail(ctx, ADG_ERR_ARG, "unknown tag_kind");
+  // Single level: one box over the domain.  AMR: AmrCore::InitFromScratch
+  // (Source/Core/Solver.h:567-571) tags the levels while their state is still
+  // zero.  The geometric vortex criterion tags its disc, so the hierarchy is
+  // clustered from it level by level; the data criteria see a zero state
+  // (the reference's TVB test reads NaN eigenvectors there and flags every
+  // cell), so every finer level starts as a full-domain grid and the first
   // step regrids from the refinement indicator.
+  const bool geometric = c.max_level > 0 && c.tag_kind == ADG_TAG_VORTEX;
   std::vector<std::vector<amr::IBox>> g;
   if (c.max_level <= 0) {
     if (!ctx->hier.build_single_level(c, &msg)) return fail(ctx, ADG_ERR_LAYOUT, msg);
   } else {
-    for (int l = 0; l <= c.max_level; ++l) {
+    const int top = geometric ? 0 : c.max_level;
+    for (int l = 0; l <= top; ++l) {
       amr::IBox dom;
       for (int d = 0; d < 3; ++d) {
         dom.lo[d] = 0;
@@ -1117,17 +1182,45 @@ int adg_init(adg_ctx* ctx) {
       }
       g.push_back(amr::chop_max_size({dom}, c.D, ctx->gp.max_grid));
     }
-    if (!ctx->hier.build(ctx->gp, g, c.reflux_box_quirk, &msg)) return fail(ctx, ADG_ERR_LAYOUT, msg);
+    if (!ctx->hier.build(ctx->gp, g, c.reflux_box_quirk, &msg, !c.no_reflux))
+      return fail(ctx, ADG_ERR_LAYOUT, msg);
   }
-  const Hierarchy& H = ctx->hier;
-  ADG_CUDA(ctx->Uw.ensure(H.n_elem() * ks->Q * ks->Np_s), "alloc Uw");
+  ADG_CUDA(ctx->Uw.ensure(ctx->hier.n_elem() * ks->Q * ks->Np_s), "alloc Uw");
+  {
+    const double t0 = 0.0;
+    ADG_CUDA(cudaMemcpyAsync(ctx->scal.p + 1, &t0, sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "reset t");
+  }
   int rc = upload_tables(ctx);
   if (rc) return rc;
+  if (geometric) {
+    // one new level per pass (AmrMesh::MakeNewGrids(time)), then passes over
+    // all levels until the boxes stop changing (its iterate_on_new_grids)
+    ADG_CUDA(cudaMemsetAsync(ctx->Uw.p, 0, ctx->hier.n_elem() * ks->Q * ks->Np_s * sizeof(double), ctx->stream),
+             "zero state");
+    for (int pass = 0; pass < c.max_level + 4; ++pass) {
+      size_t nt = 0;
+      rc = regrid_tags(ctx, &nt);
+      if (rc) return rc;
+      std::vector<std::vector<amr::IBox>> ng;
+      rc = regrid_boxes(ctx, nt, &ng);
+      if (rc) return rc;
+      if (ng == ctx->hier.grids) break;
+      rc = apply_layout(ctx, ng, std::chrono::steady_clock::now());
+      if (rc) return rc;
+    }
+    ctx->n_regrids = 0;
+    for (double& v : ctx->rg_phase_ms) v = 0.0;
+  }
+  const Hierarchy& H = ctx->hier;
+  // the analytic IC on level 0, on every level in validation mode (with the
+  // coarse-fine ghosts too in mode 2) (AmrDG.h:782-836, Solver.h:711-734)
   ICArgs ia{};
   ia.Uw = ctx->Uw.p;
   ia.elem_cell = ctx->elem_cell.p;
-  ia.elem_level = nullptr;  // level 0 elements come first
-  ia.n_elem = (int)H.level_valid_count(0);
+  ia.elem_level = c.validation_mode ? ctx->elem_level.p : nullptr;  // level 0 elements come first
+  ia.n_elem = (int)(c.validation_mode == 2 ? H.n_elem()
+                    : c.validation_mode == 1 ? H.n_valid()
+                                             : H.level_valid_count(0));
   ia.geom = level_geom(ctx);
   for (int d = 0; d < 3; ++d) {
     ia.prob_lo[d] = c.prob_lo[d];
@@ -1145,10 +1238,11 @@ int adg_init(adg_ctx* ctx) {
   cudaError_t e = ks->init_ic(ia, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "init_ic launch");
   ctx->launches++;
-  // finer levels: projection from the coarser level (AMR_interpolate_initial_condition)
+  // finer levels otherwise: projection from the coarser level
+  // (AMR_interpolate_initial_condition)
   DevBuf<int> d_dst, d_par;
   DevBuf<int8_t> d_ch;
-  for (int l = 1; l < H.nlevels(); ++l) {
+  for (int l = 1; !c.validation_mode && l < H.nlevels(); ++l) {
     std::vector<int> dst, par;
     std::vector<int8_t> ch;
     for (size_t x = H.level_valid_offset(l); x < H.level_valid_offset(l) + H.level_valid_count(l); ++x) {
@@ -1183,7 +1277,12 @@ int adg_init(adg_ctx* ctx) {
   ctx->initialised = true;
   ctx->nstep = 0;
   ctx->first_step = true;
-  rc = launch_amr_sync(ctx);
+  ctx->t_last_regrid = 0.0;
+  ctx->ghosts_stale = false;
+  // AMR_sync_initial_condition (AmrDG_Level.tpp:94-118): average down, then
+  // the ghost cells of every level (validation mode 2: the finer levels'
+  // coarse-fine ghosts keep their analytic projection until the first step)
+  rc = c.validation_mode == 2 ? launch_average_down(ctx) : launch_amr_sync(ctx);
   if (rc) return rc;
   rc = launch_dt(ctx, 0);
   if (rc) return rc;
@@ -1493,17 +1592,7 @@ int adg_tags(adg_ctx* ctx, int lev, uint8_t* out) {
   rc = flush_ghosts(ctx);
   if (rc) return rc;
   ADG_CUDA(ctx->tags.ensure(H.n_valid()), "alloc tags");
-  TagArgs ta{};
-  ta.Uw = ctx->Uw.p;
-  ta.elem_face = ctx->elem_face.p;
-  ta.face_left = ctx->face_left.p;
-  ta.face_right = ctx->face_right.p;
-  ta.e0 = (int)H.level_valid_offset(lev);
-  ta.n = (int)H.level_valid_count(lev);
-  ta.kind = ctx->cfg.tag_kind;
-  ta.threshold = ctx->cfg.tag_threshold;
-  ta.gamma = ctx->cfg.gamma;
-  ta.tags = ctx->tags.p;
+  TagArgs ta = tag_args(ctx, (int)H.level_valid_offset(lev), (int)H.level_valid_count(lev));
   cudaError_t e = ctx->ks->tag(ta, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "tag launch");
   ctx->launches++;

@@ -1,6 +1,7 @@
 // One (D, P) instantiation of the kernel set.  The build compiles this file
 // once per configuration with -DADG_D, -DADG_HDR (generated operator header),
 // -DADG_NS (its namespace) and -DADG_FACTORY (factory function name).
+#include <atomic>
 #include "adg_kernelset.hpp"
 #include ADG_HDR
 
@@ -30,18 +31,30 @@ constexpr size_t smem_bytes() {
   return m1 > m2 ? m1 : m2;
 }
 
+// The dynamic shared-memory limit of a kernel is an attribute of the current
+// device's context: it is set once per device (bit d of mask; devices past 63
+// set it on every launch), so a process that moves between GPUs sets it on
+// each of them.
+template <class F>
+cudaError_t ensure_smem_attr(std::atomic<unsigned long long>& mask, F* func, size_t bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (mask.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess && bit) mask.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
+
 template <int E, int MODE>
 cudaError_t launch_predictor_mode(const PredictorArgs& a, cudaStream_t s) {
   constexpr size_t smem = smem_bytes<E, MODE>();
   if (a.elem_list && a.list_count) {  // fallback pass (modes 0 and 3): two blocks per SM stride over the list
     if constexpr (MODE == 0 || MODE == 3) {
-      static bool attr = false;
-      if (!attr) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_predictor_list<O, E, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-      }
+      static std::atomic<unsigned long long> attr{0};
+      cudaError_t e = ensure_smem_attr(attr, k_predictor_list<O, E, MODE>, smem);
+      if (e != cudaSuccess) return e;
       int dev = 0, sms = 0;
       if (cudaGetDevice(&dev) != cudaSuccess ||
           cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
@@ -58,12 +71,9 @@ cudaError_t launch_predictor_mode(const PredictorArgs& a, cudaStream_t s) {
   if constexpr (MODE == 3) {
     return cudaErrorInvalidValue;  // mode 3 runs on element lists only
   } else {
-    static bool attr = false;
-    if (!attr) {
-      cudaError_t e = cudaFuncSetAttribute(k_predictor<O, E, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    cudaError_t e = ensure_smem_attr(attr, k_predictor<O, E, MODE>, smem);
+    if (e != cudaSuccess) return e;
     const int grid = (a.n_elem + E - 1) / E;
     if (grid <= 0) return cudaSuccess;
     k_predictor<O, E, MODE><<<grid, E * O::Q, smem, s>>>(a);
@@ -189,13 +199,9 @@ struct Impl final : KernelSet {
   }
   cudaError_t seed_infer_tc(const SeedTCArgs& a, cudaStream_t s) const override {
     if (a.n <= 0) return cudaSuccess;
-    static bool attr = false;
-    if (!attr) {
-      cudaError_t e =
-          cudaFuncSetAttribute(k_seed_infer_tc<O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSeedTcSmem);
-      if (e != cudaSuccess) return e;
-      attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    cudaError_t e = ensure_smem_attr(attr, k_seed_infer_tc<O>, kSeedTcSmem);
+    if (e != cudaSuccess) return e;
     k_seed_infer_tc<O><<<(a.n + kSeedTcRows - 1) / kSeedTcRows, kSeedTcThreads, kSeedTcSmem, s>>>(a);
     return cudaGetLastError();
   }

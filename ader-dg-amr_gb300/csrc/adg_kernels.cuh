@@ -1683,9 +1683,19 @@ struct TagArgs {
   const int* face_left;
   const int* face_right;
   int e0, n;
-  int kind;
+  int kind;               // ADG_TAG_* of include/adg.h
   double threshold, gamma;
   uint8_t* tags;
+  // the reference's criteria (kinds 2 and 3)
+  const int* elem_cell;
+  const int8_t* elem_level;
+  const double* scal;     // device scalar block: [1] = t
+  LevelGeom geom;
+  double prob_lo[2], extent[2];
+  double xc, yc, u_inf, v_inf;
+  int advect;
+  double r_max[kMaxLevels];    // amr_c[l]^2
+  double tvb_thr[kMaxLevels];  // AMR_TVB_C[l] * amr_c[l] * h_l^2
 };
 
 template <class O>
@@ -1702,12 +1712,66 @@ __device__ __forceinline__ double cell_pressure(const double* Uw, int e, double 
   return __dmul_rn(gamma - 1.0, __dsub_rn(E, __dmul_rn(0.5, ke)));
 }
 
+// The reference's isentropic-vortex criterion (Compressible_Euler.h:615-644),
+// IEEE operations in its order so that the host oracle tags the same cells.
+__device__ __forceinline__ bool tag_vortex(const TagArgs& a, int e) {
+  const int lev = a.elem_level[e];
+  const double x = __dadd_rn(a.prob_lo[0], __dmul_rn((double)a.elem_cell[3 * e] + 0.5, a.geom.dx[lev][0]));
+  const double y = __dadd_rn(a.prob_lo[1], __dmul_rn((double)a.elem_cell[3 * e + 1] + 0.5, a.geom.dx[lev][1]));
+  double xc = a.xc, yc = a.yc;
+  if (a.advect) {
+    const double t = a.scal[1];
+    xc = __dadd_rn(xc, __dmul_rn(a.u_inf, t));
+    yc = __dadd_rn(yc, __dmul_rn(a.v_inf, t));
+  }
+  double dx = __dsub_rn(x, xc), dy = __dsub_rn(y, yc);
+  const double hx = a.extent[0] / 2.0, hy = a.extent[1] / 2.0;
+  if (dx > hx) dx = __dsub_rn(dx, a.extent[0]);
+  if (dx < -hx) dx = __dadd_rn(dx, a.extent[0]);
+  if (dy > hy) dy = __dsub_rn(dy, a.extent[1]);
+  if (dy < -hy) dy = __dadd_rn(dy, a.extent[1]);
+  const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+  return r <= a.r_max[lev];
+}
+
+// The reference's Kelvin-Helmholtz criterion (Compressible_Euler.h:645-682):
+// the cell is tagged as soon as one characteristic linear slope L_EV(u_mean)
+// u_lin fails minmodB's TVB test (AmrDG_Limiter.tpp:40-61); the neighbour
+// differences minmod would take do not change the flag, so they are not
+// formed.  NaN slopes tag the cell, as in the reference.
+template <class O>
+__device__ __forceinline__ bool tag_kh_tvb(const TagArgs& a, int e) {
+  constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S;
+  const double thr = a.tvb_thr[a.elem_level[e]];
+  double ub[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) ub[q] = a.Uw[((size_t)e * Q + q) * NP_S];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const int s = O::lin_mode(d);
+    double R[Q][Q], L[Q][Q];
+    euler_eigenvectors<D>(d, ub, a.gamma, R, L);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      double du = 0.0;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) du = __dadd_rn(du, __dmul_rn(L[q][k], a.Uw[((size_t)e * Q + k) * NP_S + s]));
+      if (!(fabs(du) <= thr)) return true;
+    }
+  }
+  return false;
+}
+
 template <class O>
 __global__ void k_tag(TagArgs a) {
   constexpr int D = O::D, Q = O::Q, NP_S = O::NP_S;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const int e = a.e0 + i;
+  if (a.kind == 2 || a.kind == 3) {
+    a.tags[i] = (a.kind == 2 ? tag_vortex(a, e) : tag_kh_tvb<O>(a, e)) ? 1 : 0;
+    return;
+  }
   double ind = 0.0;
 #pragma unroll
   for (int d = 0; d < D; ++d) {

@@ -117,8 +117,10 @@ struct Hierarchy {
   // face ownership rule of AmrDG_Level.tpp:316-330): a coarse cell is
   // corrected only if one of its coarse-fine faces is flagged in its own
   // box's face array, where a box never flags its own low face.
+  // reflux = false leaves out every coarse-fine flux correction (the
+  // reference's runs without AMR_flux_correction).
   bool build(const amr::GridParams& gp, const std::vector<std::vector<amr::IBox>>& g, int reflux_quirk,
-             std::string* msg) {
+             std::string* msg, bool reflux = true) {
     D = gp.D;
     for (int d = 0; d < 3; ++d) {
       n_cell0[d] = gp.n_cell0[d];
@@ -265,7 +267,7 @@ struct Hierarchy {
     rf_dside.clear();
     rf_fine.clear();
     const int nfc = 1 << (D - 1);
-    for (int l = 0; l + 1 < nlev; ++l) {
+    for (int l = 0; reflux && l + 1 < nlev; ++l) {
       const size_t e0 = lev_valid_off[l], e1 = e0 + lev_valid_cnt[l];
       for (size_t e = e0; e < e1; ++e) {
         const int* c = &elem_cell[3 * e];

@@ -12,6 +12,8 @@
 // holds until the process exits.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "adg.h"
 #include "adg_kernelset.hpp"
 
@@ -26,18 +28,21 @@ constexpr int kMaxDevices = 64;
 // cudaGetSymbolAddress once per device (scratch_address below).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-static void* g_scratch_addr[kMaxDevices] = {nullptr};
+// Device address of the array per device.  Host threads may call at the same
+// time: every thread that finds an entry empty looks the address up itself
+// and stores the same value, so the entries are atomics.
+static std::atomic<void*> g_scratch_addr[kMaxDevices];
 
 // Per-device set-up: the device address of the scratch array on the current
 // device.  Returns nullptr if the runtime cannot provide it.
 void* scratch_address(int dev) {
   if (dev < 0 || dev >= kMaxDevices) return nullptr;
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
+  void* p = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!p) {
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return nullptr;
-    g_scratch_addr[dev] = p;
+    g_scratch_addr[dev].store(p, std::memory_order_release);
   }
-  return g_scratch_addr[dev];
+  return p;
 }
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -81,6 +86,9 @@ extern "C" int adg_ader_step_noalloc(int D, int P, const int n_cell[3], const do
                                      void* stream) {
   const KernelSet* ks = kernel_set(D, P);
   if (!ks || !n_cell || !prob_lo || !prob_hi || !U_w || !(gamma > 1.0) || !(dt > 0.0)) return ADG_ERR_ARG;
+  // An error left pending by earlier work is the caller's: report it without
+  // consuming it or launching anything.
+  if (cudaPeekAtLastError() != cudaSuccess) return ADG_ERR_CUDA;
   long long n = 1;
   for (int d = 0; d < 3; ++d) {
     const int nd = d < D ? n_cell[d] : 1;

@@ -61,8 +61,8 @@ typedef struct adg_config {
   int max_level;
   int blocking_factor;
   int dtn_regrid;           /* regrid every n steps (Mesh::dtn_regrid) */
-  int tag_kind;             /* 0 normalised density gradient, 1 pressure jump */
-  double tag_threshold;
+  int tag_kind;             /* ADG_TAG_* */
+  double tag_threshold;     /* threshold of ADG_TAG_DENSITY_GRADIENT / ADG_TAG_PRESSURE_JUMP */
   double grid_eff;
   int n_error_buf;
   int reflux_box_quirk;     /* 1: reference's per-box reflux mask (AmrDG_Interpolater.tpp:41-56) */
@@ -77,7 +77,36 @@ typedef struct adg_config {
   int limiter_t;
   double tvb_M;
   double tvb_c[8];
+  /* Regrid once dt_regrid of simulated time has passed since the last regrid
+   * (Mesh::dt_regrid, AmrDG.h:936-941; <= 0: off).  The decision reads the
+   * time from the device, one synchronisation per step while it is on. */
+  double dt_regrid;
+  /* Per-level coefficient of the reference's tagging criteria (amr_c of
+   * setGeometrySettings, Source/main.cpp:125-138; <= 0 means 1.0). */
+  double amr_c[8];
+  /* ADG_TAG_VORTEX: 1 moves the tagged disc's centre with the free stream
+   * (xc + u_inf t, yc + v_inf t); 0 keeps it at (xc, yc) as the reference's
+   * current code does (Compressible_Euler.h:629-630). */
+  int tag_advect;
+  /* Initial condition of the finer levels (Solver::setValidationMode,
+   * Solver.h:711-734): 0 the projection of the coarser level; 1 the analytic
+   * IC on every level, then average down and the ghost fill of every level
+   * (AMR_sync_initial_condition, AmrDG_Level.tpp:94-118); 2 as 1, but the
+   * finer levels' coarse-fine ghost cells keep their own analytic projection
+   * until the first step's ghost fill (how the reference's recorded
+   * static-refinement convergence runs were initialised). */
+  int validation_mode;
+  /* 1: no coarse-fine flux correction (the reference's "NO REFLUX" runs). */
+  int no_reflux;
 } adg_config;
+
+/* Refinement criteria (tag_kind). */
+#define ADG_TAG_DENSITY_GRADIENT 0 /* max_d |rho_{i+1} - rho_{i-1}| / (2 rho_i) > tag_threshold (cell means) */
+#define ADG_TAG_PRESSURE_JUMP 1    /* the same on the cell-mean pressure */
+#define ADG_TAG_VORTEX 2           /* Compressible_Euler.h:615-644: cell centre within amr_c[l]^2 of the vortex
+                                      centre (distances wrapped once by half the domain) */
+#define ADG_TAG_KH_TVB 3           /* Compressible_Euler.h:645-682: a characteristic slope of the cell fails
+                                      minmodB's test |slope| <= tvb_c[l] * amr_c[l] * h^2 */
 
 typedef struct adg_ctx adg_ctx;
 
@@ -322,7 +351,9 @@ int adg_fp64_peak_probe(double* gflops);
  * ADG_ERR_NOALLOC_CAPACITY (about 12,800 elements at D=2, P=3).  The first
  * call on a device looks up the array's device address (make it before any
  * stream capture).  All calls share the array: calls that overlap on the GPU
- * race.  Work is issued on `stream` (NULL: default stream), asynchronously. */
+ * race.  Work is issued on `stream` (NULL: default stream), asynchronously.
+ * A CUDA error already pending when the call starts returns ADG_ERR_CUDA
+ * before any launch and is left pending for its owner. */
 #define ADG_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 int adg_ader_step_noalloc(int D, int P, const int n_cell[3], const double prob_lo[3], const double prob_hi[3],
                           double gamma, double dt, double* U_w, void* stream);

@@ -33,8 +33,22 @@ struct AmrConfig {
   int max_grid = 32;
   int blocking_factor = 8;
   int dtn_regrid = 4;
+  // time-based regrid cadence (Mesh::dt_regrid, AmrDG.h:936-941; <= 0: off)
+  double dt_regrid = 0.0;
+  // 0 normalised density gradient, 1 pressure jump (this project's criteria);
+  // 2 vortex radius r <= amr_c[l]^2, 3 KH characteristic TVB troubled cell
+  // (the reference's pde_tag_cell_refinement, Compressible_Euler.h:606-685)
   int tag_kind = 0;
   double tag_threshold = 0.1;
+  double amr_c[8] = {1, 1, 1, 1, 1, 1, 1, 1};
+  // kind 2: 1 moves the tagging centre with the free stream (x0 + u_inf t)
+  int tag_advect = 0;
+  // analytic IC on every level (Solver::setValidationMode, Solver.h:711-734):
+  // 0 off (projection), 1 with the ghost FillPatch of every level, 2 with
+  // the finer levels' ghost cells left at the analytic projection
+  int validation_mode = 0;
+  // 1 skips the coarse-fine flux correction (the reference's NO REFLUX runs)
+  int no_reflux = 0;
   double grid_eff = 0.7;
   int n_error_buf = 1;
   int reflux_box_quirk = 1;
@@ -54,7 +68,11 @@ class AmrSim {
   A::GridParams gp;
   std::vector<std::vector<A::IBox>> grids;
   bool first_step = true;
+  double t_last_regrid = 0.0;
   int n_regrids = 0;
+  // regrids that changed the layout, plus the first one (the reference's
+  // n_regrids, AmrDG.h:968-983)
+  int n_layout_changes = 0;
   long n_limited = 0;
 
   AmrSim(const SimConfig& s, const AmrConfig& a) : sim(s), amr(a) {
@@ -91,22 +109,62 @@ class AmrSim {
       sim.define_level(0, to_boxes(grids[0]));
       sim.set_initial_condition(0);
     } else {
-      // Every level starts as a full-domain grid (Source/Core/Solver.h:571-573);
-      // finer levels are filled by projection from the coarser one
-      // (AMR_interpolate_initial_condition, AmrDG_Level.tpp:134-137) and all
-      // ghost cells are synchronised (AMR_sync_initial_condition).
+      // AmrCore::InitFromScratch (Solver.h:567-571) tags the levels while
+      // their state is still zero (set_init_data_component, AmrDG.tpp:306-307).
+      // The geometric vortex criterion tags its disc; the data criteria see a
+      // zero state (the reference's TVB test reads NaN eigenvectors there and
+      // flags every cell), so every level starts as a full-domain grid.
       grids.clear();
       sim.lev.clear();
-      for (int l = 0; l <= amr.max_level; ++l) {
-        grids.push_back(A::chop_max_size({full_domain(l)}, D(), amr.max_grid));
-        sim.define_level(l, to_boxes(grids[l]));
+      if (amr.tag_kind == 2) {
+        grids.push_back(A::chop_max_size({full_domain(0)}, D(), amr.max_grid));
+        sim.define_level(0, to_boxes(grids[0]));
+        // one new level per pass (AmrMesh::MakeNewGrids(time)), then passes
+        // over all levels until the boxes stop changing (iterate_on_new_grids)
+        for (int pass = 0; pass < amr.max_level + 4; ++pass) {
+          std::vector<A::TagField> tags(grids.size());
+          for (size_t l = 0; l < grids.size(); ++l) tags[l] = compute_tags((int)l);
+          std::vector<std::vector<A::IBox>> ng = A::make_new_grids(gp, grids, tags);
+          bool same = ng.size() == grids.size();
+          for (size_t l = 0; same && l < ng.size(); ++l) same = same_boxes(ng[l], grids[l]);
+          if (same) break;
+          grids = ng;
+          for (size_t l = 0; l < grids.size(); ++l) sim.define_level((int)l, to_boxes(grids[l]));
+          sim.lev.resize(grids.size());
+        }
+      } else {
+        for (int l = 0; l <= amr.max_level; ++l) {
+          grids.push_back(A::chop_max_size({full_domain(l)}, D(), amr.max_grid));
+          sim.define_level(l, to_boxes(grids[l]));
+        }
       }
+      // Solver::set_initial_condition (Solver.h:711-734): the analytic IC on
+      // level 0, on finer levels too in validation mode, else the projection
+      // of the coarser level (AMR_interpolate_initial_condition,
+      // AmrDG_Level.tpp:134-137); then AMR_sync_initial_condition
+      // (AmrDG_Level.tpp:94-120): average down after an analytic IC, and the
+      // ghost cells of every level, coarsest first.
       sim.set_initial_condition(0);
-      for (int l = 1; l <= amr.max_level; ++l) fill_from_coarse(l, nullptr);
-      for (int l = 0; l <= amr.max_level; ++l) fill_patch(l);
+      for (int l = 1; l <= finest(); ++l) {
+        if (amr.validation_mode)
+          sim.set_initial_condition(l);
+        else
+          fill_from_coarse(l, nullptr);
+      }
+      // Validation mode 2 leaves the finer levels' coarse-fine ghost cells
+      // with their own analytic projection until the first step's FillPatch,
+      // which is how the reference's recorded static-refinement convergence
+      // runs were initialised (Source/PostProcessing/convergence.py:22-27);
+      // mode 1 is the FillPatch of every level of the current
+      // AMR_sync_initial_condition.
+      if (amr.validation_mode)
+        for (int l = finest(); l > 0; --l) average_down(l);
+      for (int l = 0; l <= finest(); ++l)
+        if (l == 0 || amr.validation_mode != 2) fill_patch(l);
     }
     sim.t = 0.0;
     sim.nstep = 0;
+    t_last_regrid = 0.0;
     first_step = true;
     sim.Dt = sim.compute_Dt();
     return sim.Dt;
@@ -545,7 +603,8 @@ class AmrSim {
       }
       s.update_U_w(l);
     }
-    for (int l = F; l > 0; --l) reflux(l, regs[l]);
+    if (!amr.no_reflux)
+      for (int l = F; l > 0; --l) reflux(l, regs[l]);
   }
 
   // ---------------------------------------------------------------- tags
@@ -573,6 +632,70 @@ class AmrSim {
     return ind;
   }
 
+  // The reference's isentropic-vortex criterion (Compressible_Euler.h:615-644):
+  // the cell centre within amr_c^2 of the vortex centre, distances wrapped
+  // once by half the domain.  tag_advect moves the centre with the free
+  // stream (the commented "+ u_infty * time" of that code).
+  bool tag_vortex(const Level& L, const int* ijk, double amr_c_lev) const {
+    const double x0 = sim.cfg.icp.xc, y0 = sim.cfg.icp.yc;
+    const double Lx = sim.cfg.prob_hi[0] - sim.cfg.prob_lo[0];
+    const double Ly = sim.cfg.prob_hi[1] - sim.cfg.prob_lo[1];
+    const double x = sim.cfg.prob_lo[0] + (ijk[0] + 0.5) * L.dx[0];
+    const double y = sim.cfg.prob_lo[1] + (ijk[1] + 0.5) * L.dx[1];
+    double xc = x0, yc = y0;
+    if (amr.tag_advect) {
+      xc = x0 + sim.cfg.icp.u_inf * sim.t;
+      yc = y0 + sim.cfg.icp.v_inf * sim.t;
+    }
+    double dxv = x - xc, dyv = y - yc;
+    if (dxv > Lx / 2.0) dxv -= Lx;
+    if (dxv < -Lx / 2.0) dxv += Lx;
+    if (dyv > Ly / 2.0) dyv -= Ly;
+    if (dyv < -Ly / 2.0) dyv += Ly;
+    const double r = std::sqrt(dxv * dxv + dyv * dyv);
+    return r <= std::pow(amr_c_lev, 2);
+  }
+
+  // The reference's Kelvin-Helmholtz criterion (Compressible_Euler.h:645-682):
+  // per direction, the left eigenvectors at the cell mean project the linear
+  // mode and the halved differences to the neighbours' means; a cell is
+  // tagged as soon as one characteristic slope fails minmodB's TVB test
+  // |slope| <= AMR_TVB_C[l] * amr_c[l] * h^2 (AmrDG_Limiter.tpp:40-61): the
+  // differences only feed minmod's value, never the flag.
+  bool tag_kh_tvb(int l, const Level& L, long c) const {
+    const int Dd = D(), Q = sim.Q, Ns = sim.Np_s;
+    double h = L.dx[0];
+    for (int d = 1; d < Dd; ++d) h = std::min(h, L.dx[d]);
+    const double thr = amr.tvb_c[l] * amr.amr_c[l] * std::pow(h, 2.0);
+    auto U = [&](int q, int n, long cc) { return L.Uw[((size_t)q * Ns + n) * L.ncell + cc]; };
+    double ub[5];
+    for (int q = 0; q < Q; ++q) ub[q] = U(q, 0, c);
+    for (int d = 0; d < Dd; ++d) {
+      const int s = lin_mode(d);
+      double R[5][5], Lm[5][5];
+      eigenvectors(d, ub, Dd, sim.cfg.gamma, R, Lm);
+      for (int q = 0; q < Q; ++q) {
+        double Du = 0.0;
+        for (int k = 0; k < Q; ++k) Du += Lm[q][k] * U(k, s, c);
+        if (!(std::abs(Du) <= thr)) return true;
+      }
+    }
+    return false;
+  }
+
+  // Spatial mode of degree one in direction d alone (get_lin_mode_idx).
+  int lin_mode(int d) const {
+    for (int n = 0; n < sim.Np_s; ++n) {
+      bool ok = sim.el.mi_s[n][d] == 1;
+      for (int a = 0; a < D(); ++a)
+        if (a != d && sim.el.mi_s[n][a] != 0) ok = false;
+      if (ok) return n;
+    }
+    return 0;
+  }
+
+  // AMR_tag_cell_refinement (AmrDG_TagCellRef.tpp:4-52): FillBoundary, then
+  // the criterion on every valid cell.
   A::TagField compute_tags(int l) {
     sim.fill_boundary(l);
     const Level& L = sim.lev[l];
@@ -582,7 +705,14 @@ class AmrSim {
       if (L.status[c] != ST_VALID) continue;
       int ijk[3];
       L.coords(c, ijk[0], ijk[1], ijk[2]);
-      if (tag_indicator(L, c, ijk) > amr.tag_threshold) t.f[t.idx(ijk[0], ijk[1], ijk[2])] = 1;
+      bool tag;
+      if (amr.tag_kind == 2)
+        tag = tag_vortex(L, ijk, amr.amr_c[l]);
+      else if (amr.tag_kind == 3)
+        tag = tag_kh_tvb(l, L, c);
+      else
+        tag = tag_indicator(L, c, ijk) > amr.tag_threshold;
+      if (tag) t.f[t.idx(ijk[0], ijk[1], ijk[2])] = 1;
     }
     return t;
   }
@@ -609,7 +739,7 @@ class AmrSim {
     for (int l = max_crse + 1; l <= F; ++l) tags[l].init(sim.lev[l].n);
     std::vector<std::vector<A::IBox>> ng = A::make_new_grids(gp, grids, tags);
     const int new_finest = (int)ng.size() - 1;
-    bool coarse_changed = false;
+    bool coarse_changed = false, coarse_changed_any = false;
     for (int l = 1; l <= new_finest; ++l) {
       bool changed = l > F || !same_boxes(ng[l], grids[l]);
       if (l <= F) {
@@ -626,10 +756,13 @@ class AmrSim {
         fill_from_coarse(l, nullptr);
       }
       coarse_changed = changed;
+      coarse_changed_any = coarse_changed_any || changed;
     }
+    const bool changed_any = new_finest != F || coarse_changed_any;
     sim.lev.resize(new_finest + 1);
     grids.resize(new_finest + 1);
     n_regrids++;
+    if (changed_any || first_step) n_layout_changes++;
   }
 
   static bool same_boxes(const std::vector<A::IBox>& a, const std::vector<A::IBox>& b) {
@@ -643,8 +776,14 @@ class AmrSim {
   // ----------------------------------------------------------------- step
   double step() {
     if (amr.max_level > 0) {
-      bool due = first_step || (amr.dtn_regrid > 0 && sim.nstep % amr.dtn_regrid == 0);
-      if (due) regrid();
+      // AmrDG.h:936-986: at the first step, every dtn_regrid steps, or once
+      // dt_regrid of time has passed since the last regrid
+      bool due = first_step || (amr.dtn_regrid > 0 && sim.nstep % amr.dtn_regrid == 0) ||
+                 (amr.dt_regrid > 0 && sim.t - t_last_regrid >= amr.dt_regrid - 1e-12);
+      if (due) {
+        regrid();
+        t_last_regrid = sim.t;
+      }
       first_step = false;
     }
     ader();

@@ -25,7 +25,7 @@ struct oracle_cfg {
   int max_level;
   int blocking_factor;
   int dtn_regrid;
-  int tag_kind;       // 0 normalised density gradient, 1 pressure jump
+  int tag_kind;       // 0 density gradient, 1 pressure jump, 2 vortex radius, 3 KH TVB
   double tag_threshold;
   double grid_eff;
   int n_error_buf;
@@ -33,6 +33,11 @@ struct oracle_cfg {
   int t_limit;           // TVB limiter every t_limit steps (0: off)
   double tvb_M;
   double tvb_c[8];       // per-level TVB coefficient
+  double dt_regrid;      // regrid once this much time has passed (<= 0: off)
+  double amr_c[8];       // per-level coefficient of tag kinds 2 and 3
+  int tag_advect;        // kind 2: centre moves with the free stream
+  int validation_mode;   // analytic IC on every level (1, 2: see AmrConfig)
+  int no_reflux;         // 1: no coarse-fine flux correction
 };
 
 void* oracle_create(const oracle_cfg* c) {
@@ -68,6 +73,11 @@ void* oracle_create(const oracle_cfg* c) {
   a.t_limit = c->t_limit;
   a.tvb_M = c->tvb_M;
   for (int l = 0; l < 8; ++l) a.tvb_c[l] = c->tvb_c[l];
+  a.dt_regrid = c->dt_regrid;
+  for (int l = 0; l < 8; ++l) a.amr_c[l] = c->amr_c[l];
+  a.tag_advect = c->tag_advect;
+  a.validation_mode = c->validation_mode;
+  a.no_reflux = c->no_reflux;
   try {
     return new AmrSim(s, a);
   } catch (...) {
@@ -78,6 +88,9 @@ void* oracle_create(const oracle_cfg* c) {
 void oracle_destroy(void* h) { delete (AmrSim*)h; }
 
 long oracle_limited_count(void* h) { return ((AmrSim*)h)->n_limited; }
+
+// Regrids that changed the layout, plus the first one (AmrDG.h:968-983).
+int oracle_layout_changes(void* h) { return ((AmrSim*)h)->n_layout_changes; }
 
 int oracle_set_threads(int n) {
 #ifdef _OPENMP

@@ -219,13 +219,15 @@ class Sim {
       if (L.status[c] == ST_NONE) continue;
       int ijk[3];
       L.coords(c, ijk[0], ijk[1], ijk[2]);
-      // level-0 linear cell index (periodically wrapped) for the noise hash
-      int w[3];
-      for (int d = 0; d < 3; ++d) {
-        w[d] = ijk[d];
-        if (d < D) w[d] = ((w[d] % L.n[d]) + L.n[d]) % L.n[d];
+      // linear index of the covering level-0 cell (periodically wrapped) for
+      // the noise hash
+      int w[3] = {0, 0, 0}, n0[3] = {1, 1, 1};
+      for (int d = 0; d < D; ++d) {
+        n0[d] = cfg.n_cell[d];
+        w[d] = ijk[d] >> l;
+        w[d] = ((w[d] % n0[d]) + n0[d]) % n0[d];
       }
-      uint64_t cell_l0 = (uint64_t)w[0] + (uint64_t)L.n[0] * ((uint64_t)w[1] + (uint64_t)L.n[1] * (uint64_t)w[2]);
+      uint64_t cell_l0 = (uint64_t)w[0] + (uint64_t)n0[0] * ((uint64_t)w[1] + (uint64_t)n0[1] * (uint64_t)w[2]);
       std::vector<double> icv((size_t)Q * qs);
       for (int m = 0; m < qs; ++m) {
         double x[3] = {0, 0, 0};

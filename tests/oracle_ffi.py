@@ -30,6 +30,8 @@ class OracleCfg(ctypes.Structure):
         ("tag_threshold", ctypes.c_double), ("grid_eff", ctypes.c_double),
         ("n_error_buf", ctypes.c_int), ("reflux_box_quirk", ctypes.c_int),
         ("t_limit", ctypes.c_int), ("tvb_M", ctypes.c_double), ("tvb_c", ctypes.c_double * 8),
+        ("dt_regrid", ctypes.c_double), ("amr_c", ctypes.c_double * 8),
+        ("tag_advect", ctypes.c_int), ("validation_mode", ctypes.c_int), ("no_reflux", ctypes.c_int),
     ]
 
 
@@ -64,6 +66,8 @@ def lib():
         L.oracle_num_levels.restype = ctypes.c_int
         L.oracle_limited_count.argtypes = [vp]
         L.oracle_limited_count.restype = ctypes.c_long
+        L.oracle_layout_changes.argtypes = [vp]
+        L.oracle_layout_changes.restype = ctypes.c_int
         L.oracle_get_boxes.argtypes = [vp, ctypes.c_int, ip, ctypes.c_int]
         L.oracle_get_boxes.restype = ctypes.c_int
         for f in ("oracle_get_uw", "oracle_set_uw", "oracle_get_uw_grown", "oracle_get_hw_grown"):
@@ -86,7 +90,8 @@ def make_cfg(D=2, P=1, n=(32, 32, 1), lo=(0.0, 0.0, 0.0), hi=(10.0, 10.0, 1.0), 
              ic="vortex", u_inf=1.0, v_inf=0.0, c_dt=0.5, gamma=1.4, seed=12345, noise_amp=1e-3,
              max_grid=1024, max_level=0, blocking_factor=8, dtn_regrid=4, tag_kind=0,
              tag_threshold=0.1, grid_eff=0.7, n_error_buf=1, reflux_box_quirk=1, xc=5.0, yc=5.0, beta=5.0,
-             t_limit=0, tvb_M=0.0, tvb_c=None):
+             t_limit=0, tvb_M=0.0, tvb_c=None, dt_regrid=0.0, amr_c=None, tag_advect=0,
+             validation_mode=0, no_reflux=0):
     c = OracleCfg()
     c.D, c.P, c.gamma, c.c_dt = D, P, gamma, c_dt
     for d in range(3):
@@ -103,6 +108,9 @@ def make_cfg(D=2, P=1, n=(32, 32, 1), lo=(0.0, 0.0, 0.0), hi=(10.0, 10.0, 1.0), 
     c.t_limit, c.tvb_M = t_limit, tvb_M
     for l in range(8):
         c.tvb_c[l] = 1.0 if tvb_c is None else tvb_c[l]
+        c.amr_c[l] = 1.0 if amr_c is None or l >= len(amr_c) else amr_c[l]
+    c.dt_regrid, c.tag_advect = dt_regrid, tag_advect
+    c.validation_mode, c.no_reflux = validation_mode, no_reflux
     return c
 
 
@@ -174,6 +182,10 @@ class OracleSim:
     def limited_count(self):
         """Cells the TVB limiter has modified so far."""
         return int(self.L.oracle_limited_count(self.h))
+
+    def layout_changes(self):
+        """Regrids that changed the layout, plus the first one."""
+        return int(self.L.oracle_layout_changes(self.h))
 
     def tags(self, lev):
         n = self.ncells_level(lev)

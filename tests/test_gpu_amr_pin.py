@@ -1,0 +1,152 @@
+"""The GPU's multi-level path against the reference's recorded multi-level
+outputs and against the oracle, with the reference's own refinement criteria.
+
+* The two-level isentropic vortex (p = 2, the reference's preset with
+  amr_c[0] = 1.4 and blocking factor 4): density L2 error at t = 0 and after
+  one period with static refinement, against the numbers the reference's
+  post-processing script records (tests/golden/vortex_amr_p2_l2.json).
+* Regrid cadences (every step, every dt_regrid of time) with the vortex
+  criterion's centre fixed or advected, without reflux, and the
+  Kelvin-Helmholtz characteristic TVB criterion: tags and boxes identical to
+  the oracle's before and after every step, every modal coefficient within
+  1e-12 relative.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle_ffi as O
+from parity import G, rel_err
+from test_oracle_amr_pin import run_to, vortex_amr_cfg
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "vortex_amr_p2_l2.json")))
+
+
+def gpu_vortex_amr(N, validation_mode=1, dtn_regrid=0, dt_regrid=0.0, tag_advect=0, reflux=True):
+    s = G.AmrDG(P=2, D=2)
+    s.setGeometrySettings(prob_lo=(0, 0), prob_hi=(10, 10), n_cell=(N, N), max_level=1, max_grid=128,
+                          blocking_factor=4, dtn_regrid=dtn_regrid, dt_regrid=dt_regrid, amr_c=[1.4])
+    s.setAmrSettings(tag_kind="isentropic_vortex", grid_eff=0.7, n_error_buf=1, tag_advect=tag_advect, reflux=reflux)
+    s.setValidationMode(validation_mode)
+    s.settings(c_dt=0.9)
+    s.init(G.Compressible_Euler().settings("isentropic_vortex", u_inf=1.0, v_inf=0.0))
+    return s
+
+
+def gpu_run_to(s, T):
+    n = 0
+    while s.time < T:
+        if T - s.time < s.Dt:
+            s.Dt = T - s.time
+        s.time_integration()
+        n += 1
+    return n
+
+
+def ref_value(run, N):
+    return GOLD["runs"][run]["L2"][GOLD["N"].index(N)]
+
+
+@pytest.mark.parametrize("run", ["t0_analytic_ic", "t0_projected_ic"])
+@pytest.mark.parametrize("N", [8, 16, 32])
+def test_gpu_initial_hierarchy_error_matches_reference(run, N):
+    s = gpu_vortex_amr(N, validation_mode=GOLD["runs"][run]["validation_mode"])
+    assert s.num_levels() == 2
+    assert s.boxes(1).tolist() == [[N // 2, N // 2, 0, 3 * N // 2 - 1, 3 * N // 2 - 1, 0]]
+    got, ref = s.norm(2, 0), ref_value(run, N)
+    assert abs(got - ref) / ref < 1e-12, (got, ref)
+
+
+@pytest.mark.parametrize("run,N", [("static_analytic_ic", 8), ("static_analytic_ic", 16), ("static_analytic_ic", 32),
+                                   ("static_analytic_ic", 64), ("static_projected_ic", 8),
+                                   ("static_projected_ic", 16), ("static_projected_ic", 32)])
+def test_gpu_static_refinement_error_matches_reference(run, N):
+    s = gpu_vortex_amr(N, validation_mode=GOLD["runs"][run]["validation_mode"])
+    gpu_run_to(s, 10.0)
+    got, ref = s.norm(2, 0), ref_value(run, N)
+    assert abs(got - ref) / ref < 1e-11, (got, ref)
+    assert s.status() == 0
+
+
+def assert_same_hierarchy(g, o, what):
+    assert g.num_levels() == o.num_levels(), what
+    for l in range(o.num_levels()):
+        assert np.array_equal(g.boxes(l), o.boxes(l)), f"boxes of level {l} {what}"
+
+
+@pytest.mark.parametrize("kw,steps", [
+    (dict(validation_mode=1, dtn_regrid=1, tag_advect=1), 40),
+    (dict(validation_mode=2, dt_regrid=0.5, tag_advect=1), 40),
+    (dict(validation_mode=0, dtn_regrid=1, tag_advect=1, reflux=False), 40),
+])
+def test_gpu_vortex_regrid_cadences_match_oracle(kw, steps):
+    okw = dict(kw)
+    okw["no_reflux"] = 0 if okw.pop("reflux", True) else 1
+    o = O.OracleSim(vortex_amr_cfg(8, **okw))
+    o.init()
+    g = gpu_vortex_amr(8, **kw)
+    assert_same_hierarchy(g, o, "after init")
+    for l in range(o.num_levels()):
+        assert rel_err(g.get_U_w(l), o.get_uw(l)) < 1e-13
+    moved = 0
+    for s in range(steps):
+        b0 = o.boxes(1).tolist()
+        assert np.array_equal(g.tags(0), o.tags(0).astype(np.uint8)), f"tags before step {s}"
+        o.step()
+        g.time_integration()
+        assert_same_hierarchy(g, o, f"after step {s}")
+        moved += o.boxes(1).tolist() != b0
+        assert abs(g.Dt - o.dt) <= 1e-12 * o.dt
+    for l in range(o.num_levels()):
+        assert rel_err(g.get_U_w(l), o.get_uw(l)) < 1e-12, f"level {l}"
+    assert moved >= 1  # the advected criterion moved the fine level
+    assert g.status() == 0
+
+
+def test_gpu_no_reflux_differs_from_reflux_like_the_oracle():
+    a = gpu_vortex_amr(8, validation_mode=2)
+    b = gpu_vortex_amr(8, validation_mode=2, reflux=False)
+    gpu_run_to(a, 1.0)
+    gpu_run_to(b, 1.0)
+    oa = O.OracleSim(vortex_amr_cfg(8, validation_mode=2))
+    ob = O.OracleSim(vortex_amr_cfg(8, validation_mode=2, no_reflux=1))
+    oa.init()
+    ob.init()
+    run_to(oa, 1.0)
+    run_to(ob, 1.0)
+    for l in range(2):
+        assert rel_err(b.get_U_w(l), ob.get_uw(l)) < 1e-12
+        assert rel_err(a.get_U_w(l), oa.get_uw(l)) < 1e-12
+    assert rel_err(a.get_U_w(0), b.get_U_w(0)) > 1e-8
+
+
+def test_gpu_kh_tvb_criterion_matches_oracle():
+    """The reference's Kelvin-Helmholtz criterion (characteristic TVB test,
+    amr_c = M per level) on its KH initial condition, three levels."""
+    cfg = O.make_cfg(D=2, P=2, n=(32, 32, 1), hi=(1, 1, 1), ic="kh_ref", c_dt=0.5, max_grid=16, max_level=2,
+                     blocking_factor=4, dtn_regrid=2, tag_kind=3, amr_c=[20.0, 40.0])
+    o = O.OracleSim(cfg)
+    o.init()
+    g = G.AmrDG(P=2, D=2)
+    g.setGeometrySettings(prob_lo=(0, 0), prob_hi=(1, 1), n_cell=(32, 32), max_level=2, max_grid=16,
+                          blocking_factor=4, dtn_regrid=2, amr_c=[20.0, 40.0])
+    g.setAmrSettings(tag_kind="kelvin_helmolz_instability")
+    g.settings(c_dt=0.5)
+    g.init(G.Compressible_Euler().settings("kelvin_helmolz_instability"))
+    assert_same_hierarchy(g, o, "after init")
+    ntags = 0
+    for s in range(6):
+        for l in range(min(2, o.num_levels())):
+            to, tg = o.tags(l).astype(np.uint8), g.tags(l)
+            assert np.array_equal(to, tg), f"tags of level {l} before step {s}"
+            ntags += int(tg.sum())
+        o.step()
+        g.time_integration()
+        assert_same_hierarchy(g, o, f"after step {s}")
+    assert ntags > 0 and o.num_levels() == 3
+    for l in range(o.num_levels()):
+        assert rel_err(g.get_U_w(l), o.get_uw(l)) < 1e-12, f"level {l}"
