@@ -68,7 +68,10 @@ def test_gpu_static_refinement_error_matches_reference(run, N):
     s = gpu_vortex_amr(N, validation_mode=GOLD["runs"][run]["validation_mode"])
     gpu_run_to(s, 10.0)
     got, ref = s.norm(2, 0), ref_value(run, N)
-    assert abs(got - ref) / ref < 1e-11, (got, ref)
+    # 1e-11 relative, or 1e-15 absolute: at N = 64 the error (7.7e-6) is so
+    # small that 1e-11 of it is below the rounding of the O(1) density the
+    # 3829 steps accumulate (the GPU contracts to FMA, the reference need not)
+    assert abs(got - ref) < max(1e-11 * ref, 1e-15), (got, ref)
     assert s.status() == 0
 
 
