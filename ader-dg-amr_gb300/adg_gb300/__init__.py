@@ -135,6 +135,7 @@ def lib():
         "adg_interp_gather": ([vp, vp, ctypes.c_int64, vp, i], i),
         "adg_average_down": ([vp], i),
         "adg_fill_ghosts": ([vp], i),
+        "adg_limit": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
         "adg_write_plotfile": ([vp, ctypes.c_char_p, i, i, ctypes.POINTER(ctypes.c_char_p)], i),
         "adg_read_plotfile": ([vp, ctypes.c_char_p, i, dp], i),
         "adg_plotfile_info": ([ctypes.c_char_p, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i), dp,
@@ -478,6 +479,14 @@ class AmrDG:
     def average_down(self):
         """Solver::AMR_average_fine_coarse on the context's layout."""
         self._check(self._L.adg_average_down(self.ctx), "adg_average_down")
+
+    def Limiter_w(self):
+        """The TVB limiter of the finest level on the current state
+        (AmrDG::Limiter_w, AmrDG.h:1657-1855), after ADER(); returns the
+        elements it modified."""
+        n = ctypes.c_int64()
+        self._check(self._L.adg_limit(self.ctx, ctypes.byref(n)), "adg_limit")
+        return n.value
 
     def fill_ghosts(self):
         """The coarse-interpolated ghost cells of FillPatchTwoLevels on the context's layout."""

@@ -1664,6 +1664,21 @@ int adg_average_down(adg_ctx* ctx) {
   return ADG_OK;
 }
 
+int adg_limit(adg_ctx* ctx, int64_t* n_limited) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (ctx->cfg.limiter_t <= 0 || !ctx->ubar_old.p)
+    return fail(ctx, ADG_ERR_STATE, "adg_limit needs a context created with the TVB limiter (limiter_t > 0)");
+  unsigned long long before = 0, after = 0;
+  ADG_CUDA(cudaMemcpyAsync(&before, ctx->limited.p, sizeof(before), cudaMemcpyDeviceToHost, ctx->stream), "count");
+  rc = launch_limiter(ctx);
+  if (rc) return rc;
+  ADG_CUDA(cudaMemcpyAsync(&after, ctx->limited.p, sizeof(after), cudaMemcpyDeviceToHost, ctx->stream), "count");
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "limiter sync");
+  if (n_limited) *n_limited = (int64_t)(after - before);
+  return ADG_OK;
+}
+
 int adg_fill_ghosts(adg_ctx* ctx) {
   int rc = check_ready(ctx);
   if (rc) return rc;

@@ -219,6 +219,13 @@ int adg_interp_scatter(adg_ctx* ctx, const double* coarse, const int8_t* child, 
 int adg_interp_gather(adg_ctx* ctx, const double* fine, int64_t n, double* coarse, int mem);
 int adg_average_down(adg_ctx* ctx);
 int adg_fill_ghosts(adg_ctx* ctx);
+/* The TVB limiter of the finest level on the current state (Limiter_w,
+ * AmrDG.h:1657-1855), the stage the evolve loop runs between ADER and the
+ * average down (AmrDG.h:990-997): call it after adg_ader, whose predictor
+ * records the cell means an outflow boundary's neighbour takes.  Needs
+ * limiter_t > 0 at creation; *n_limited (may be NULL) receives the elements
+ * this call modified. */
+int adg_limit(adg_ctx* ctx, int64_t* n_limited);
 
 /* Completed steps of the evolve loop (the reference's n, AmrDG.h:868-877,
  * 1012); a restart from a plotfile continues its count. */

@@ -113,6 +113,20 @@ double oracle_get_time(void* h) { return ((AmrSim*)h)->sim.t; }
 // (regrid?, ADER, average down, FillPatch, t += Dt, set_Dt). Returns new Dt.
 double oracle_step(void* h) { return ((AmrSim*)h)->step(); }
 
+// The TVB limiter of the finest level on the current state; returns the
+// cells it modified.
+long oracle_limit(void* h) {
+  AmrSim* s = (AmrSim*)h;
+  return s->limit_tvb(s->finest());
+}
+
+// The ghost cells of every level from the valid data (the end-of-step
+// FillPatch, AmrDG.h:1004-1013).
+void oracle_fill_patch(void* h) {
+  AmrSim* s = (AmrSim*)h;
+  for (int l = 0; l <= s->finest(); ++l) s->fill_patch(l);
+}
+
 // Only the ADER part of a step with the current Dt (no Dt update).
 void oracle_ader(void* h) { ((AmrSim*)h)->ader(); }
 
@@ -148,6 +162,17 @@ void oracle_predictor(void* h, int l) { ((AmrSim*)h)->predictor_only(l); }
 // Lp error norm of component q over leaf cells (AmrDG.h:1399-1655):
 // against the analytic IC (other == NULL) or another solution.
 double oracle_norm(void* h, void* other, int p, int q) { return ((AmrSim*)h)->norm((AmrSim*)other, p, q); }
+
+// Lp norm of component q of (other - this) over the leaf cells, the other
+// solution given per level as valid cells in canonical order on this
+// solution's layout (the reference's norm machinery applied to two DG
+// solutions).
+double oracle_norm_diff(void* h, const double* const* other_levels, int p, int q) {
+  AmrSim* s = (AmrSim*)h;
+  AmrSim tmp(*s);
+  for (int l = 0; l < (int)tmp.sim.lev.size(); ++l) tmp.set_uw(l, other_levels[l]);
+  return s->norm(&tmp, p, q);
+}
 
 // Tags of level l from the current state (1 per valid cell, box order).
 long oracle_tags(void* h, int l, int8_t* out) { return ((AmrSim*)h)->tags_valid(l, out); }

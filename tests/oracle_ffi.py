@@ -61,6 +61,9 @@ def lib():
             getattr(L, f).argtypes = [vp]
         L.oracle_set_dt.argtypes = [vp, ctypes.c_double]
         L.oracle_ader.argtypes = [vp]
+        L.oracle_limit.argtypes = [vp]
+        L.oracle_limit.restype = ctypes.c_long
+        L.oracle_fill_patch.argtypes = [vp]
         L.oracle_predictor.argtypes = [vp, ctypes.c_int]
         L.oracle_num_levels.argtypes = [vp]
         L.oracle_num_levels.restype = ctypes.c_int
@@ -77,6 +80,8 @@ def lib():
         L.oracle_tags.restype = ctypes.c_long
         L.oracle_norm.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int]
         L.oracle_norm.restype = ctypes.c_double
+        L.oracle_norm_diff.argtypes = [vp, ctypes.POINTER(dp), ctypes.c_int, ctypes.c_int]
+        L.oracle_norm_diff.restype = ctypes.c_double
         L.oracle_matrix.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, dp,
                                     ctypes.c_int, ip, ip]
         L.oracle_matrix.restype = ctypes.c_int
@@ -154,6 +159,14 @@ class OracleSim:
     def ader(self):
         self.L.oracle_ader(self.h)
 
+    def limit(self):
+        """TVB limiter of the finest level; returns the cells modified."""
+        return int(self.L.oracle_limit(self.h))
+
+    def fill_patch(self):
+        """Ghost cells of every level from the valid data."""
+        self.L.oracle_fill_patch(self.h)
+
     def num_levels(self):
         return self.L.oracle_num_levels(self.h)
 
@@ -193,6 +206,18 @@ class OracleSim:
         w = self.L.oracle_tags(self.h, lev, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)))
         assert w == n
         return out
+
+    def norm_diff(self, levels, p=2, q=0):
+        """Lp norm of component q of (levels - this solution) over the leaf
+        cells; levels[l] holds level l's valid cells in canonical order on
+        this solution's layout."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in levels]
+        assert len(arrs) == self.num_levels()
+        for l, a in enumerate(arrs):
+            assert a.size == self.ncells_level(l) * self.Q * self.Np_s
+        ptrs = (ctypes.POINTER(ctypes.c_double) * len(arrs))(
+            *[a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in arrs])
+        return self.L.oracle_norm_diff(self.h, ptrs, p, q)
 
     def norm(self, p=2, q=0, other=None):
         return self.L.oracle_norm(self.h, other.h if other is not None else None, p, q)
