@@ -60,6 +60,15 @@ TAG_KINDS = {"density_gradient": 0, "pressure_jump": 1, "isentropic_vortex": 2, 
              "kelvin_helmolz_instability": 3, "kh_tvb": 3}
 
 
+class AdgPatch(ctypes.Structure):
+    """adg_patch: one box of the caller's per-(level, q) arrays."""
+    _fields_ = [
+        ("level", ctypes.c_int), ("lo", ctypes.c_int * 3), ("hi", ctypes.c_int * 3), ("nghost", ctypes.c_int),
+        ("U_w", ctypes.c_void_p * 5), ("jstride", ctypes.c_int64), ("kstride", ctypes.c_int64),
+        ("nstride", ctypes.c_int64),
+    ]
+
+
 class AdgError(RuntimeError):
     pass
 
@@ -136,6 +145,9 @@ def lib():
         "adg_average_down": ([vp], i),
         "adg_fill_ghosts": ([vp], i),
         "adg_limit": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_set_patches": ([vp, ctypes.POINTER(AdgPatch), i], i),
+        "adg_read_patches": ([vp], i),
+        "adg_write_patches": ([vp], i),
         "adg_write_plotfile": ([vp, ctypes.c_char_p, i, i, ctypes.POINTER(ctypes.c_char_p)], i),
         "adg_read_plotfile": ([vp, ctypes.c_char_p, i, dp], i),
         "adg_plotfile_info": ([ctypes.c_char_p, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i), dp,
@@ -479,6 +491,20 @@ class AmrDG:
     def average_down(self):
         """Solver::AMR_average_fine_coarse on the context's layout."""
         self._check(self._L.adg_average_down(self.ctx), "adg_average_down")
+
+    def set_patches(self, patches):
+        """Register the caller's per-box device arrays (a list of AdgPatch)
+        that tile the current layout."""
+        arr = (AdgPatch * max(1, len(patches)))(*patches)
+        self._check(self._L.adg_set_patches(self.ctx, arr, len(patches)), "adg_set_patches")
+
+    def read_patches(self):
+        """Queue the copy of the registered patches' valid cells into the state."""
+        self._check(self._L.adg_read_patches(self.ctx), "adg_read_patches")
+
+    def write_patches(self):
+        """Queue the copy of the state into the registered patches' valid cells."""
+        self._check(self._L.adg_write_patches(self.ctx), "adg_write_patches")
 
     def Limiter_w(self):
         """The TVB limiter of the finest level on the current state

@@ -17,6 +17,7 @@
 #include "adg_kernelset.hpp"
 #include "adg_layout.hpp"
 #include "adg_mlp.cuh"
+#include "adg_patches.cuh"
 #include "plotfile.hpp"
 #include <random>
 
@@ -136,6 +137,13 @@ struct adg_ctx {
   bool first_step = true;
   int n_regrids = 0;
   double t_last_regrid = 0.0;  // time of the last regrid (dt_regrid cadence)
+  // caller's per-box arrays (adg_set_patches), valid for the layout they were
+  // registered on
+  DevBuf<int> patch_pid;
+  DevBuf<long long> patch_off, patch_nstride;
+  DevBuf<double*> patch_qptr;
+  std::vector<std::vector<amr::IBox>> patch_grids;
+  bool patches_set = false;
 
   // device state
   DevBuf<double> Uw, Rvol, Tr, Fnum, Hw_dbg;
@@ -212,6 +220,7 @@ struct adg_ctx {
     sx.release(); sy0.release(); sy1.release(); syo.release(); hseed.release(); hseed_f.release(); fb_list.release(); fb_count.release();
     fb_total.release(); Uw_alt.release(); remap_i.release(); remap_c.release(); l2_flush.release();
     ubar_old.release(); limited.release();
+    patch_pid.release(); patch_off.release(); patch_nstride.release(); patch_qptr.release();
     xfer_in.release(); xfer_out.release(); xfer_child.release();
     if (tab_ev) cudaEventSynchronize(tab_ev), cudaEventDestroy(tab_ev);
     if (tag_ev) cudaEventSynchronize(tag_ev), cudaEventDestroy(tag_ev);
@@ -1663,6 +1672,95 @@ int adg_average_down(adg_ctx* ctx) {
   ADG_CUDA(cudaStreamSynchronize(ctx->stream), "average down sync");
   return ADG_OK;
 }
+
+int adg_set_patches(adg_ctx* ctx, const adg_patch* patches, int n) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  const Hierarchy& H = ctx->hier;
+  const int D = ctx->cfg.D, Q = ctx->ks->Q;
+  if (n < 0 || (n > 0 && !patches)) return fail(ctx, ADG_ERR_ARG, "bad patch list");
+  const size_t nv = H.n_valid();
+  std::vector<int> pid(nv, -1);
+  std::vector<long long> off(nv, 0), nstr((size_t)n, 0);
+  std::vector<double*> qptr((size_t)n * Q, nullptr);
+  for (int p = 0; p < n; ++p) {
+    const adg_patch& pt = patches[p];
+    if (pt.level < 0 || pt.level >= H.nlevels() || pt.nghost < 0)
+      return fail(ctx, ADG_ERR_ARG, "patch " + std::to_string(p) + ": bad level or ghost width");
+    int dims[3];
+    H.dims(pt.level, dims);
+    long long ext[3] = {1, 1, 1};
+    for (int d = 0; d < 3; ++d) {
+      const int lo = d < D ? pt.lo[d] : 0, hi = d < D ? pt.hi[d] : 0;
+      if (lo > hi || lo < 0 || hi >= dims[d])
+        return fail(ctx, ADG_ERR_ARG, "patch " + std::to_string(p) + ": box outside the level");
+      if (d < D) ext[d] = hi - lo + 1 + 2LL * pt.nghost;
+    }
+    if (pt.jstride < ext[0] || (D > 2 && pt.kstride < pt.jstride * ext[1]) ||
+        pt.nstride < (D > 2 ? pt.kstride * ext[2] : pt.jstride * ext[1]))
+      return fail(ctx, ADG_ERR_ARG, "patch " + std::to_string(p) + ": strides smaller than the grown box");
+    for (int q = 0; q < Q; ++q) {
+      if (!pt.U_w[q]) return fail(ctx, ADG_ERR_ARG, "patch " + std::to_string(p) + ": null array");
+      qptr[(size_t)p * Q + q] = pt.U_w[q];
+    }
+    nstr[p] = pt.nstride;
+    const int lo2 = D > 2 ? pt.lo[2] : 0, hi2 = D > 2 ? pt.hi[2] : 0;
+    for (int k = lo2; k <= hi2; ++k)
+      for (int j = pt.lo[1]; j <= pt.hi[1]; ++j)
+        for (int i = pt.lo[0]; i <= pt.hi[0]; ++i) {
+          const int c[3] = {i, j, k};
+          const int e = H.elem_at(pt.level, c);
+          if (e < 0 || (size_t)e >= nv)
+            return fail(ctx, ADG_ERR_LAYOUT, "patch " + std::to_string(p) + " covers a cell outside the layout");
+          if (pid[e] >= 0) return fail(ctx, ADG_ERR_LAYOUT, "patches overlap");
+          pid[e] = p;
+          off[e] = (long long)(i - pt.lo[0] + pt.nghost) + (long long)(j - pt.lo[1] + pt.nghost) * pt.jstride +
+                   (D > 2 ? (long long)(k - lo2 + pt.nghost) * pt.kstride : 0LL);
+        }
+  }
+  for (size_t e = 0; e < nv; ++e)
+    if (pid[e] < 0) return fail(ctx, ADG_ERR_LAYOUT, "patches leave a valid cell of the layout uncovered");
+  ADG_CUDA(ctx->patch_pid.ensure(nv), "alloc patch table");
+  ADG_CUDA(ctx->patch_off.ensure(nv), "alloc patch table");
+  ADG_CUDA(ctx->patch_nstride.ensure(std::max(n, 1)), "alloc patch table");
+  ADG_CUDA(ctx->patch_qptr.ensure((size_t)std::max(n, 1) * Q), "alloc patch table");
+  ADG_CUDA(cudaMemcpyAsync(ctx->patch_pid.p, pid.data(), nv * sizeof(int), cudaMemcpyHostToDevice, ctx->stream), "h2d");
+  ADG_CUDA(cudaMemcpyAsync(ctx->patch_off.p, off.data(), nv * sizeof(long long), cudaMemcpyHostToDevice, ctx->stream),
+           "h2d");
+  if (n > 0) {
+    ADG_CUDA(cudaMemcpyAsync(ctx->patch_nstride.p, nstr.data(), n * sizeof(long long), cudaMemcpyHostToDevice,
+                             ctx->stream), "h2d");
+    ADG_CUDA(cudaMemcpyAsync(ctx->patch_qptr.p, qptr.data(), qptr.size() * sizeof(double*), cudaMemcpyHostToDevice,
+                             ctx->stream), "h2d");
+  }
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "patch table upload");
+  ctx->patch_grids = H.grids;
+  ctx->patches_set = true;
+  return ADG_OK;
+}
+
+static int patch_copy(adg_ctx* ctx, int dir) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!ctx->patches_set || ctx->patch_grids != ctx->hier.grids)
+    return fail(ctx, ADG_ERR_LAYOUT, "no patches registered for the current layout (adg_set_patches)");
+  PatchTab t{};
+  t.pid = ctx->patch_pid.p;
+  t.off = ctx->patch_off.p;
+  t.qptr = ctx->patch_qptr.p;
+  t.nstride = ctx->patch_nstride.p;
+  t.n = (int)ctx->hier.n_valid();
+  t.Q = ctx->ks->Q;
+  t.NS = ctx->ks->Np_s;
+  cudaError_t e = launch_patch_copy(dir, t, ctx->Uw.p, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "patch copy launch");
+  ctx->launches++;
+  if (dir == 0 && ctx->hier.nlevels() > 1) ctx->ghosts_stale = true;
+  return ADG_OK;
+}
+
+int adg_read_patches(adg_ctx* ctx) { return patch_copy(ctx, 0); }
+int adg_write_patches(adg_ctx* ctx) { return patch_copy(ctx, 1); }
 
 int adg_limit(adg_ctx* ctx, int64_t* n_limited) {
   int rc = check_ready(ctx);

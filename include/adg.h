@@ -227,6 +227,36 @@ int adg_fill_ghosts(adg_ctx* ctx);
  * this call modified. */
 int adg_limit(adg_ctx* ctx, int64_t* n_limited);
 
+/* Zero-copy boundary to the caller's per-box device arrays.
+ *
+ * The reference keeps the state as one MultiFab per (level, q) whose
+ * FArrayBoxes hold the Np_s modes of U_w as components, with nghost ghost
+ * cells (Source/NumericalMethod/AmrDG/AmrDG.tpp:300-333, Solver.h:408-457).
+ * An adg_patch describes one box of that hierarchy: its level and valid box,
+ * the ghost width of its arrays, the Q device pointers (FArrayBox data of
+ * U_w(level, q), x fastest over the grown box, then y, z and the component)
+ * and the strides of j, k and the component in doubles.
+ * adg_set_patches registers patches that tile the context's current layout
+ * exactly (every valid cell in one patch; a layout from adg_set_layout with
+ * the same BoxArrays, or the context's own); after a layout change they must
+ * be registered again (ADG_ERR_LAYOUT until then).  adg_read_patches copies
+ * every valid cell of the patches into the context's state, adg_write_patches
+ * the state into the patches' valid cells (ghost cells are the caller's
+ * FillPatch); both are device-to-device kernels queued on the context's
+ * stream (adg_synchronize before the host reads the arrays), so an AMReX
+ * build with device MultiFabs needs no host copy per step.  No reference
+ * counterpart beyond the data layout. */
+typedef struct adg_patch {
+  int level;
+  int lo[3], hi[3];      /* valid box in the level's cell index space */
+  int nghost;            /* ghost cells on every side of the arrays */
+  double* U_w[5];        /* device pointer per conserved variable q < Q */
+  int64_t jstride, kstride, nstride;  /* doubles between j, k and component neighbours */
+} adg_patch;
+int adg_set_patches(adg_ctx* ctx, const adg_patch* patches, int n);
+int adg_read_patches(adg_ctx* ctx);
+int adg_write_patches(adg_ctx* ctx);
+
 /* Completed steps of the evolve loop (the reference's n, AmrDG.h:868-877,
  * 1012); a restart from a plotfile continues its count. */
 int adg_get_step(const adg_ctx* ctx, int64_t* n);
