@@ -566,10 +566,10 @@ class AmrDG:
 
     def time_kernels(self, nsteps=3):
         """Average per-step duration (ms) of each kernel kind, CUDA events."""
-        out = (ctypes.c_double * 6)()
-        self._check(self._L.adg_time_kernels(self.ctx, int(nsteps), out, 6), "adg_time_kernels")
+        out = (ctypes.c_double * 8)()
+        self._check(self._L.adg_time_kernels(self.ctx, int(nsteps), out, 8), "adg_time_kernels")
         return {"predictor": out[0], "numflux": out[1], "corrector": out[2], "dt": out[3], "amr_sync": out[4],
-                "seed_inference": out[5]}
+                "seed_inference": out[5], "seeded_predictor": out[6], "fallback": out[7]}
 
     def dof_updates(self):
         """(total DOF updates so far, ms of host time spent in regrids)."""

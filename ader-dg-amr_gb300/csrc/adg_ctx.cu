@@ -2026,19 +2026,20 @@ int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds) {
   int rc = check_ready(ctx);
   if (rc) return rc;
   if (!ms || nkinds < 1 || nsteps < 1) return ADG_ERR_ARG;
-  const int NEV = 7;
+  const int NEV = 8, NK = 8;
   const bool seeded = ctx->seed_mode && ctx->seed;
   std::vector<cudaEvent_t> ev((size_t)NEV * nsteps);
   for (auto& x : ev) ADG_CUDA(cudaEventCreate(&x), "event");
   for (int s = 0; s < nsteps && rc == ADG_OK; ++s) rc = host_step(ctx, false, &ev[(size_t)s * NEV]);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  double acc[NK] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (rc == ADG_OK && e == cudaSuccess) {
-    // kinds: predictor stage, numflux, corrector, Dt, AMR sync, seed inference
-    const int from[6] = {0, 1, 2, 4, 3, 0}, to[6] = {1, 2, 3, 5, 4, 6};
+    // kinds: predictor stage, numflux, corrector, Dt, AMR sync, seed
+    // inference, seeded predictor, fallback pass
+    const int from[NK] = {0, 1, 2, 4, 3, 0, 6, 7}, to[NK] = {1, 2, 3, 5, 4, 6, 7, 1};
     for (int s = 0; s < nsteps; ++s)
-      for (int k = 0; k < 6; ++k) {
-        if (k == 5 && !seeded) continue;
+      for (int k = 0; k < NK; ++k) {
+        if (k >= 5 && !seeded) continue;
         float f = 0.f;
         cudaEventElapsedTime(&f, ev[(size_t)s * NEV + from[k]], ev[(size_t)s * NEV + to[k]]);
         acc[k] += f;
@@ -2047,7 +2048,7 @@ int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds) {
   for (auto& x : ev) cudaEventDestroy(x);
   if (rc) return rc;
   if (e != cudaSuccess) return cuda_fail(ctx, e, "time kernels");
-  for (int k = 0; k < nkinds; ++k) ms[k] = (k < 6) ? acc[k] / nsteps : 0.0;
+  for (int k = 0; k < nkinds; ++k) ms[k] = (k < NK) ? acc[k] / nsteps : 0.0;
   return ADG_OK;
 }
 
@@ -2346,6 +2347,7 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base, cudaEvent_t
   const int Es = ctx->seed_mode == 2 && ctx->cfg.D == 2 ? 8 : ctx->E;
   e = ks->predictor(pa, Es, st, ctx->seed_mode);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "seeded predictor");
+  if (ev) cudaEventRecord(ev[7], st);  // end of the seeded predictor, start of the fallback pass
   // full FP64 Picard for the rejected elements; in a mode-2 step with the
   // seeded elements' final stage (mode 3), so that every trace tile is a split tile
   PredictorArgs fb = base;

@@ -57,6 +57,13 @@ GPU_IC = {"kh_noise": "kh_noise", "vortex": "isentropic_vortex", "blast3d": "bla
 METRIC = "DOF-updates/s at 1 GB300: learned-seed+batched vs plain GPU FP64 vs CPU, at equal L2"
 
 
+def _jsonable(o):
+    """numpy scalars in the JSON line as plain numbers / booleans."""
+    if hasattr(o, "item"):
+        return o.item()
+    raise TypeError(f"{type(o).__name__} is not JSON serializable")
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -249,15 +256,16 @@ def run_accuracy(args, w):
                          "dt_rel": abs(g.Dt - o.dt) / o.dt, "gpu_status": g.status(),
                          "limited": [g.limited_count(), o.limited_count()] if "limiter" in w else None,
                          "wall_s": {"oracle": t_cpu, "gpu_stream_steps": t_gpu}}}
-    print(json.dumps(line))
+    print(json.dumps(line, default=_jsonable))
     return 0
 
 
-def cpu_baseline(w, max_seconds=20.0, threads=None):
+def cpu_baseline(w, max_seconds=20.0, threads=None, max_steps=50):
     """The oracle (C++/OpenMP restatement of the reference) on the host cores:
     a bounded sample of the same workload (whole grid, the steps after the
     first, which allocates and, with AMR, builds the first hierarchy from the
-    initial full-domain levels; later regrids are inside the sample)."""
+    initial full-domain levels; later regrids are inside the sample): up to
+    max_steps steps or max_seconds."""
     import oracle_ffi as O
     from math import comb
 
@@ -274,35 +282,39 @@ def cpu_baseline(w, max_seconds=20.0, threads=None):
         steps += 1
         dof += sum(s.ncells_level(l) for l in range(s.num_levels())) * per_cell
         el = time.perf_counter() - t0
-        if el > max_seconds or steps >= 50:
+        if el > max_seconds or steps >= max_steps:
             break
     grid = "x".join(map(str, w["n"][:w["D"]]))
     what = f"{steps} steps of the full {grid}" + (f" base grid with {s.num_levels()} levels" if amr else " grid")
-    return {"value": dof / el, "unit": "DOF-updates/s", "cores": threads, "kind": "port",
+    return {"value": dof / el, "unit": "DOF-updates/s", "cores": threads, "kind": "port", "steps": steps,
             "ms_per_step": el * 1e3 / steps,
             "sample": f"{what} ({el:.1f} s), CPU oracle (reference algorithm restated in C++/OpenMP)"}
 
 
 def base_config(args, w, world):
-    """The workload keys both arms report."""
+    """The workload keys both arms report (identical in both; how each arm ran
+    goes under "run")."""
     return {"workload": args.workload, "D": w["D"], "P": w["P"], "base_cells": list(w["n"][:w["D"]]),
-            "amr": w.get("amr"), "ic": w["ic"], "c_dt": w["c_dt"], "limiter": w.get("limiter"),
-            "parallelism": "replicas" if world > 1 else "1 GPU"}
+            "amr": w.get("amr"), "ic": w["ic"], "c_dt": w["c_dt"], "limiter": w.get("limiter")}
 
 
 def run_reference(args, w):
+    """The reference's algorithm on the host cores (the oracle: the reference
+    itself cannot be built here) for --steps steps after one untimed step,
+    unless that exceeds a few minutes; "steps" reports the steps timed."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    base = cpu_baseline(w, max_seconds=max(5.0, 60.0 / max(1, args.steps + args.warmup)))
+    base = cpu_baseline(w, max_seconds=180.0, max_steps=max(1, args.steps))
     val = base["value"]
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "DOF-updates/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["ms_per_step"], "higher_is_better": True,
+            "steps": base["steps"], "warmup": args.warmup, "ms_per_step": base["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {**base_config(args, w, 1), "parallelism": "host cores of rank 0"},
+            "config": base_config(args, w, 1),
+            "run": {"parallelism": f"host cores of rank 0 ({base['cores']} threads)", "warmup_steps_run": 1},
             "cpu_baseline": base,
             "e2e": {"value": val, "unit": "DOF-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+    print(json.dumps(line, default=_jsonable))
     return 0
 
 
@@ -346,16 +358,24 @@ def l2_density_level0(Ua, Ub, w):
 
 L2_FLUSH_BYTES = 256 << 20  # twice the 129 MB L2: written before every timed step
 
-# DRAM bytes (read + write) of one plain k_predictor launch, from the ncu
-# capture summarised in the named profile (same workload and code)
-PROFILED_TRAFFIC = {
-    "kh_p3_amr3": (24.68e6, "profiles/k_predictor_kh_p3_amr3.md"),
-    "kh_p3_256": (285.34e6, "profiles/k_predictor_kh_p3_256.md"),
-}
-# FP64 pipe activity of the predictor kernels (ncu, sm__pipe_fp64_cycles_active of peak, same files)
-PROFILED_FP64_ACTIVE = {
-    "kh_p3_amr3": {"plain_predictor": 0.757, "seeded_predictor": 0.637},
-    "kh_p3_256": {"plain_predictor": 0.839},
+# Per launch of the dominant kernels on the headline workload (ncu, same
+# code and layout; profiles/fp64_issue_k_predictor_kh_p3_amr3.md): FP64-pipe
+# thread instruction slots (smsp__inst_executed_pipe_fp64 x 32), the
+# DFMA+DADD+DMUL part of them, DRAM bytes read + written, FP64 pipe activity,
+# elements predicted.
+PROFILED_LAUNCH = {
+    "kh_p3_amr3": {
+        "plain_predictor": dict(kernel="k_predictor<D2P3, E=8, MODE 0> (3 FP64 Picard sweeps, corrector volume "
+                                       "term, face traces)",
+                                fp64_pipe_slots=301.576e6, fp64_arith=296.329e6, dram_bytes=24.63e6,
+                                fp64_active=0.756, elements=15616,
+                                source="profiles/fp64_issue_k_predictor_kh_p3_amr3.md"),
+        "seeded_predictor": dict(kernel="k_predictor<D2P3, E=8, MODE 2> (2 FP32 sweeps from the seed, split "
+                                        "FP64/FP32 final stage)",
+                                 fp64_pipe_slots=34.855e6, fp64_arith=29.436e6, dram_bytes=16.89e6,
+                                 fp64_active=0.633, elements=15616,
+                                 source="profiles/fp64_issue_k_predictor_kh_p3_amr3.md"),
+    },
 }
 
 
@@ -427,7 +447,7 @@ def train_seed(G, w, n_pairs=2_000_000, epochs=40, cache=None):
                   "epochs": epochs + epochs // 2}
 
 
-def timed_run(G, w, E, steps, warmup, seed=None, mode=0, sweeps=0, tol=1e-3, plain_sweeps=0):
+def timed_run(G, w, E, steps, warmup, seed=None, mode=0, sweeps=0, tol=1e-3, plain_sweeps=0, clocks=True):
     s = make_sim(G, w, E, sweeps=plain_sweeps)
     if seed is not None and mode:
         seed.attach(s, mode=mode, sweeps=sweeps, tol=tol)
@@ -437,17 +457,212 @@ def timed_run(G, w, E, steps, warmup, seed=None, mode=0, sweeps=0, tol=1e-3, pla
     lf0 = s.leaf_dof_updates()
     n0 = s.launch_count()
     r0 = s.regrid_count()
-    _, rms0 = s.dof_updates()
     ph0 = s.regrid_profile()
-    ms = s.advance_timed_flushed(steps, flush_bytes=L2_FLUSH_BYTES, use_graph=True)
+    local = dist_env()[2]
+    with ClockSampler(local) as clk:  # nvidia-smi samples during the timed steps themselves
+        ms = s.advance_timed_flushed(steps, flush_bytes=L2_FLUSH_BYTES, use_graph=True)
     d1, rms = s.dof_updates()
     ph1 = s.regrid_profile()
     out = {"ms": ms, "dof": d1 - d0, "launches": s.launch_count() - n0, "regrids": s.regrid_count() - r0,
            "regrid_host_ms": {k: ph1[k] - ph0[k] for k in ph1}, "sim": s, "dof_per_s": (d1 - d0) / (ms * 1e-3),
-           "leaf_dof_per_s": (s.leaf_dof_updates() - lf0) / (ms * 1e-3)}
+           "leaf_dof_per_s": (s.leaf_dof_updates() - lf0) / (ms * 1e-3), "clocks": clk.summary()}
     if seed is not None and mode:
         fb, n = G.seed_stats(s)
         out["fallback_rate"] = fb / max(1, n)
+    return out
+
+
+def leaf_masks(sim, w):
+    """Per level, which valid cells (in the level's state order: x fastest
+    over the level's index space) are not covered by the next finer level."""
+    import numpy as np
+
+    D, nl = w["D"], sim.num_levels()
+    out = []
+    for l in range(nl):
+        n = [w["n"][d] << l for d in range(D)]
+        mask = np.zeros(n[::-1], bool)
+        for bx in sim.boxes(l):
+            mask[tuple(slice(bx[d], bx[3 + d] + 1) for d in range(D))[::-1]] = True
+        idx = np.argwhere(mask)
+        leaf = np.ones(len(idx), bool)
+        if l + 1 < nl:
+            fm = np.zeros(n[::-1], bool)
+            for bx in sim.boxes(l + 1):
+                fm[tuple(slice(bx[d] // 2, bx[3 + d] // 2 + 1) for d in range(D))[::-1]] = True
+            leaf = ~fm[tuple(idx.T)]
+        out.append(leaf)
+    return out
+
+
+def same_layout(a, b):
+    import numpy as np
+
+    return a.num_levels() == b.num_levels() and all(
+        np.array_equal(a.boxes(l), b.boxes(l)) for l in range(a.num_levels()))
+
+
+def l2_density_leaf(sa, sb, w):
+    """Exact modal L2 norm of the density difference of two runs with the same
+    layout over the leaf cells of every level (the fine data where a level is
+    refined, as the reference's LpNorm_DG_AMR counts it)."""
+    import numpy as np
+
+    M = np.array(mass_diag(w))
+    vol_dom = 1.0
+    for k in range(w["D"]):
+        vol_dom *= w["hi"][k] - w["lo"][k]
+    total = 0.0
+    for l, leaf in enumerate(leaf_masks(sa, w)):
+        d = sa.get_U_w(l)[leaf, 0, :] - sb.get_U_w(l)[leaf, 0, :]
+        cell = vol_dom / np.prod([w["n"][k] << l for k in range(w["D"])])
+        total += cell / 2 ** w["D"] * float(np.sum(M[None, :] * d * d))
+    return (total / vol_dom) ** 0.5
+
+
+def e2e_device_patches(G, s, w, steps):
+    """The same metric through the zero-copy boundary: the state of every box
+    of every level in its own per-variable device arrays laid out as AMReX
+    FArrayBoxes (one ghost cell, modes as components); every step gathers the
+    valid cells into the library (adg_read_patches), runs the step and
+    scatters them back (adg_write_patches).  No host copies."""
+    import torch
+
+    D, Q = w["D"], w["D"] + 2
+    Nps = s.Np_s
+    keep = []
+
+    def register():
+        keep.clear()
+        patches = []
+        for l in range(s.num_levels()):
+            for b in s.boxes(l):
+                ext = [int(b[3 + d] - b[d] + 1 + 2) if d < D else 1 for d in range(3)]
+                p = G.AdgPatch()
+                p.level, p.nghost = l, 1
+                for d in range(3):
+                    p.lo[d], p.hi[d] = int(b[d]), int(b[3 + d])
+                for q in range(Q):
+                    a = torch.full((Nps, ext[2], ext[1], ext[0]), float("nan"), dtype=torch.float64, device="cuda")
+                    keep.append(a)
+                    p.U_w[q] = a.data_ptr()
+                p.jstride, p.kstride, p.nstride = ext[0], ext[0] * ext[1], ext[0] * ext[1] * ext[2]
+                patches.append(p)
+        s.set_patches(patches)
+        s.write_patches()
+        return len(patches)
+
+    torch.cuda.synchronize()
+    npatch = register()
+    L, ctx = s._L, s.ctx
+    d0, _ = s.dof_updates()
+    s.synchronize()
+    t0 = time.perf_counter()
+    reregistered = 0
+    for _ in range(steps):
+        if L.adg_read_patches(ctx) != 0:  # a regrid changed the layout: the caller re-binds its arrays
+            npatch = register()
+            reregistered += 1
+            s.read_patches()
+        if L.adg_advance(ctx, 1, 1) != 0:
+            raise G.AdgError("adg_advance failed")
+        if L.adg_write_patches(ctx) != 0:
+            npatch = register()
+            reregistered += 1
+        s.synchronize()
+    el = time.perf_counter() - t0
+    d1, _ = s.dof_updates()
+    return {"value": (d1 - d0) / el, "unit": "DOF-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+            "patches": npatch, "rebinds_after_regrid": reregistered, "steps": steps,
+            "path": "adg_read_patches + adg_advance(1 step, graph) + adg_write_patches per step on per-(box, q) "
+                    "device arrays with one ghost cell (AMReX FArrayBox layout)"}
+
+
+def roofline_line(G, w, workload, head_name, km_head, km_plain, el_per_step):
+    """roofline of the headline path's dominant kernel: FP64-pipe issue (the
+    ncu-counted FP64-pipe instruction slots of one launch, 2 flops each as the
+    DFMA peak counts them) over the live CUDA-event duration, against the DFMA
+    issue rate measured in this run."""
+    from math import comb
+
+    D, P = w["D"], w["P"]
+    Q, Nps = D + 2, comb(P + D, D)
+    peak = G.fp64_peak_gflops() / 1e3
+    alg, issued = G.flops_per_element(D, P)
+    qbd = (P + 1) ** D
+    alg_pred = alg - 2 * Q * 2 * D * Nps * qbd
+    seeded = head_name.startswith("seed") and km_head.get("seed_inference", 0.0) > 0.0
+    key = "seeded_predictor" if seeded else "plain_predictor"
+    t = km_head["seeded_predictor"] if seeded else km_plain["predictor"]
+    prof = PROFILED_LAUNCH.get(workload, {}).get(key)
+    line = {"bound": "fp64", "unit": "TFLOP/s", "peak": peak,
+            "peak_source": "FP64 DFMA-chain probe on this GPU in this run (adg_fp64_peak_probe; "
+                           "MEASURED_PEAKS.json has no FP64 figure)",
+            "kernel_ms": t}
+    if prof:
+        achieved = 2.0 * prof["fp64_pipe_slots"] / (t * 1e-3) / 1e12
+        line.update({
+            "kernel": prof["kernel"], "achieved": achieved, "frac": achieved / peak,
+            "traffic": prof["dram_bytes"], "traffic_source": prof["source"],
+            "fp64_pipe_slots_per_launch": prof["fp64_pipe_slots"],
+            "fp64_arith_frac": 2.0 * prof["fp64_arith"] / (t * 1e-3) / 1e12 / peak,
+            "fp64_pipe_active_ncu": prof["fp64_active"],
+            "elements_per_launch": prof["elements"],
+            "effective_dense_tflops": alg_pred * prof["elements"] / (t * 1e-3) / 1e12,
+            "note": ("achieved = the kernel's FP64-pipe instruction slots per launch (ncu) x 2 / its event-timed "
+                     "duration: the FP64 issue rate, cross-checked by fp64_pipe_active_ncu; "
+                     "effective_dense_tflops counts the method's dense matrix-form flops per element (" +
+                     f"{alg_pred:.0f}) instead, which the generated sum-factorised operators do not issue"),
+        })
+    else:
+        line.update({"kernel": key, "achieved": None, "frac": None, "traffic": None,
+                     "effective_dense_tflops": alg_pred * el_per_step / (t * 1e-3) / 1e12,
+                     "note": "no FP64 instruction count profiled for this workload"})
+    return line
+
+
+def seed_roofline(w, km_head, el_per_step, peak):
+    """The TF32 tensor-core seed network and the seeded predictor's FP64 part."""
+    from math import comb
+
+    D, P = w["D"], w["P"]
+    Q, Nps = D + 2, comb(P + D, D)
+    Nst = comb(P + D + 1, D + 1)
+    n_in, n_out, hid = Q * Nps + 1, Q * Nst, 128
+    tf32 = 2 * (n_in * hid + 2 * hid * hid + hid * n_out)
+    t_inf = km_head["seed_inference"]
+    tf32_peak = measured_peaks().get("bf16_tflops", 1900.0) / 2.0
+    a32 = tf32 * el_per_step / (t_inf * 1e-3) / 1e12
+    return {"tf32_tensor": {"kernel": "k_seed_infer_tc (4 layers, tcgen05 kind::tf32)",
+                            "algorithmic_flops_per_element": tf32, "ms": t_inf, "achieved": a32,
+                            "peak": tf32_peak, "unit": "TFLOP/s", "frac": a32 / tf32_peak,
+                            "peak_source": "half the measured dense bf16 burst (MEASURED_PEAKS.json)"},
+            "fallback_ms": km_head.get("fallback")}
+
+
+OTHER_CONFIGS = ("vortex_p1_32", "kh_p3_256", "blast3d_p2_amr2")
+
+
+def run_other_configs(G, args):
+    """The other benchmark configurations at their stated sizes, plain FP64
+    (and the 3D blast with its learned seed), timed the same way."""
+    out = {}
+    for name in OTHER_CONFIGS:
+        w = WORKLOADS[name]
+        steps = min(args.steps, 20)
+        r = timed_run(G, w, 0, steps, 3)
+        entry = {"plain_fp64": {"value": r["dof_per_s"], "ms_per_step": r["ms"] / steps, "steps": steps,
+                                "leaf_value": r["leaf_dof_per_s"], "clocks": r["clocks"]}}
+        r["sim"].close()
+        if "amr" in w and not args.no_seed:
+            seed, info = train_seed(G, w, n_pairs=1_000_000, epochs=30)
+            rs = timed_run(G, w, 0, steps, 3, seed=seed, mode=2, sweeps=2, tol=1e-3)
+            entry["seed_2sweeps_fp32"] = {"value": rs["dof_per_s"], "ms_per_step": rs["ms"] / steps,
+                                          "fallback_rate": rs.get("fallback_rate"), "seed_training": info,
+                                          "clocks": rs["clocks"]}
+            rs["sim"].close()
+            seed.close()
+        out[name] = entry
     return out
 
 
@@ -491,6 +706,7 @@ def run_ours(args, w):
     # plain FP64 path (P sweeps)
     plain = timed_run(G, w, E, args.steps, args.warmup)
     variants["plain_fp64"] = plain
+    accuracy = None
     if seed is not None:
         ref = make_sim(G, w, E, sweeps=8)  # converged Picard, accuracy reference
         ref.advance(args.warmup + args.steps, use_graph=True)
@@ -498,11 +714,41 @@ def run_ours(args, w):
         for name, kw in SEED_VARIANTS.items():
             variants[name] = timed_run(G, w, E, args.steps, args.warmup, seed=seed, tol=1e-3, **kw)
         variants["noseed_1sweep_fp64"] = timed_run(G, w, E, args.steps, args.warmup, plain_sweeps=1)
+        orc = None
+        if not args.no_oracle_accuracy:
+            import oracle_ffi as O
+
+            O.set_threads(os.cpu_count())
+            orc = oracle_sim(w)
+            orc.init()
+            for _ in range(args.warmup + args.steps):
+                orc.step()
         for v in variants.values():
-            v["l2_density_vs_converged"] = l2_density_level0(v["sim"].get_U_w(0), U_ref, w)
+            sv = v["sim"]
+            v["l2_density_vs_converged"] = l2_density_level0(sv.get_U_w(0), U_ref, w)
+            v["l2_density_leaf_vs_converged"] = l2_density_leaf(sv, ref, w) if same_layout(sv, ref) else None
+            if orc is not None and same_layout(sv, orc):
+                v["l2_density_leaf_vs_oracle"] = orc.norm_diff([sv.get_U_w(l) for l in range(sv.num_levels())], 2, 0)
         plain_err = variants["plain_fp64"]["l2_density_vs_converged"]
         ok = {k: v for k, v in variants.items() if k.startswith("seed") and v["l2_density_vs_converged"] <= 1.01 * plain_err}
         head_name = max(ok, key=lambda k: ok[k]["dof_per_s"]) if ok else "plain_fp64"
+        plain_leaf = variants["plain_fp64"].get("l2_density_leaf_vs_converged")
+        accuracy = {
+            "criterion": "L2 density against a converged-Picard (8 FP64 sweeps) run of the same workload after the "
+                         "same steps within 1.01x of the plain FP64 path's; level-0 field (exact modal norm) decides",
+            "plain": plain_err, "headline": variants[head_name].get("l2_density_vs_converged"),
+            "leaf_cells": {"plain": plain_leaf, "headline": variants[head_name].get("l2_density_leaf_vs_converged"),
+                           "headline_passes": (None if plain_leaf is None or
+                                               variants[head_name].get("l2_density_leaf_vs_converged") is None else
+                                               variants[head_name]["l2_density_leaf_vs_converged"] <= 1.01 * plain_leaf)},
+            "vs_fp64_oracle": {k: v.get("l2_density_leaf_vs_oracle") for k, v in variants.items()},
+            "vs_fp64_oracle_note": ("the oracle runs the reference's algorithm (P = 3 FP64 sweeps): the plain path "
+                                    "differs from it by rounding only, so against the oracle every seeded variant's "
+                                    "figure is its deviation from the reference's predictor, not an error that the "
+                                    "1.01x criterion can compare"),
+            "config4_as_stated": {"variant": "seed_1sweep_fp64", "l2": variants["seed_1sweep_fp64"]["l2_density_vs_converged"],
+                                  "passes": variants["seed_1sweep_fp64"]["l2_density_vs_converged"] <= 1.01 * plain_err},
+        }
     else:
         head_name = "plain_fp64"
     head = variants[head_name]
@@ -555,52 +801,17 @@ def run_ours(args, w):
     e2e_val = (d_after - d_before) * world / e2e_s
     for h in hosts:
         h.free()
+    try:
+        e2e_dev = e2e_device_patches(G, s, w, e2e_steps)
+    except Exception as ex:  # torch absent or no device memory: report, do not fail the line
+        e2e_dev = {"unavailable": f"{type(ex).__name__}: {ex}"}
 
-    # roofline: the FP64 predictor kernel of the plain path on this workload
     km_plain = plain["sim"].time_kernels(3)
     km_head = head["sim"].time_kernels(3)
-    alg, issued = G.flops_per_element(w["D"], w["P"])
-    qbd = (w["P"] + 1) ** w["D"]
-    alg_pred = alg - 2 * Q * 2 * w["D"] * Nps * qbd
-    # elements the predictor processed per step in the plain run (valid + ghost)
     el_per_step = plain["dof"] / args.steps / (Q * Nps)
-    peak = G.fp64_peak_gflops() / 1e3
-    achieved = alg_pred * el_per_step / (km_plain["predictor"] * 1e-3) / 1e12
-    traffic, traffic_src = PROFILED_TRAFFIC.get(args.workload, (None, None))
-    seed_roof = None
+    roof = roofline_line(G, w, args.workload, head_name, km_head, km_plain, el_per_step)
     if head_name.startswith("seed") and km_head.get("seed_inference", 0.0) > 0.0:
-        # seeded path: the seeded predictor's final stage (corrector volume
-        # term + face traces, counted as the method's dense flops; computed
-        # as an FP64 time-independent part and FP32 changes), TF32 network on
-        # the tensor cores, time-weighted blend
-        D, P = w["D"], w["P"]
-        Nst, qst = comb(P + D + 1, D + 1), (P + 1) ** (D + 1)
-        n_in, n_out, hid = Q * Nps + 1, Q * Nst, 128
-        f64 = 2 * Q * qst * Nst + 2 * D * 2 * Q * qbd * Nst + 2 * Q * D * Nps * qst + 2 * Q * Nps
-        tf32 = 2 * (n_in * hid + 2 * hid * hid + hid * n_out)
-        t_inf = km_head["seed_inference"]
-        t_pred = km_head["predictor"] - t_inf
-        tf32_peak = measured_peaks().get("bf16_tflops", 1900.0) / 2.0
-        a64 = f64 * el_per_step / (t_pred * 1e-3) / 1e12
-        a32 = tf32 * el_per_step / (t_inf * 1e-3) / 1e12
-        seed_roof = {
-            "fp64": {"kernel": "k_predictor (seeded: FP32 sweeps, final stage split into an FP64 "
-                               "time-independent part and FP32 changes)",
-                     "algorithmic_flops_per_element": f64, "ms": t_pred, "achieved": a64, "peak": peak,
-                     "unit": "TFLOP/s", "frac": a64 / peak,
-                     "note": ("algorithmic = the dense flops of the final stage (volume term and face traces at "
-                              "every space-time point); the kernel computes the time-dependent part in FP32 and "
-                              "issues about 2.2 k FP64 instructions per element, so frac exceeds 1; the FP64 "
-                              "pipe activity (ncu) is in fp64_pipe_active_ncu")},
-            "tf32_tensor": {"kernel": "k_seed_infer_tc (4 layers, tcgen05 kind::tf32)",
-                            "algorithmic_flops_per_element": tf32, "ms": t_inf, "achieved": a32,
-                            "peak": tf32_peak, "unit": "TFLOP/s", "frac": a32 / tf32_peak,
-                            "peak_source": "half the measured dense bf16 burst (MEASURED_PEAKS.json)"},
-            "blended_frac": (a64 / peak * t_pred + a32 / tf32_peak * t_inf) / (t_pred + t_inf),
-        }
-    with ClockSampler(local) as clk:
-        clk_ms = head["sim"].advance_timed(min(args.steps, 50), use_graph=True)
-    clocks = clk.summary()
+        roof["seed_path"] = seed_roofline(w, km_head, el_per_step, roof["peak"])
     line = {
         "metric": METRIC, "value": value, "unit": "DOF-updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -609,42 +820,39 @@ def run_ours(args, w):
                          "FP64 state, corrector, numerical-flux moments and the time-independent part of the "
                          "predictor; FP32 Picard sweeps and flux changes; TF32 tensor-core seed network"),
         "data": "synthetic",
-        "config": {**base_config(args, w, world), "path": head_name, "elems_per_block": E, "cuda_graph": True,
-                   "l2": f"flushed before every timed step ({L2_FLUSH_BYTES >> 20} MiB device memset, outside "
-                         "the per-step CUDA-event intervals that are summed)"},
+        "config": base_config(args, w, world),
+        "run": {"path": head_name, "elems_per_block": E, "cuda_graph": True,
+                "parallelism": "replicas" if world > 1 else "1 GPU",
+                "l2": f"flushed before every timed step ({L2_FLUSH_BYTES >> 20} MiB device memset, outside "
+                      "the per-step CUDA-event intervals that are summed)"},
         "leaf_value": head["leaf_dof_per_s"] * world,
         "e2e": {"value": e2e_val, "unit": "DOF-updates/s", "h2d_bytes_per_step": h2d // e2e_steps,
                 "d2h_bytes_per_step": d2h // e2e_steps},
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
-                     "seed_path": seed_roof,
-                     "kernel": "k_predictor (plain FP64 path of this workload)", "kernel_ms": km_plain["predictor"],
-                     "algorithmic_flops_per_element": alg_pred, "elements_per_launch": el_per_step,
-                     "elements_note": ("valid elements of all levels (on AMR layouts the launch runs the uncovered "
-                                       "ones, the covered ones that border them and the coarse-fine ghosts)"),
-                     "issued_linear_fp64_per_element": issued,
-                     "fp64_pipe_active_ncu": PROFILED_FP64_ACTIVE.get(args.workload),
-                     "note": ("frac counts the reference's dense matrix-form flops per element (the per-unit "
-                              "figure of the method); the generated sum-factorised operators issue "
-                              f"{issued:.0f} linear FP64 operations per element for the same result, so frac "
-                              "exceeds 1 while the FP64 pipe runs at the ncu-measured activity"),
-                     "peak_source": "DFMA-chain probe on this GPU in this run (MEASURED_PEAKS.json has no FP64 figure)"},
+        "e2e_device_patches": e2e_dev,
+        "roofline": roof,
         "kernel_ms": {"plain": km_plain, "headline": km_head},
         "variants": {k: {kk: vv for kk, vv in v.items() if kk != "sim"} for k, v in variants.items()},
         "gpu_launches": head["launches"],
-        "clocks": clocks,
+        "clocks": head["clocks"],
         "status": head["sim"].status(),
     }
     if seed_info:
-        line["seed_training"] = seed_info
-        line["equal_l2"] = {"criterion": "L2 density (level-0 field, exact modal norm) against a converged-Picard "
-                                         "FP64 run within 1.01x of the plain FP64 path's",
-                            "plain": variants["plain_fp64"]["l2_density_vs_converged"],
-                            "headline": head.get("l2_density_vs_converged")}
+        line["seed_training"] = dict(seed_info)
+        cost = seed_info.get("collect_s", 0.0) + seed_info.get("train_s", 0.0)
+        gain_ms = (variants["plain_fp64"]["ms"] - head["ms"]) / args.steps
+        line["seed_training"]["collect_plus_train_s"] = cost
+        line["seed_training"]["break_even_steps"] = (cost * 1e3 / gain_ms) if gain_ms > 0 else None
+        line["seed_training"]["note"] = ("collection (Picard predictor on perturbed runs) and training are outside "
+                                         "the timed steps; break_even_steps = their time / the per-step saving of "
+                                         "the headline path over the plain FP64 path")
+    if accuracy:
+        line["equal_l2"] = accuracy
+    if not args.no_other_configs and rank == 0:
+        line["other_configs"] = run_other_configs(G, args)
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(w, max_seconds=args.cpu_seconds)
-        print(json.dumps(line))
+        print(json.dumps(line, default=_jsonable))
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
@@ -661,6 +869,10 @@ def main():
     ap.add_argument("--no-seed", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-oracle-accuracy", action="store_true",
+                    help="skip the equal-L2 comparison of every variant with the FP64 oracle")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip the timing of the other benchmark configurations")
     ap.add_argument("--only", default=None,
                     choices=["plain_fp64", "noseed_1sweep_fp64"] + list(SEED_VARIANTS),
                     help="time one variant only and print its record (profiling runs)")

@@ -321,7 +321,8 @@ int adg_advance_timed_flushed(adg_ctx* ctx, int nsteps, int use_graph, int64_t f
  * 0 predictor (+ corrector volume term and face traces; with a seed
  * attached: the seed inference, the seeded predictor and the fallback),
  * 1 numerical flux, 2 corrector update, 3 time-step reduction, 4 AMR
- * synchronisation, 5 the seed inference alone (0 without a seed). */
+ * synchronisation, 5 the seed inference alone, 6 the seeded predictor alone,
+ * 7 the fallback pass (5-7: 0 without a seed). */
 int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds);
 
 /* Page-locked host buffers for host<->device state copies. */
