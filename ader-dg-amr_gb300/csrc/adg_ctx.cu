@@ -1103,9 +1103,10 @@ int adg_ctx_create(const adg_config* cfg, adg_ctx** out) {
   ctx->sweeps = cfg->picard_sweeps > 0 ? cfg->picard_sweeps : cfg->P;
   if (ctx->sweeps < 1) ctx->sweeps = 1;
   std::vector<int> ch = ks->elems_per_block_choices();
+  const int E0 = cfg->D == 2 ? 16 : 8;  // default where it is built, else the one choice of the configuration
   ctx->E = (cfg->elems_per_block > 0 && std::find(ch.begin(), ch.end(), cfg->elems_per_block) != ch.end())
                ? cfg->elems_per_block
-               : (cfg->D == 2 ? 16 : 8);
+               : (std::find(ch.begin(), ch.end(), E0) != ch.end() ? E0 : ch.front());
   cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete ctx;
@@ -2247,7 +2248,7 @@ cudaError_t grow_rows(DevBuf<float>& b, size_t keep, size_t need) {
 // as a K-major B operand, at 4 KB aligned offsets.
 int seed_pack_tc(adg_seed* s) {
   s->packed = false;
-  if (s->h != kSeedTcHidden) return ADG_OK;
+  if (s->h != kSeedTcHidden || !seed_tc_fits(s->Q, (s->n_in - 1) / s->Q, s->n_out / s->Q)) return ADG_OK;
   const int K1 = seed_tc_k1(s->n_in), N4 = seed_tc_n4(s->n_out), H = s->h;
   const int Kp[4] = {K1, H, H, H}, Np[4] = {H, H, H, N4};
   const int fin[4] = {s->n_in, H, H, H}, fout[4] = {H, H, H, s->n_out};
@@ -2653,6 +2654,8 @@ int adg_seed_attach(adg_ctx* ctx, adg_seed* s, int mode, int sweeps, double tol)
   } else {
     if (s->D != ctx->cfg.D || s->P != ctx->cfg.P || mode < 1 || mode > 2 || sweeps < 0 || !(tol > 0))
       return fail(ctx, ADG_ERR_ARG, "bad seed attach arguments");
+    if (!ctx->ks->seed_modes())
+      return fail(ctx, ADG_ERR_ARG, "the learned seed is built for D = 2 with P <= 3 and D = 3 with P <= 2");
     ctx->seed = s;
     ctx->seed_mode = mode;
     ctx->seed_sweeps = sweeps;

@@ -81,12 +81,29 @@ cudaError_t launch_predictor_mode(const PredictorArgs& a, cudaStream_t s) {
   }
 }
 
+// The learned-seed path (predictor modes 1-3, the fused TF32 inference) is
+// built for the elements whose network layers fit the fused kernel
+// (seed_tc_fits: D = 2 with P <= 3, D = 3 with P <= 2).  Higher degrees run
+// the plain FP64 path only, with one elements-per-block choice, which keeps
+// their (large, generated) translation units quick to compile.
+constexpr bool kSeedModes = seed_tc_fits(O::Q, O::NP_S, O::NP_ST);
+
 template <int E>
 cudaError_t launch_predictor(const PredictorArgs& a, cudaStream_t s, int mode) {
-  if (mode == 1) return launch_predictor_mode<E, 1>(a, s);
-  if (mode == 2) return launch_predictor_mode<E, 2>(a, s);
-  if (mode == 3) return launch_predictor_mode<E, 3>(a, s);
+  if constexpr (kSeedModes) {
+    if (mode == 1) return launch_predictor_mode<E, 1>(a, s);
+    if (mode == 2) return launch_predictor_mode<E, 2>(a, s);
+    if (mode == 3) return launch_predictor_mode<E, 3>(a, s);
+  } else {
+    if (mode != 0) return cudaErrorNotSupported;
+  }
   return launch_predictor_mode<E, 0>(a, s);
+}
+
+// Elements per block of the plain-only configurations: the largest of 16, 8,
+// 4 whose FP64 sweep buffers fit the 227 KB of shared memory of a block.
+constexpr int lite_elems() {
+  return smem_bytes<16, 0>() <= 227 * 1024 ? 16 : smem_bytes<8, 0>() <= 227 * 1024 ? 8 : 4;
 }
 
 struct Impl final : KernelSet {
@@ -103,7 +120,14 @@ struct Impl final : KernelSet {
     TR_TILE = tr_tile<O>();
     linear_fp64_per_column = O::LINEAR_FP64_PER_COLUMN;
   }
-#if ADG_D == 2
+  bool seed_modes() const override { return kSeedModes; }
+#if ADG_LITE
+  std::vector<int> elems_per_block_choices() const override { return {lite_elems()}; }
+  size_t predictor_smem(int) const override { return smem_bytes<lite_elems(), 0>(); }
+  cudaError_t predictor(const PredictorArgs& a, int, cudaStream_t s, int mode) const override {
+    return launch_predictor<lite_elems()>(a, s, mode);
+  }
+#elif ADG_D == 2
   std::vector<int> elems_per_block_choices() const override { return {8, 16, 32}; }
   size_t predictor_smem(int E) const override {
     return E == 8 ? smem_bytes<8, 0>() : E == 16 ? smem_bytes<16, 0>() : smem_bytes<32, 0>();
@@ -198,12 +222,16 @@ struct Impl final : KernelSet {
     return cudaGetLastError();
   }
   cudaError_t seed_infer_tc(const SeedTCArgs& a, cudaStream_t s) const override {
-    if (a.n <= 0) return cudaSuccess;
-    static std::atomic<unsigned long long> attr{0};
-    cudaError_t e = ensure_smem_attr(attr, k_seed_infer_tc<O>, kSeedTcSmem);
-    if (e != cudaSuccess) return e;
-    k_seed_infer_tc<O><<<(a.n + kSeedTcRows - 1) / kSeedTcRows, kSeedTcThreads, kSeedTcSmem, s>>>(a);
-    return cudaGetLastError();
+    if constexpr (!seed_tc_fits(O::Q, O::NP_S, O::NP_ST)) {
+      return cudaErrorNotSupported;  // layers too wide for the fused kernel: the SIMT path serves
+    } else {
+      if (a.n <= 0) return cudaSuccess;
+      static std::atomic<unsigned long long> attr{0};
+      cudaError_t e = ensure_smem_attr(attr, k_seed_infer_tc<O>, kSeedTcSmem);
+      if (e != cudaSuccess) return e;
+      k_seed_infer_tc<O><<<(a.n + kSeedTcRows - 1) / kSeedTcRows, kSeedTcThreads, kSeedTcSmem, s>>>(a);
+      return cudaGetLastError();
+    }
   }
   cudaError_t limit_tvb(const LimiterArgs& a, cudaStream_t s) const override {
     if (a.n <= 0) return cudaSuccess;

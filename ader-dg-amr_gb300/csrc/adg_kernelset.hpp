@@ -18,6 +18,8 @@ struct KernelSet {
   int linear_fp64_per_column;
   virtual ~KernelSet() = default;
   virtual std::vector<int> elems_per_block_choices() const = 0;
+  // the learned-seed predictor modes (1-3) are built for this (D, P)
+  virtual bool seed_modes() const = 0;
   virtual size_t predictor_smem(int E) const = 0;
   // mode 0: FP64 Picard; 1 / 2: seeded, FP64 / FP32 sweeps; 3: FP64 Picard with
   // mode 2's final stage (element lists only: the fallback of a mode-2 step).
@@ -52,13 +54,21 @@ const KernelSet* kernels_D2P2();
 const KernelSet* kernels_D2P3();
 const KernelSet* kernels_D3P1();
 const KernelSet* kernels_D3P2();
+const KernelSet* kernels_D2P4();
+const KernelSet* kernels_D2P5();
+const KernelSet* kernels_D2P6();
+const KernelSet* kernels_D3P3();
 
 inline const KernelSet* kernel_set(int D, int P) {
   if (D == 2 && P == 1) return kernels_D2P1();
   if (D == 2 && P == 2) return kernels_D2P2();
   if (D == 2 && P == 3) return kernels_D2P3();
+  if (D == 2 && P == 4) return kernels_D2P4();
+  if (D == 2 && P == 5) return kernels_D2P5();
+  if (D == 2 && P == 6) return kernels_D2P6();
   if (D == 3 && P == 1) return kernels_D3P1();
   if (D == 3 && P == 2) return kernels_D3P2();
+  if (D == 3 && P == 3) return kernels_D3P3();
   return nullptr;
 }
 

@@ -147,7 +147,14 @@ extern "C" int adg_ader_step_noalloc(int D, int P, const int n_cell[3], const do
   pa.Rvol = (double*)(base + o_rv);
   pa.Tr = (double*)(base + o_tr);
   pa.Hw_out = nullptr;
-  if (ks->predictor(pa, D == 2 ? 16 : 8, s) != cudaSuccess) return ADG_ERR_CUDA;
+  int E = D == 2 ? 16 : 8;
+  {
+    const std::vector<int> ch = ks->elems_per_block_choices();
+    bool built = false;
+    for (int c : ch) built = built || c == E;
+    if (!built) E = ch.front();  // the higher degrees build one choice
+  }
+  if (ks->predictor(pa, E, s) != cudaSuccess) return ADG_ERR_CUDA;
 
   FaceArgs fa{};
   fa.Tr = pa.Tr;

@@ -157,6 +157,14 @@ struct SeedTCArgs {
 
 constexpr uint32_t kStatusSeedWait = 8u;
 
+// The fused kernel's buffers hold layers of at most 128 inputs and outputs
+// and a state row of kSeedTcUfLd values: (D, P) with Q Np_s + 1 <= 128
+// inputs and Q Np_st <= 128 outputs (D = 2, P <= 3; D = 3, P <= 2).  Larger
+// elements infer the seed with the SIMT kernels.
+__host__ __device__ constexpr bool seed_tc_fits(int Q, int np_s, int np_st) {
+  return seed_tc_k1(Q * np_s + 1) <= 128 && seed_tc_n4(Q * np_st) <= 128 && Q * np_s <= kSeedTcUfLd;
+}
+
 template <class O>
 __global__ void __launch_bounds__(kSeedTcThreads, 1) k_seed_infer_tc(SeedTCArgs a) {
   constexpr int Q = O::Q, NP_S = O::NP_S, NP_ST = O::NP_ST;

@@ -326,22 +326,27 @@ def stage_from_map(in_keys, out_keys, fn):
 
 
 def chain_dense(stages):
+    """The dense matrix of a chain of stages (float64 products)."""
+    import numpy as np
+
     M = None
     for st in stages:
-        S = [[0.0] * st.n_in for _ in range(st.n_out)]
+        S = np.zeros((st.n_out, st.n_in))
         for r, terms in enumerate(st.rows):
             for c, v in terms:
-                S[r][c] += v
-        if M is None:
-            M = S
-        else:
-            M = [[sum(S[i][k] * M[k][j] for k in range(len(M))) for j in range(len(M[0]))] for i in range(len(S))]
-    return M
+                S[r, c] += v
+        M = S if M is None else S @ M
+    return M.tolist()
 
 
-def check_chain(stages, dense, name, tol=1e-12):
+def check_chain(stages, dense, name, tol=1e-12, scale=None):
+    """The chain's product equals the dense operator to tol relative to
+    scale (default: the dense operator's largest entry; an operator that is
+    zero up to rounding is checked against the scale of the operator it
+    derives from)."""
     M = chain_dense(stages)
-    scale = max(abs(v) for r in dense for v in r) or 1.0
+    if scale is None:
+        scale = max(abs(v) for r in dense for v in r) or 1.0
     err = max(abs(M[i][j] - dense[i][j]) for i in range(len(dense)) for j in range(len(dense[0])))
     if err > tol * scale:
         raise SystemExit(f"chain check failed for {name}: {err / scale}")
@@ -469,7 +474,10 @@ def build_ops(el):
         stages = [st1] + rest + [perm_i, cst]
         dense = [[sum(el.A[d][r][el.pts_st.index((i,) + pt)] for i in range(N))
                   for pt in itertools.product(range(N), repeat=D)] for r in range(el.Np_st)]
-        check_chain(stages, dense, f"proj_init{d}", tol=1e-11)
+        # proj_init[0] is zero up to rounding (the x_0 projection of an
+        # x_0-independent flux): checked on the scale of A_d
+        check_chain(stages, dense, f"proj_init{d}", tol=1e-11,
+                    scale=max(abs(v) for r in el.A[d] for v in r))
         ops[f"proj_init{d}"] = (stages, len(grid_keys), el.Np_st)
 
     # ---- W U: (Np_s) -> (Np_st)

@@ -46,7 +46,8 @@ extern "C" {
 #define ADG_IC_CONST 4      /* uniform free stream */
 
 typedef struct adg_config {
-  int D, P;                 /* spatial dimension 2|3, polynomial degree 1..3 */
+  int D, P;                 /* spatial dimension 2|3; polynomial degree 1..6 at D = 2, 1..3 at D = 3
+                               (the learned seed: P <= 3 at D = 2, P <= 2 at D = 3) */
   double gamma;             /* adiabatic index (Compressible_Euler.cpp:42-47) */
   double c_dt;              /* CFL safety factor (Solver::c_dt) */
   int n_cell[3];            /* level-0 cells per dimension */

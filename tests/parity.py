@@ -17,7 +17,13 @@ CASES = {
     "vortex_p3_outflow": (2, 3, (16, 12, 1), (0, 0, 0), (10, 7.5, 1), (0, 0, 1), "vortex", dict(u_inf=0.3, v_inf=0.2)),
     "blast3d_p2": (3, 2, (8, 8, 8), (0, 0, 0), (1, 1, 1), (0, 0, 0), "blast3d", dict()),
     "blast3d_p1_per": (3, 1, (8, 6, 4), (0, 0, 0), (1, 0.75, 0.5), (1, 1, 1), "blast3d", dict()),
+    # higher degrees (plain FP64 path)
+    "vortex_p4": (2, 4, (16, 12, 1), (0, 0, 0), (10, 7.5, 1), (1, 1, 1), "vortex", dict(u_inf=1.0, v_inf=0.5)),
+    "kh_p5_outflow": (2, 5, (12, 12, 1), (0, 0, 0), (1, 1, 1), (0, 1, 1), "kh_noise", dict(seed=5, noise_amp=1e-3)),
+    "vortex_p6": (2, 6, (8, 8, 1), (0, 0, 0), (10, 10, 1), (1, 1, 1), "vortex", dict(u_inf=1.0, v_inf=0.0)),
+    "blast3d_p3": (3, 3, (6, 6, 6), (0, 0, 0), (1, 1, 1), (0, 0, 0), "blast3d", dict()),
 }
+HIGH_DEGREE = ("vortex_p4", "kh_p5_outflow", "vortex_p6", "blast3d_p3")
 
 ORACLE_IC = {"vortex": "vortex", "kh_noise": "kh_noise", "blast3d": "blast3d", "const": "const"}
 GPU_IC = {"vortex": "isentropic_vortex", "kh_noise": "kh_noise", "blast3d": "blast3d", "const": "const"}
@@ -55,6 +61,8 @@ def rel_err(a, b):
 
 
 AMR_CASES = {
+    "kh_p4_amr": (2, 4, (16, 16, 1), (1, 1, 1), (1, 1, 1), "kh_noise", dict(seed=11, noise_amp=1e-3),
+                  dict(max_level=1, max_grid=8, blocking_factor=4, dtn_regrid=2, tag_kind=0, tag_threshold=0.05)),
     # name: (D, P, n_cell, hi, periodic, ic, extra, amr)
     "kh_p3_amr": (2, 3, (16, 16, 1), (1, 1, 1), (1, 1, 1), "kh_noise", dict(seed=12345, noise_amp=1e-3),
                   dict(max_level=2, max_grid=16, blocking_factor=8, dtn_regrid=4, tag_kind=0, tag_threshold=0.1)),

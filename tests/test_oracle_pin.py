@@ -34,3 +34,14 @@ def test_vortex_l2_matches_reference_outputs(P, N):
     got = s.norm(2, 0)
     # the reference sums cell norms in a thread-dependent order
     assert abs(got - ref) / ref < 1e-11, (got, ref)
+
+
+def test_p6_vortex_error_near_thesis_table():
+    """p = 6 (the highest degree the thesis reports, Table 5.2 p. 40: L1
+    5.4456e-5, L2 8.3997e-5 at N = 8).  The thesis runs used a slightly
+    different set-up than the reference's recorded ones (its p = 3, N = 8 L2,
+    2.7705e-3, is 0.6 % from the recorded 2.7878e-3), so the oracle is
+    checked to the same closeness, not to rounding."""
+    s = run_vortex(6, 8)
+    assert abs(s.norm(1, 0) - 5.4456e-5) / 5.4456e-5 < 0.01
+    assert abs(s.norm(2, 0) - 8.3997e-5) / 8.3997e-5 < 0.01
