@@ -145,6 +145,8 @@ def lib():
         "adg_average_down": ([vp], i),
         "adg_fill_ghosts": ([vp], i),
         "adg_limit": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
+        "adg_autotune": ([vp, i, ctypes.POINTER(i), dp, i], i),
+        "adg_block_choices": ([vp, ctypes.POINTER(i), i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)], i),
         "adg_set_patches": ([vp, ctypes.POINTER(AdgPatch), i], i),
         "adg_read_patches": ([vp], i),
         "adg_write_patches": ([vp], i),
@@ -505,6 +507,24 @@ class AmrDG:
     def write_patches(self):
         """Queue the copy of the state into the registered patches' valid cells."""
         self._check(self._L.adg_write_patches(self.ctx), "adg_write_patches")
+
+    def autotune(self, nsteps=3):
+        """Time every elements-per-block choice of the predictor on the current
+        layout (state restored), keep and record the fastest; returns
+        {"E": choice, "ms": {E: per-step predictor ms}}."""
+        ch = self.block_choices()["choices"]
+        E = ctypes.c_int()
+        ms = (ctypes.c_double * len(ch))()
+        self._check(self._L.adg_autotune(self.ctx, int(nsteps), ctypes.byref(E), ms, len(ch)), "adg_autotune")
+        return {"E": E.value, "ms": {c: ms[i] for i, c in enumerate(ch)}}
+
+    def block_choices(self):
+        """Built elements-per-block choices and the ones in use."""
+        ch = (ctypes.c_int * 16)()
+        n, ep, es = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self._L.adg_block_choices(self.ctx, ch, 16, ctypes.byref(n), ctypes.byref(ep), ctypes.byref(es)),
+                    "adg_block_choices")
+        return {"choices": list(ch[:n.value]), "plain": ep.value, "seeded": es.value}
 
     def Limiter_w(self):
         """The TVB limiter of the finest level on the current state

@@ -20,6 +20,10 @@
 #include "adg_patches.cuh"
 #include "plotfile.hpp"
 #include <random>
+#include <cstdlib>
+#include <filesystem>
+#include <fstream>
+#include <sstream>
 
 namespace adg {
 
@@ -189,6 +193,7 @@ struct adg_ctx {
   int n_rollbacks = 0;
   // learned seed
   adg_seed* seed = nullptr;
+  int Es = 0;  // elements per block of the seeded predictor (0: 8 for the FP32 sweeps at D = 2, else E)
   int seed_mode = 0, seed_sweeps = 1;
   double seed_tol = 1e-3;
   DevBuf<float> sx, sy0, sy1, syo;     // features, ping-pong activations, outputs
@@ -1163,6 +1168,8 @@ int adg_set_stream(adg_ctx* ctx, void* stream) {
   return ADG_OK;
 }
 
+static void apply_tuned_choices(adg_ctx* ctx);
+
 int adg_init(adg_ctx* ctx) {
   if (!ctx) return ADG_ERR_ARG;
   const adg_config& c = ctx->cfg;
@@ -1297,6 +1304,7 @@ int adg_init(adg_ctx* ctx) {
   rc = launch_dt(ctx, 0);
   if (rc) return rc;
   ADG_CUDA(cudaStreamSynchronize(ctx->stream), "init sync");
+  apply_tuned_choices(ctx);
   return ADG_OK;
 }
 
@@ -2023,6 +2031,153 @@ int adg_advance_timed_flushed(adg_ctx* ctx, int nsteps, int use_graph, int64_t f
   return ADG_OK;
 }
 
+// ---- autotuner: elements per block of the predictor stages ---------------
+// Per GPU model, (D, P), level-0 grid, finest level and stage, the fastest
+// elements-per-block choice measured by adg_autotune, kept in a text file
+// (ADG_TUNE_CACHE, else $HOME/.cache/adg_gb300/tune.txt), one "key E" line each.
+namespace {
+
+std::string tune_cache_path() {
+  const char* p = std::getenv("ADG_TUNE_CACHE");
+  if (p && *p) return p;
+  const char* h = std::getenv("HOME");
+  return std::string(h && *h ? h : "/tmp") + "/.cache/adg_gb300/tune.txt";
+}
+
+std::string tune_key(const adg_ctx* ctx, const char* stage) {
+  int dev = 0;
+  cudaDeviceProp prop{};
+  std::string gpu = "gpu";
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess) {
+    gpu = prop.name;
+    for (char& ch : gpu)
+      if (ch == ' ' || ch == '\t') ch = '_';
+    gpu += "/" + std::to_string(prop.multiProcessorCount) + "sm";
+  }
+  const adg_config& c = ctx->cfg;
+  std::ostringstream k;
+  k << gpu << "/D" << c.D << "P" << c.P << "/n" << c.n_cell[0] << "x" << (c.D > 1 ? c.n_cell[1] : 1) << "x"
+    << (c.D > 2 ? c.n_cell[2] : 1) << "/L" << c.max_level << "/" << stage;
+  return k.str();
+}
+
+bool tune_lookup(const std::string& key, int* E) {
+  std::ifstream f(tune_cache_path());
+  std::string k;
+  int e = 0;
+  bool found = false;
+  while (f >> k >> e)
+    if (k == key) {
+      *E = e;
+      found = true;
+    }
+  return found;
+}
+
+void tune_store(const std::string& key, int E) {
+  const std::string path = tune_cache_path();
+  std::vector<std::pair<std::string, int>> rows;
+  {
+    std::ifstream f(path);
+    std::string k;
+    int e = 0;
+    while (f >> k >> e)
+      if (k != key) rows.emplace_back(k, e);
+  }
+  rows.emplace_back(key, E);
+  std::error_code ec;
+  std::filesystem::create_directories(std::filesystem::path(path).parent_path(), ec);
+  std::ofstream f(path, std::ios::trunc);
+  for (const auto& r : rows) f << r.first << " " << r.second << "\n";
+}
+
+bool choice_built(const KernelSet* ks, int E) {
+  const std::vector<int> ch = ks->elems_per_block_choices();
+  return std::find(ch.begin(), ch.end(), E) != ch.end();
+}
+
+}  // namespace
+
+// Cached choices for a context created with elems_per_block = 0.
+static void apply_tuned_choices(adg_ctx* ctx) {
+  if (ctx->cfg.elems_per_block > 0) return;
+  int E = 0;
+  if (tune_lookup(tune_key(ctx, "plain"), &E) && choice_built(ctx->ks, E)) ctx->E = E;
+  if (ctx->seed_mode && tune_lookup(tune_key(ctx, ctx->seed_mode == 2 ? "seeded_fp32" : "seeded_fp64"), &E) &&
+      choice_built(ctx->ks, E))
+    ctx->Es = E;
+}
+
+int adg_autotune(adg_ctx* ctx, int nsteps, int* E_out, double* ms, int cap) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (nsteps < 1) return fail(ctx, ADG_ERR_ARG, "nsteps must be positive");
+  rc = flush_ghosts(ctx);
+  if (rc) return rc;
+  const std::vector<int> ch = ctx->ks->elems_per_block_choices();
+  const bool seeded = ctx->seed_mode && ctx->seed;
+  // host counters a step moves; the device state is snapshotted
+  const long long nstep = ctx->nstep, dof = ctx->dof_updates, leaf = ctx->leaf_dof_updates,
+                  pred = ctx->seed_predicted, launches = ctx->launches;
+  const int E0 = ctx->E, Es0 = ctx->Es;
+  rc = snapshot_step_state(ctx);
+  if (rc) return rc;
+  const int NEV = 8;
+  std::vector<cudaEvent_t> ev((size_t)NEV * nsteps);
+  for (auto& x : ev) ADG_CUDA(cudaEventCreate(&x), "event");
+  std::vector<double> t(ch.size(), 0.0);
+  for (size_t i = 0; i < ch.size() && rc == ADG_OK; ++i) {
+    if (seeded)
+      ctx->Es = ch[i];
+    else
+      ctx->E = ch[i];
+    for (int s = 0; s < nsteps && rc == ADG_OK; ++s) rc = launch_step(ctx, &ev[(size_t)s * NEV]);
+    if (rc == ADG_OK) {
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) rc = cuda_fail(ctx, e, "autotune");
+    }
+    for (int s = 0; s < nsteps && rc == ADG_OK; ++s) {
+      float f = 0.f;
+      // the predictor stage (plain) or the seeded predictor alone
+      cudaEventElapsedTime(&f, ev[(size_t)s * NEV + (seeded ? 6 : 0)], ev[(size_t)s * NEV + (seeded ? 7 : 1)]);
+      t[i] += f / nsteps;
+    }
+    if (rc == ADG_OK) rc = restore_step_state(ctx);
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  ctx->nstep = nstep;
+  ctx->dof_updates = dof;
+  ctx->leaf_dof_updates = leaf;
+  ctx->seed_predicted = pred;
+  ctx->launches = launches;
+  ctx->E = E0;
+  ctx->Es = Es0;
+  if (rc) return rc;
+  ADG_CUDA(cudaStreamSynchronize(ctx->stream), "autotune restore");
+  size_t best = 0;
+  for (size_t i = 1; i < ch.size(); ++i)
+    if (t[i] < t[best]) best = i;
+  if (seeded)
+    ctx->Es = ch[best];
+  else
+    ctx->E = ch[best];
+  tune_store(tune_key(ctx, seeded ? (ctx->seed_mode == 2 ? "seeded_fp32" : "seeded_fp64") : "plain"), ch[best]);
+  ctx->graph_stale = true;  // the captured step used the old choice
+  if (E_out) *E_out = ch[best];
+  for (int i = 0; i < cap && ms; ++i) ms[i] = i < (int)ch.size() ? t[i] : 0.0;
+  return ADG_OK;
+}
+
+int adg_block_choices(const adg_ctx* ctx, int* choices, int cap, int* n, int* E_plain, int* E_seeded) {
+  if (!ctx) return ADG_ERR_ARG;
+  const std::vector<int> ch = ctx->ks->elems_per_block_choices();
+  for (int i = 0; i < cap && choices && i < (int)ch.size(); ++i) choices[i] = ch[i];
+  if (n) *n = (int)ch.size();
+  if (E_plain) *E_plain = ctx->E;
+  if (E_seeded) *E_seeded = ctx->Es > 0 ? ctx->Es : (ctx->seed_mode == 2 && ctx->cfg.D == 2 ? 8 : ctx->E);
+  return ADG_OK;
+}
+
 int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds) {
   int rc = check_ready(ctx);
   if (rc) return rc;
@@ -2345,7 +2500,7 @@ int launch_seeded_predictor(adg_ctx* ctx, const PredictorArgs& base, cudaEvent_t
   // the FP32 predictor at D = 2 runs one-warp blocks (8 elements): 16 of them
   // per SM, so the element groups spread evenly over the SMs (at D = 3 the
   // 40-thread blocks of 8 elements idle 3/8 of their lanes: the tuned E stays)
-  const int Es = ctx->seed_mode == 2 && ctx->cfg.D == 2 ? 8 : ctx->E;
+  const int Es = ctx->Es > 0 ? ctx->Es : (ctx->seed_mode == 2 && ctx->cfg.D == 2 ? 8 : ctx->E);
   e = ks->predictor(pa, Es, st, ctx->seed_mode);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "seeded predictor");
   if (ev) cudaEventRecord(ev[7], st);  // end of the seeded predictor, start of the fallback pass
@@ -2664,6 +2819,7 @@ int adg_seed_attach(adg_ctx* ctx, adg_seed* s, int mode, int sweeps, double tol)
     ADG_CUDA(ctx->fb_total.ensure(1), "alloc");
     ADG_CUDA(cudaMemset(ctx->fb_total.p, 0, sizeof(unsigned long long)), "reset");
     ctx->seed_predicted = 0;
+    apply_tuned_choices(ctx);
   }
   ctx->tables_dirty = true;  // resizes the inference buffers, drops the graph
   return ADG_OK;

@@ -30,6 +30,8 @@ import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# the library's autotuner records its choices next to the build
+os.environ.setdefault("ADG_TUNE_CACHE", os.path.join(ROOT, "ader-dg-amr_gb300", "_build", "tune_cache.txt"))
 sys.path.insert(0, os.path.join(ROOT, "ader-dg-amr_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
@@ -171,31 +173,26 @@ def make_sim(G, w, E=0, sweeps=0, seed=None, noise_amp=None):
 
 
 def autotune(G, w, steps=3):
-    """Pick elements-per-block of the predictor by timing each variant on this
-    workload; the winner is cached per (D, P, cells) next to the library."""
-    cache = os.path.join(ROOT, "ader-dg-amr_gb300", "_build", "autotune.json")
-    key = f"D{w['D']}P{w['P']}_n{'x'.join(map(str, w['n'][:w['D']]))}"
-    try:
-        db = json.load(open(cache))
-    except Exception:
-        db = {}
-    if key in db:
-        return db[key]["E"], db[key]
-    choices = [8, 16, 32] if w["D"] == 2 else [4, 8, 16]
-    res = {}
-    for E in choices:
-        s = make_sim(G, w, E)
-        s.advance(2, use_graph=False)
-        res[E] = s.time_kernels(steps)["predictor"]
-        s.close()
-    best = min(res, key=res.get)
-    db[key] = {"E": best, "predictor_ms": {str(k): v for k, v in res.items()}}
-    try:
-        os.makedirs(os.path.dirname(cache), exist_ok=True)
-        json.dump(db, open(cache, "w"), indent=1)
-    except Exception:
-        pass
-    return best, db[key]
+    """The library's autotuner (adg_autotune) on this workload: every
+    elements-per-block choice of the plain predictor timed on the workload's
+    own layout after two steps (state restored); the choice is recorded in
+    the tune cache (ADG_TUNE_CACHE) and taken by the contexts created
+    afterwards with elems_per_block = 0, which is what the timed runs use."""
+    s = make_sim(G, w, 0)
+    s.advance(2, use_graph=False)
+    r = s.autotune(steps)
+    s.close()
+    return 0, {"E": r["E"], "predictor_ms": {str(k): v for k, v in r["ms"].items()}}
+
+
+def autotune_seeded(G, w, seed, steps=3):
+    """The same for the seeded FP32 predictor (two sweeps from the seed)."""
+    s = make_sim(G, w, 0)
+    seed.attach(s, mode=2, sweeps=2, tol=1e-3)
+    s.advance(2, use_graph=False)
+    r = s.autotune(steps)
+    s.close()
+    return {"E": r["E"], "predictor_ms": {str(k): v for k, v in r["ms"].items()}}
 
 
 def oracle_sim(w):
@@ -693,8 +690,10 @@ def run_ours(args, w):
     seed_info = None
     is_amr = "amr" in w
     only = args.only
+    tune_seeded = None
     if is_amr and not args.no_seed and only != "plain_fp64":
         seed, seed_info = train_seed(G, w, cache=seed_cache_path(args.workload) if args.seed_cache else None)
+        tune_seeded = autotune_seeded(G, w, seed)
     if only:  # one variant, for profiling: no accuracy reference, no JSON contract line
         kw = SEED_VARIANTS.get(only, {})
         r = timed_run(G, w, E, args.steps, args.warmup, seed=seed if kw else None, **kw,
@@ -821,7 +820,7 @@ def run_ours(args, w):
                          "predictor; FP32 Picard sweeps and flux changes; TF32 tensor-core seed network"),
         "data": "synthetic",
         "config": base_config(args, w, world),
-        "run": {"path": head_name, "elems_per_block": E, "cuda_graph": True,
+        "run": {"path": head_name, "autotune": {"plain": tune, "seeded": tune_seeded}, "cuda_graph": True,
                 "parallelism": "replicas" if world > 1 else "1 GPU",
                 "l2": f"flushed before every timed step ({L2_FLUSH_BYTES >> 20} MiB device memset, outside "
                       "the per-step CUDA-event intervals that are summed)"},

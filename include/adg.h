@@ -326,6 +326,24 @@ int adg_advance_timed_flushed(adg_ctx* ctx, int nsteps, int use_graph, int64_t f
  * 7 the fallback pass (5-7: 0 without a seed). */
 int adg_time_kernels(adg_ctx* ctx, int nsteps, double* ms, int nkinds);
 
+/* Autotuner of the predictor's elements per block (the launch shape of its
+ * largest kernel; results do not depend on it, bit for bit): times every
+ * choice the configuration is built with for nsteps steps of the context's
+ * current layout, from a snapshot of the state that is restored afterwards
+ * (the context's state, time, step count and counters are unchanged), keeps
+ * the fastest in the context and records it per GPU model, (D, P), level-0
+ * grid, finest level and stage (plain FP64, or the attached seed's mode) in
+ * a text file: ADG_TUNE_CACHE, else $HOME/.cache/adg_gb300/tune.txt.
+ * Contexts created with elems_per_block = 0 take the recorded choice at
+ * adg_init and adg_seed_attach.  With a seed attached the seeded predictor is
+ * tuned, else the plain one.  *E_out (may be NULL) receives the choice,
+ * ms[i] (cap entries, may be NULL) the per-step predictor time of choice i in
+ * the order of the configuration's choices.  No reference counterpart. */
+int adg_autotune(adg_ctx* ctx, int nsteps, int* E_out, double* ms, int cap);
+/* The elements-per-block choices the configuration is built with (up to cap)
+ * and the ones in use by the plain and the seeded predictor. */
+int adg_block_choices(const adg_ctx* ctx, int* choices, int cap, int* n, int* E_plain, int* E_seeded);
+
 /* Page-locked host buffers for host<->device state copies. */
 int adg_host_alloc(size_t bytes, void** ptr);
 int adg_host_free(void* ptr);
