@@ -392,7 +392,14 @@ def seed_cache_path(name):
     return os.path.join(ROOT, "ader-dg-amr_gb300", "_build", f"seed_{name}.npy")
 
 
-def train_seed(G, w, n_pairs=2_000_000, epochs=40, cache=None):
+# Adam schedules of the seed, (epochs, batch, learning rate) stages: the
+# headline's (2 M pairs, 8 s on a GB300) and config 4's recipe for a single
+# sweep from the seed (8 M pairs and a three-stage decay, about 70 s)
+SEED_SCHEDULE = ((40, 8192, 1e-3), (20, 8192, 2e-4))
+SEED_SCHEDULE_1SWEEP = ((80, 16384, 2e-3), (60, 16384, 5e-4), (40, 16384, 1e-4))
+
+
+def train_seed(G, w, n_pairs=2_000_000, schedule=SEED_SCHEDULE, cache=None):
     """Learned seed trained on pairs from the Picard predictor (8 sweeps) of
     perturbed single-level and AMR runs of the workload's configuration (2D),
     or of the workload's own AMR run (3D).
@@ -434,14 +441,15 @@ def train_seed(G, w, n_pairs=2_000_000, epochs=40, cache=None):
         s.close()
         k += 1
     t1 = time.perf_counter()
-    loss = seed.train(epochs, batch=8192, lr=1e-3)
-    loss = seed.train(epochs // 2, batch=8192, lr=2e-4)
+    loss = None
+    for ep, batch, lr in schedule:
+        loss = seed.train(ep, batch=batch, lr=lr)
     t2 = time.perf_counter()
     if cache:
         os.makedirs(os.path.dirname(cache), exist_ok=True)
         np.save(cache, seed.get_params())
     return seed, {"pairs": seed.num_samples(), "collect_s": t1 - t0, "train_s": t2 - t1, "final_loss": loss,
-                  "epochs": epochs + epochs // 2}
+                  "epochs": sum(st[0] for st in schedule), "schedule": [list(st) for st in schedule]}
 
 
 def timed_run(G, w, E, steps, warmup, seed=None, mode=0, sweeps=0, tol=1e-3, plain_sweeps=0, clocks=True):
@@ -652,7 +660,7 @@ def run_other_configs(G, args):
                                 "leaf_value": r["leaf_dof_per_s"], "clocks": r["clocks"]}}
         r["sim"].close()
         if "amr" in w and not args.no_seed:
-            seed, info = train_seed(G, w, n_pairs=1_000_000, epochs=30)
+            seed, info = train_seed(G, w, n_pairs=1_000_000, schedule=((30, 8192, 1e-3), (15, 8192, 2e-4)))
             rs = timed_run(G, w, 0, steps, 3, seed=seed, mode=2, sweeps=2, tol=1e-3)
             entry["seed_2sweeps_fp32"] = {"value": rs["dof_per_s"], "ms_per_step": rs["ms"] / steps,
                                           "fallback_rate": rs.get("fallback_rate"), "seed_training": info,
@@ -713,6 +721,12 @@ def run_ours(args, w):
         for name, kw in SEED_VARIANTS.items():
             variants[name] = timed_run(G, w, E, args.steps, args.warmup, seed=seed, tol=1e-3, **kw)
         variants["noseed_1sweep_fp64"] = timed_run(G, w, E, args.steps, args.warmup, plain_sweeps=1)
+        c4_info = None
+        if not args.no_config4_recipe:  # config 4 as stated: one sweep from a seed trained longer
+            seed4, c4_info = train_seed(G, w, n_pairs=8_000_000, schedule=SEED_SCHEDULE_1SWEEP)
+            for name, kw in (("c4_seed_1sweep_fp64", dict(mode=1, sweeps=1)),
+                             ("c4_seed_1sweep_fp32", dict(mode=2, sweeps=1))):
+                variants[name] = timed_run(G, w, E, args.steps, args.warmup, seed=seed4, tol=1e-3, **kw)
         orc = None
         if not args.no_oracle_accuracy:
             import oracle_ffi as O
@@ -729,12 +743,18 @@ def run_ours(args, w):
             if orc is not None and same_layout(sv, orc):
                 v["l2_density_leaf_vs_oracle"] = orc.norm_diff([sv.get_U_w(l) for l in range(sv.num_levels())], 2, 0)
         plain_err = variants["plain_fp64"]["l2_density_vs_converged"]
-        ok = {k: v for k, v in variants.items() if k.startswith("seed") and v["l2_density_vs_converged"] <= 1.01 * plain_err}
-        head_name = max(ok, key=lambda k: ok[k]["dof_per_s"]) if ok else "plain_fp64"
         plain_leaf = variants["plain_fp64"].get("l2_density_leaf_vs_converged")
+
+        def passes(v):  # within 1.01x of the plain path on the level-0 field and on the leaf cells
+            leaf = v.get("l2_density_leaf_vs_converged")
+            return (v["l2_density_vs_converged"] <= 1.01 * plain_err and
+                    (leaf is None or plain_leaf is None or leaf <= 1.01 * plain_leaf))
+        ok = {k: v for k, v in variants.items() if (k.startswith("seed") or k.startswith("c4_")) and passes(v)}
+        head_name = max(ok, key=lambda k: ok[k]["dof_per_s"]) if ok else "plain_fp64"
         accuracy = {
             "criterion": "L2 density against a converged-Picard (8 FP64 sweeps) run of the same workload after the "
-                         "same steps within 1.01x of the plain FP64 path's; level-0 field (exact modal norm) decides",
+                         "same steps within 1.01x of the plain FP64 path's, on the level-0 field (exact modal norm) "
+                         "and on the leaf cells of every level: the headline variant passes both",
             "plain": plain_err, "headline": variants[head_name].get("l2_density_vs_converged"),
             "leaf_cells": {"plain": plain_leaf, "headline": variants[head_name].get("l2_density_leaf_vs_converged"),
                            "headline_passes": (None if plain_leaf is None or
@@ -745,8 +765,17 @@ def run_ours(args, w):
                                     "differs from it by rounding only, so against the oracle every seeded variant's "
                                     "figure is its deviation from the reference's predictor, not an error that the "
                                     "1.01x criterion can compare"),
-            "config4_as_stated": {"variant": "seed_1sweep_fp64", "l2": variants["seed_1sweep_fp64"]["l2_density_vs_converged"],
-                                  "passes": variants["seed_1sweep_fp64"]["l2_density_vs_converged"] <= 1.01 * plain_err},
+            "config4_as_stated": {v: {"l2_level0": variants[v]["l2_density_vs_converged"],
+                                      "l2_leaf": variants[v].get("l2_density_leaf_vs_converged"),
+                                      "passes_level0": bool(variants[v]["l2_density_vs_converged"] <= 1.01 * plain_err),
+                                      "passes_leaf": (None if variants[v].get("l2_density_leaf_vs_converged") is None
+                                                      or plain_leaf is None else
+                                                      bool(variants[v]["l2_density_leaf_vs_converged"]
+                                                           <= 1.01 * plain_leaf)),
+                                      "dof_per_s": variants[v]["dof_per_s"]}
+                                  for v in ("seed_1sweep_fp64", "c4_seed_1sweep_fp64", "c4_seed_1sweep_fp32")
+                                  if v in variants},
+            "config4_seed_training": c4_info,
         }
     else:
         head_name = "plain_fp64"
@@ -870,6 +899,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-oracle-accuracy", action="store_true",
                     help="skip the equal-L2 comparison of every variant with the FP64 oracle")
+    ap.add_argument("--no-config4-recipe", action="store_true",
+                    help="skip config 4's single-sweep recipe (a longer-trained seed, about a minute)")
     ap.add_argument("--no-other-configs", action="store_true",
                     help="skip the timing of the other benchmark configurations")
     ap.add_argument("--only", default=None,
