@@ -1569,13 +1569,18 @@ __global__ void k_average_down(double* Uw, const int* rec, int nrec) {
   }
   __syncthreads();
   double* out = fine;  // the children are consumed: [RB][EL] coarse states
-  if (L == 0 && r < nr) {
+  // mode n of every (record, variable) summed by row n mod 2^D: the FP64 work
+  // of the sums spread over all warps (and so over the SM's four schedulers)
+  if (r < nr) {
 #pragma unroll
-    for (int n = 0; n < NP_S; ++n) {
-      double sum = 0.0;
+    for (int n0 = 0; n0 < NP_S; n0 += NOV) {
+      const int n = n0 + L;
+      if (n < NP_S) {
+        double sum = 0.0;
 #pragma unroll
-      for (int l = 0; l < NOV; ++l) sum = __dadd_rn(sum, part[l][n][x]);  // as k_interp_gather
-      out[r * EL + q * NP_S + n] = (1.0 / NOV) * (O::minv(n) * sum);
+        for (int l = 0; l < NOV; ++l) sum = __dadd_rn(sum, part[l][n][x]);  // as k_interp_gather
+        out[r * EL + q * NP_S + n] = (1.0 / NOV) * (O::minv(n) * sum);
+      }
     }
   }
   __syncthreads();
