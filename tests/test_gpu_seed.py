@@ -315,6 +315,40 @@ def test_tensor_core_seed_matches_float64_restatement():
     assert e_max < 1e-2 and e_rms < 3e-3, (e_max, e_rms)
 
 
+@pytest.mark.parametrize("case", ["vortex_p1", "vortex_p2", "blast3d_p1_per", "blast3d_p2"])
+def test_tensor_core_seed_matches_simt_path_on_every_configuration(case):
+    """The fused tcgen05 inference against the SIMT FP32 path on the other
+    compiled (D, P): output widths that are not a multiple of four (D = 3),
+    a partial last tile (192 elements) and the FP64 output.  Both paths give
+    H = W U + rho_mean Dt/dx Y(x); their network parts H - W U differ by the
+    TF32 rounding of the operands only."""
+    torch = pytest.importorskip("torch")
+    import oracle_ffi as O
+    s = make_gpu(case)
+    seed = G.PredictorSeed(s.D, s.P, hidden=128, rng_seed=19)
+    seed.attach(s, mode=2, sweeps=2, tol=1e-3)
+    s.time_integration()
+    U = s.get_U_w()
+    n, Q, Ns = U.shape
+    Nst = s.Np_st
+    out = {}
+    for path in (0, 1):
+        b = torch.full((n * Q * Nst,), float("nan"), dtype=torch.float64, device="cuda")
+        s.seed_infer(b.data_ptr(), path)
+        torch.cuda.synchronize()
+        out[path] = b.cpu().numpy().reshape(n, Q, Nst)
+    assert s.status() == 0
+    assert np.all(np.isfinite(out[0])) and np.all(np.isfinite(out[1]))
+    W = O.matrix(s.D, s.P, "Mk_h_w_inv") @ O.matrix(s.D, s.P, "Mk_pred")  # a 0/1 selection
+    WU = np.einsum("kn,eqn->eqk", W, U)
+    net0, net1 = out[0] - WU, out[1] - WU
+    scale = np.max(np.abs(net0))
+    assert scale > 0.0
+    e_max = np.max(np.abs(net1 - net0)) / scale
+    e_rms = np.sqrt(np.mean((net1 - net0) ** 2)) / np.sqrt(np.mean(net0 ** 2))
+    assert e_max < 1e-2 and e_rms < 3e-3, (e_max, e_rms)
+
+
 @pytest.mark.parametrize("mode", [1, 2])
 def test_seeded_run_stays_close_to_plain_run(mode):
     seed, _, _ = _trained_seed()
