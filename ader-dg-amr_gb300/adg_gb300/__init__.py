@@ -96,6 +96,8 @@ def lib():
         "adg_level_cells": ([vp, i, ctypes.POINTER(ctypes.c_int64)], i),
         "adg_get_state": ([vp, i, vp, i], i),
         "adg_set_state": ([vp, i, vp, i], i),
+        "adg_set_readback": ([vp, i, vp, ctypes.c_int64], i),
+        "adg_readback_active": ([vp, i, ctypes.POINTER(i)], i),
         "adg_get_dt": ([vp, dp], i),
         "adg_set_dt": ([vp, ctypes.c_double], i),
         "adg_compute_dt": ([vp, dp], i),
@@ -469,6 +471,26 @@ class AmrDG:
         assert pinned.array.shape == (self.level_cells(lev), self.Q, self.Np_s)
         self._check(self._L.adg_set_state(self.ctx, lev, pinned.array.ctypes.data, ADG_MEM_HOST_ASYNC),
                     "adg_set_state")
+
+    def set_readback(self, pinned, lev=0):
+        """Register a PinnedArray of shape (capacity, Q, Np_s), capacity at
+        least the level's cells, whose first level_cells(lev) rows receive
+        level lev's state at the end of every step of advance(), copied beside
+        the rest of the step (adg_set_readback); None clears.  Valid after
+        synchronize(); see readback_active() after a regrid."""
+        if pinned is None:
+            self._check(self._L.adg_set_readback(self.ctx, lev, None, 0), "adg_set_readback")
+            return
+        assert pinned.array.shape[1:] == (self.Q, self.Np_s) and pinned.array.shape[0] >= self.level_cells(lev)
+        self._check(self._L.adg_set_readback(self.ctx, lev, pinned.array.ctypes.data, pinned.array.shape[0]),
+                    "adg_set_readback")
+
+    def readback_active(self, lev=0):
+        """False once a regrid removed the level or grew it past the buffer
+        (the registration is then dropped)."""
+        v = ctypes.c_int()
+        self._check(self._L.adg_readback_active(self.ctx, lev, ctypes.byref(v)), "adg_readback_active")
+        return bool(v.value)
 
     # ------------------------------------------------------------ L2ProjInterp
     def amr_scatter(self, coarse, child):

@@ -212,6 +212,15 @@ struct adg_ctx {
   // down and the Dt reduction (disjoint elements)
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // step readback (adg_set_readback): page-locked host buffers that receive
+  // a level's valid state at the end of every step, copied on their own
+  // stream once the step's last writer of the level has run
+  double* rb_host[kMaxLevels] = {};
+  int64_t rb_cap[kMaxLevels] = {};  // capacity in cells
+  cudaStream_t rb = nullptr;
+  cudaEvent_t rb_ev[kMaxLevels] = {};
+  cudaEvent_t rb_join = nullptr;
+  bool rb_pending = false;
 
   ~adg_ctx() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
@@ -236,6 +245,10 @@ struct adg_ctx {
     if (fork_ev) cudaEventDestroy(fork_ev);
     if (join_ev) cudaEventDestroy(join_ev);
     if (side) cudaStreamDestroy(side);
+    if (rb) cudaStreamSynchronize(rb), cudaStreamDestroy(rb);
+    for (cudaEvent_t& e : rb_ev)
+      if (e) cudaEventDestroy(e);
+    if (rb_join) cudaEventDestroy(rb_join);
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 };
@@ -547,22 +560,79 @@ int flush_ghosts(adg_ctx* ctx) {
   return ctx->hier.nlevels() > 1 ? launch_ghost_fill(ctx) : ADG_OK;
 }
 
-int launch_average_down(adg_ctx* ctx) {
+// Readback of level lev (adg_set_readback) once the step's last writer of
+// the level is queued on the context's stream: the copy waits for that point
+// only and runs on the readback stream beside the rest of the step.  A
+// registration whose buffer no longer holds the level is dropped, so that it
+// never writes past a buffer or into one the caller has released.
+int readback_level(adg_ctx* ctx, int lev) {
+  if (lev < 0 || lev >= kMaxLevels || !ctx->rb_host[lev]) return ADG_OK;
+  const Hierarchy& H = ctx->hier;
+  if (lev >= H.nlevels() || (int64_t)H.level_valid_count(lev) > ctx->rb_cap[lev]) {
+    ctx->rb_host[lev] = nullptr;
+    ctx->rb_cap[lev] = 0;
+    return ADG_OK;
+  }
+  const size_t per = (size_t)ctx->ks->Q * ctx->ks->Np_s;
+  ADG_CUDA(cudaEventRecord(ctx->rb_ev[lev], ctx->stream), "readback fork");
+  ADG_CUDA(cudaStreamWaitEvent(ctx->rb, ctx->rb_ev[lev], 0), "readback fork");
+  ADG_CUDA(cudaMemcpyAsync(ctx->rb_host[lev], ctx->Uw.p + H.level_valid_offset(lev) * per,
+                           H.level_valid_count(lev) * per * sizeof(double), cudaMemcpyDeviceToHost, ctx->rb),
+           "readback copy");
+  ctx->rb_pending = true;
+  return ADG_OK;
+}
+
+// The step's readback copies joined back into the context's stream: later
+// work on the stream (the next step, a regrid, adg_set_state) waits for them.
+int readback_join(adg_ctx* ctx) {
+  if (!ctx->rb_pending) return ADG_OK;
+  ctx->rb_pending = false;
+  ADG_CUDA(cudaEventRecord(ctx->rb_join, ctx->rb), "readback join");
+  ADG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->rb_join, 0), "readback join");
+  return ADG_OK;
+}
+
+// Registrations of levels the layout no longer has, or that outgrew their
+// buffer, are dropped (they never reactivate into a buffer the caller may
+// have released); true if any remains.
+bool readback_prune(adg_ctx* ctx) {
+  bool any = false;
+  for (int l = 0; l < kMaxLevels; ++l) {
+    if (!ctx->rb_host[l]) continue;
+    if (l >= ctx->hier.nlevels() || (int64_t)ctx->hier.level_valid_count(l) > ctx->rb_cap[l]) {
+      ctx->rb_host[l] = nullptr;
+      ctx->rb_cap[l] = 0;
+    } else {
+      any = true;
+    }
+  }
+  return any;
+}
+
+// readback: each coarser level is read back once its average down is queued
+// (the finest one before the call).
+int launch_average_down(adg_ctx* ctx, bool readback = false) {
   const Hierarchy& H = ctx->hier;
   if (H.nlevels() <= 1) return ADG_OK;
   const int NOV1 = (1 << ctx->cfg.D) + 1;
   for (int lf = H.nlevels() - 1; lf >= 1; --lf) {
     const int nrec = (int)(H.ad_rec[lf].size() / NOV1);
-    if (!nrec) continue;
-    cudaError_t e = ctx->ks->average_down(ctx->Uw.p, ctx->ad_all.p + ctx->ad_off[lf], nrec, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "average down launch");
-    ctx->launches++;
+    if (nrec) {
+      cudaError_t e = ctx->ks->average_down(ctx->Uw.p, ctx->ad_all.p + ctx->ad_off[lf], nrec, ctx->stream);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "average down launch");
+      ctx->launches++;
+    }
+    if (readback) {
+      int rc = readback_level(ctx, lf - 1);
+      if (rc) return rc;
+    }
   }
   return ADG_OK;
 }
 
-int launch_amr_sync(adg_ctx* ctx) {
-  int rc = launch_average_down(ctx);
+int launch_amr_sync(adg_ctx* ctx, bool readback = false) {
+  int rc = launch_average_down(ctx, readback);
   if (rc) return rc;
   return ctx->hier.nlevels() > 1 ? launch_ghost_fill(ctx) : ADG_OK;
 }
@@ -635,13 +705,20 @@ int launch_step(adg_ctx* ctx, cudaEvent_t* ev = nullptr) {
     rc = launch_limiter(ctx);
     if (rc) return rc;
   }
+  // the finest level is final here (the average down writes coarser ones)
+  const bool rb = !ev && ctx->rb && readback_prune(ctx);
+  if (rb) {
+    rc = readback_level(ctx, ctx->hier.nlevels() - 1);
+    if (rc) return rc;
+  }
   const bool fork = !ev && ctx->side && ctx->hier.nlevels() > 1 && !ctx->hier.gf_elem.empty();
   if (!fork) {
-    rc = launch_amr_sync(ctx);
+    rc = launch_amr_sync(ctx, rb);
     if (rc) return rc;
     if (ev) cudaEventRecord(ev[4], ctx->stream);
     rc = launch_dt(ctx, 1);
     if (ev) cudaEventRecord(ev[5], ctx->stream);
+    if (rc == ADG_OK && rb) rc = readback_join(ctx);
     return rc;
   }
   // ghost fill on the side stream: it reads valid coarse parents (never
@@ -655,8 +732,9 @@ int launch_step(adg_ctx* ctx, cudaEvent_t* ev = nullptr) {
   ctx->stream = main;
   if (rc) return rc;
   ADG_CUDA(cudaEventRecord(ctx->join_ev, ctx->side), "join");
-  rc = launch_average_down(ctx);
+  rc = launch_average_down(ctx, rb);
   if (rc == ADG_OK) rc = launch_dt(ctx, 1);
+  if (rc == ADG_OK && rb) rc = readback_join(ctx);
   ADG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0), "join");
   return rc;
 }
@@ -1172,6 +1250,7 @@ static void apply_tuned_choices(adg_ctx* ctx);
 
 int adg_init(adg_ctx* ctx) {
   if (!ctx) return ADG_ERR_ARG;
+  for (int l = 0; l < kMaxLevels; ++l) ctx->rb_host[l] = nullptr, ctx->rb_cap[l] = 0;  // a new layout
   const adg_config& c = ctx->cfg;
   const KernelSet* ks = ctx->ks;
   std::string msg;
@@ -1346,6 +1425,41 @@ int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem) {
            "set_state copy");
   if (lev + 1 < ctx->hier.nlevels()) ctx->ghosts_stale = true;  // the finer level's ghosts project from this level
   if (mem != ADG_MEM_HOST_ASYNC) ADG_CUDA(cudaStreamSynchronize(ctx->stream), "set_state sync");
+  return ADG_OK;
+}
+
+int adg_set_readback(adg_ctx* ctx, int lev, double* host, int64_t capacity_cells) {
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (lev < 0 || lev >= ctx->hier.nlevels() || lev >= kMaxLevels) return fail(ctx, ADG_ERR_ARG, "bad level");
+  if (!host) {
+    ctx->rb_host[lev] = nullptr;
+    ctx->rb_cap[lev] = 0;
+    ctx->graph_stale = true;
+    return ADG_OK;
+  }
+  if (capacity_cells < (int64_t)ctx->hier.level_valid_count(lev))
+    return fail(ctx, ADG_ERR_ARG, "readback buffer smaller than the level's valid cells");
+  cudaPointerAttributes pa{};
+  if (cudaPointerGetAttributes(&pa, host) != cudaSuccess || pa.type != cudaMemoryTypeHost) {
+    cudaGetLastError();
+    return fail(ctx, ADG_ERR_ARG, "readback buffer must be page-locked host memory");
+  }
+  if (!ctx->rb) {
+    ADG_CUDA(cudaStreamCreateWithFlags(&ctx->rb, cudaStreamNonBlocking), "readback stream");
+    for (cudaEvent_t& e : ctx->rb_ev) ADG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "readback event");
+    ADG_CUDA(cudaEventCreateWithFlags(&ctx->rb_join, cudaEventDisableTiming), "readback event");
+  }
+  ctx->rb_host[lev] = host;
+  ctx->rb_cap[lev] = capacity_cells;
+  ctx->graph_stale = true;  // the step's graph now carries the copy
+  return ADG_OK;
+}
+
+int adg_readback_active(adg_ctx* ctx, int lev, int* active) {
+  if (!ctx || !active || lev < 0) return ADG_ERR_ARG;
+  readback_prune(ctx);
+  *active = lev < kMaxLevels && ctx->rb_host[lev] != nullptr;
   return ADG_OK;
 }
 

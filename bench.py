@@ -560,6 +560,10 @@ def e2e_device_patches(G, s, w, steps):
     torch.cuda.synchronize()
     npatch = register()
     L, ctx = s._L, s.ctx
+    # one untimed step: a graph made stale by the caller's earlier settings
+    # is captured again here, not in the timed steps
+    if L.adg_read_patches(ctx) != 0 or L.adg_advance(ctx, 1, 1) != 0 or L.adg_write_patches(ctx) != 0:
+        npatch = register()
     d0, _ = s.dof_updates()
     s.synchronize()
     t0 = time.perf_counter()
@@ -785,8 +789,9 @@ def run_ours(args, w):
 
     # end to end through the C ABI with host buffers: every step copies the
     # state of every level in from page-locked host memory, runs the step
-    # (graph replay) and copies every level back out; the copies are queued
-    # on the context's stream and the host waits once per step for the result
+    # (graph replay) and reads every level back out (the step readback: each
+    # level's copy starts once the step has finished writing it, beside the
+    # step's tail); the host waits once per step for the result
     s = head["sim"]
     L, ctx = s._L, s.ctx
     e2e_steps = max(5, min(args.steps, 50))
@@ -798,35 +803,43 @@ def run_ours(args, w):
     def level_cells():
         return [s.level_cells(l) for l in range(s.num_levels())]
 
-    def new_hosts(cells):
-        hs = [G.PinnedArray((n, Q, Nps)) for n in cells]
-        for l, h in enumerate(hs):
-            h.array[:] = s.get_U_w(l)
-        return hs, [h.array.ctypes.data for h in hs]
-
+    # host copies of every level sized for its largest layout (the level
+    # fully refined), registered for the step readback (adg_set_readback):
+    # each step's result lands in them beside the step's tail
+    amr_levels = w.get("amr", {}).get("max_level", 0) + 1
+    full = [1] * amr_levels
+    for lev in range(amr_levels):
+        for d in range(w["D"]):
+            full[lev] *= w["n"][d] << lev
+    hosts = [G.PinnedArray((full[l], Q, Nps)) for l in range(amr_levels)]
+    ptrs = [h.array.ctypes.data for h in hosts]
     cells = level_cells()
-    hosts, ptrs = new_hosts(cells)
+    for l in range(len(cells)):
+        hosts[l].array[:cells[l]] = s.get_U_w(l)
+        s.set_readback(hosts[l], l)
+    s.advance(1, use_graph=True)  # capture the step with its readback copies before timing
+    s.synchronize()
+    cells = level_cells()
     h2d = d2h = 0
     t0 = time.perf_counter()
     d_before, _ = s.dof_updates()
     for _ in range(e2e_steps):
-        if cells != [h.array.shape[0] for h in hosts]:  # a regrid changed the layout
-            for h in hosts:
-                h.free()
-            hosts, ptrs = new_hosts(cells)
-        for l, p in enumerate(ptrs):
-            check(L.adg_set_state(ctx, l, p, G.ADG_MEM_HOST_ASYNC), "adg_set_state")
-            h2d += hosts[l].array.nbytes
+        for l in range(len(cells)):
+            check(L.adg_set_state(ctx, l, ptrs[l], G.ADG_MEM_HOST_ASYNC), "adg_set_state")
+            h2d += cells[l] * Q * Nps * 8
         check(L.adg_advance(ctx, 1, 1), "adg_advance")
         cells = level_cells()
-        for l, p in enumerate(ptrs):
-            if l < len(cells) and hosts[l].array.shape[0] == cells[l]:
-                check(L.adg_get_state(ctx, l, p, G.ADG_MEM_HOST_ASYNC), "adg_get_state")
-                d2h += hosts[l].array.nbytes
+        for l in range(len(cells)):
+            if not s.readback_active(l):  # not registered (cannot happen with full-size buffers)
+                check(L.adg_get_state(ctx, l, ptrs[l], G.ADG_MEM_HOST_ASYNC), "adg_get_state")
+            d2h += cells[l] * Q * Nps * 8
         check(L.adg_synchronize(ctx), "adg_synchronize")
     e2e_s = barrier_max(time.perf_counter() - t0)
     d_after, _ = s.dof_updates()
     e2e_val = (d_after - d_before) * world / e2e_s
+    for l in range(s.num_levels()):
+        s.set_readback(None, l)
+    s.synchronize()
     for h in hosts:
         h.free()
     try:

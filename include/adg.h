@@ -135,8 +135,28 @@ int adg_num_levels(const adg_ctx* ctx, int* nlev);
 int adg_level_cells(const adg_ctx* ctx, int lev, int64_t* ncells);
 int adg_get_state(adg_ctx* ctx, int lev, double* dst, int mem);
 int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem);
+/* Step readback: register a page-locked host buffer with room for
+ * capacity_cells * Q * Np_s doubles (at least the level's valid cells) that
+ * receives level lev's state, as adg_get_state returns it (the level's
+ * current valid cells, adg_level_cells), at the end of every step of
+ * adg_advance.  The copy waits only for the step's last writer of that level
+ * (the corrector or limiter for the finest level, the average down onto it
+ * for the others) and runs on its own stream beside the rest of the step;
+ * the next step and anything queued after adg_advance are ordered after it,
+ * and it is complete after adg_synchronize.  host = NULL clears; a cleared
+ * or replaced buffer may be released after adg_synchronize.  Regrids keep
+ * the registration while the level's cells fit; one that removes the level
+ * or grows it past the capacity drops it, and no copy of the new layout goes
+ * into the buffer (adg_readback_active then reports 0 and the buffer does
+ * not hold that step's state: read it with adg_get_state).  Steps of
+ * adg_time_kernels do not read back.  For a caller that keeps the state on
+ * the host: the per-step output of U_w(l, q) at the end of a step of
+ * AmrDG::evolve (after the limiter and the average down,
+ * Source/NumericalMethod/AmrDG/AmrDG.h:988-1025). */
+int adg_set_readback(adg_ctx* ctx, int lev, double* host, int64_t capacity_cells);
+int adg_readback_active(adg_ctx* ctx, int lev, int* active);
 /* Waits for everything queued on the context's stream (copies of
- * ADG_MEM_HOST_ASYNC, steps of adg_advance). */
+ * ADG_MEM_HOST_ASYNC, steps of adg_advance and their readback). */
 int adg_synchronize(adg_ctx* ctx);
 
 /* Time step size: current Dt (device-computed), set an explicit Dt, or

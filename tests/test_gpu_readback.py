@@ -1,0 +1,107 @@
+"""Step readback (adg_set_readback): registered page-locked host buffers
+receive every level's state at the end of each step of adg_advance, copied
+beside the step's tail.  The buffers must equal adg_get_state after every
+step bit for bit, on one level and on AMR layouts that regrid (graph and
+direct launches), with buffers sized for the level's largest layout and with
+tight ones that a regrid outgrows (the registration is then dropped); the
+results of the steps do not change."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from parity import AMR_CASES, G, make_gpu, make_gpu_amr
+
+pytestmark = pytest.mark.gpu
+
+
+def _capacity(s, case, lev, tight):
+    if tight:
+        return s.level_cells(lev)
+    n = AMR_CASES[case][2]
+    full = 1
+    for d in range(s.D):
+        full *= n[d] << lev
+    return full
+
+
+def _run(s, case, steps, use_graph, tight):
+    """Steps with readback on every level; returns how often a registration
+    was found dropped (a level grown past its buffer or a new level)."""
+    bufs = {}
+
+    def register(lev):
+        b = G.PinnedArray((_capacity(s, case, lev, tight), s.Q, s.Np_s))
+        s.set_readback(b, lev)
+        bufs[lev] = b
+
+    for lev in range(s.num_levels()):
+        register(lev)
+    dropped = 0
+    for _ in range(steps):
+        for b in bufs.values():
+            b.array[:] = np.nan
+        s.advance(1, use_graph=use_graph)
+        s.synchronize()
+        for lev in range(s.num_levels()):
+            u = s.get_U_w(lev)
+            if lev in bufs and s.readback_active(lev):
+                got = bufs[lev].array[: u.shape[0]]
+                assert np.array_equal(got, u), lev
+                assert np.all(np.isnan(bufs[lev].array[u.shape[0]:]))  # nothing past the level's cells
+            else:
+                assert lev not in bufs or s.level_cells(lev) > bufs[lev].array.shape[0]
+                dropped += 1
+                if lev in bufs:
+                    bufs.pop(lev).free()  # dropped: the library no longer writes it
+                register(lev)
+        for lev in [l for l in bufs if l >= s.num_levels()]:
+            bufs.pop(lev).free()  # a level the layout no longer has: dropped too
+    for lev in range(s.num_levels()):
+        if lev in bufs:
+            s.set_readback(None, lev)
+    s.synchronize()
+    for b in bufs.values():
+        b.free()
+    return dropped
+
+
+@pytest.mark.parametrize("case,use_graph,tight", [("kh_p3_amr", True, False), ("kh_p3_amr", False, False),
+                                                  ("kh_p3_amr", True, True), ("kh_p2_amr_rect", True, True)])
+def test_readback_equals_get_state_after_every_step_amr(case, use_graph, tight):
+    a = make_gpu_amr(case)
+    b = make_gpu_amr(case)
+    dropped = _run(a, case, 12, use_graph, tight)
+    if not tight:
+        assert dropped == 0  # buffers for the largest layout never drop
+    b.advance(12, use_graph=use_graph)  # the same steps without readback
+    assert a.num_levels() == b.num_levels()
+    for lev in range(a.num_levels()):
+        assert np.array_equal(a.get_U_w(lev), b.get_U_w(lev)), lev
+    assert a.status() == 0
+
+
+def test_readback_single_level():
+    a = make_gpu("kh_p3")
+    b = make_gpu("kh_p3")
+    assert _run(a, None, 5, True, True) == 0
+    b.advance(5)
+    assert np.array_equal(a.get_U_w(0), b.get_U_w(0))
+
+
+def test_readback_argument_checks():
+    s = make_gpu("kh_p3")
+    n = s.level_cells(0)
+    L, ctx = s._L, s.ctx
+    pageable = np.zeros((n, s.Q, s.Np_s))
+    assert L.adg_set_readback(ctx, 0, pageable.ctypes.data, n) != 0  # not page-locked
+    p = G.PinnedArray((n, s.Q, s.Np_s))
+    assert L.adg_set_readback(ctx, 0, p.array.ctypes.data, n - 1) != 0  # smaller than the level
+    assert L.adg_set_readback(ctx, 1, p.array.ctypes.data, n) != 0  # no such level
+    v = ctypes.c_int(7)
+    assert L.adg_readback_active(ctx, 0, ctypes.byref(v)) == 0 and v.value == 0
+    assert L.adg_set_readback(ctx, 0, p.array.ctypes.data, n) == 0
+    assert s.readback_active(0)
+    s.set_readback(None, 0)
+    assert not s.readback_active(0)
+    p.free()
