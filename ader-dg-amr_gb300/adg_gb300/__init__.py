@@ -27,6 +27,7 @@ ADG_OK = 0
 ADG_MEM_HOST = 0
 ADG_MEM_DEVICE = 1
 ADG_MEM_HOST_ASYNC = 2
+ADG_ALL_LEVELS = -1
 IC_CODES = {"isentropic_vortex": 0, "vortex": 0, "kh_noise": 1, "kelvin_helmolz_instability": 2,
             "kh_ref": 2, "blast3d": 3, "const": 4}
 

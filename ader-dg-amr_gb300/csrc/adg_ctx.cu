@@ -217,6 +217,8 @@ struct adg_ctx {
   // stream once the step's last writer of the level has run
   double* rb_host[kMaxLevels] = {};
   int64_t rb_cap[kMaxLevels] = {};  // capacity in cells
+  double* rb_all = nullptr;         // every level packed in level order (ADG_ALL_LEVELS)
+  int64_t rb_all_cap = 0;
   cudaStream_t rb = nullptr;
   cudaEvent_t rb_ev[kMaxLevels] = {};
   cudaEvent_t rb_join = nullptr;
@@ -566,19 +568,27 @@ int flush_ghosts(adg_ctx* ctx) {
 // registration whose buffer no longer holds the level is dropped, so that it
 // never writes past a buffer or into one the caller has released.
 int readback_level(adg_ctx* ctx, int lev) {
-  if (lev < 0 || lev >= kMaxLevels || !ctx->rb_host[lev]) return ADG_OK;
+  if (lev < 0 || lev >= kMaxLevels) return ADG_OK;
   const Hierarchy& H = ctx->hier;
-  if (lev >= H.nlevels() || (int64_t)H.level_valid_count(lev) > ctx->rb_cap[lev]) {
+  if (ctx->rb_host[lev] && (lev >= H.nlevels() || (int64_t)H.level_valid_count(lev) > ctx->rb_cap[lev])) {
     ctx->rb_host[lev] = nullptr;
     ctx->rb_cap[lev] = 0;
-    return ADG_OK;
   }
+  if (ctx->rb_all && (int64_t)H.n_valid() > ctx->rb_all_cap) {
+    ctx->rb_all = nullptr;
+    ctx->rb_all_cap = 0;
+  }
+  if (lev >= H.nlevels() || (!ctx->rb_host[lev] && !ctx->rb_all)) return ADG_OK;
   const size_t per = (size_t)ctx->ks->Q * ctx->ks->Np_s;
+  const size_t off = H.level_valid_offset(lev) * per, bytes = H.level_valid_count(lev) * per * sizeof(double);
   ADG_CUDA(cudaEventRecord(ctx->rb_ev[lev], ctx->stream), "readback fork");
   ADG_CUDA(cudaStreamWaitEvent(ctx->rb, ctx->rb_ev[lev], 0), "readback fork");
-  ADG_CUDA(cudaMemcpyAsync(ctx->rb_host[lev], ctx->Uw.p + H.level_valid_offset(lev) * per,
-                           H.level_valid_count(lev) * per * sizeof(double), cudaMemcpyDeviceToHost, ctx->rb),
-           "readback copy");
+  if (ctx->rb_host[lev])
+    ADG_CUDA(cudaMemcpyAsync(ctx->rb_host[lev], ctx->Uw.p + off, bytes, cudaMemcpyDeviceToHost, ctx->rb),
+             "readback copy");
+  if (ctx->rb_all)  // the packed buffer holds the levels at the same offsets as the state
+    ADG_CUDA(cudaMemcpyAsync(ctx->rb_all + off, ctx->Uw.p + off, bytes, cudaMemcpyDeviceToHost, ctx->rb),
+             "readback copy");
   ctx->rb_pending = true;
   return ADG_OK;
 }
@@ -597,7 +607,11 @@ int readback_join(adg_ctx* ctx) {
 // buffer, are dropped (they never reactivate into a buffer the caller may
 // have released); true if any remains.
 bool readback_prune(adg_ctx* ctx) {
-  bool any = false;
+  if (ctx->rb_all && (int64_t)ctx->hier.n_valid() > ctx->rb_all_cap) {
+    ctx->rb_all = nullptr;
+    ctx->rb_all_cap = 0;
+  }
+  bool any = ctx->rb_all != nullptr;
   for (int l = 0; l < kMaxLevels; ++l) {
     if (!ctx->rb_host[l]) continue;
     if (l >= ctx->hier.nlevels() || (int64_t)ctx->hier.level_valid_count(l) > ctx->rb_cap[l]) {
@@ -1251,6 +1265,8 @@ static void apply_tuned_choices(adg_ctx* ctx);
 int adg_init(adg_ctx* ctx) {
   if (!ctx) return ADG_ERR_ARG;
   for (int l = 0; l < kMaxLevels; ++l) ctx->rb_host[l] = nullptr, ctx->rb_cap[l] = 0;  // a new layout
+  ctx->rb_all = nullptr;
+  ctx->rb_all_cap = 0;
   const adg_config& c = ctx->cfg;
   const KernelSet* ks = ctx->ks;
   std::string msg;
@@ -1402,10 +1418,12 @@ int adg_level_cells(const adg_ctx* ctx, int lev, int64_t* ncells) {
 int adg_get_state(adg_ctx* ctx, int lev, double* dst, int mem) {
   int rc = check_ready(ctx);
   if (rc) return rc;
-  if (!dst || lev < 0 || lev >= ctx->hier.nlevels() || mem < 0 || mem > 2) return fail(ctx, ADG_ERR_ARG, "bad level, pointer or memory kind");
+  const bool all = lev == ADG_ALL_LEVELS;
+  if (!dst || (!all && (lev < 0 || lev >= ctx->hier.nlevels())) || mem < 0 || mem > 2)
+    return fail(ctx, ADG_ERR_ARG, "bad level, pointer or memory kind");
   const size_t per = (size_t)ctx->ks->Q * ctx->ks->Np_s;
-  const size_t off = ctx->hier.level_valid_offset(lev) * per;
-  const size_t cnt = ctx->hier.level_valid_count(lev) * per;
+  const size_t off = all ? 0 : ctx->hier.level_valid_offset(lev) * per;  // the levels are stored in order
+  const size_t cnt = (all ? ctx->hier.n_valid() : ctx->hier.level_valid_count(lev)) * per;
   ADG_CUDA(cudaMemcpyAsync(dst, ctx->Uw.p + off, cnt * sizeof(double),
                            mem == ADG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream),
            "get_state copy");
@@ -1416,14 +1434,17 @@ int adg_get_state(adg_ctx* ctx, int lev, double* dst, int mem) {
 int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem) {
   int rc = check_ready(ctx);
   if (rc) return rc;
-  if (!src || lev < 0 || lev >= ctx->hier.nlevels() || mem < 0 || mem > 2) return fail(ctx, ADG_ERR_ARG, "bad level, pointer or memory kind");
+  const bool all = lev == ADG_ALL_LEVELS;
+  if (!src || (!all && (lev < 0 || lev >= ctx->hier.nlevels())) || mem < 0 || mem > 2)
+    return fail(ctx, ADG_ERR_ARG, "bad level, pointer or memory kind");
   const size_t per = (size_t)ctx->ks->Q * ctx->ks->Np_s;
-  const size_t off = ctx->hier.level_valid_offset(lev) * per;
-  const size_t cnt = ctx->hier.level_valid_count(lev) * per;
+  const size_t off = all ? 0 : ctx->hier.level_valid_offset(lev) * per;
+  const size_t cnt = (all ? ctx->hier.n_valid() : ctx->hier.level_valid_count(lev)) * per;
   ADG_CUDA(cudaMemcpyAsync(ctx->Uw.p + off, src, cnt * sizeof(double),
                            mem == ADG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream),
            "set_state copy");
-  if (lev + 1 < ctx->hier.nlevels()) ctx->ghosts_stale = true;  // the finer level's ghosts project from this level
+  if (all ? ctx->hier.nlevels() > 1 : lev + 1 < ctx->hier.nlevels())
+    ctx->ghosts_stale = true;  // the finer level's ghosts project from this level
   if (mem != ADG_MEM_HOST_ASYNC) ADG_CUDA(cudaStreamSynchronize(ctx->stream), "set_state sync");
   return ADG_OK;
 }
@@ -1431,14 +1452,20 @@ int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem) {
 int adg_set_readback(adg_ctx* ctx, int lev, double* host, int64_t capacity_cells) {
   int rc = check_ready(ctx);
   if (rc) return rc;
-  if (lev < 0 || lev >= ctx->hier.nlevels() || lev >= kMaxLevels) return fail(ctx, ADG_ERR_ARG, "bad level");
+  const bool all = lev == ADG_ALL_LEVELS;
+  if (!all && (lev < 0 || lev >= ctx->hier.nlevels() || lev >= kMaxLevels)) return fail(ctx, ADG_ERR_ARG, "bad level");
   if (!host) {
-    ctx->rb_host[lev] = nullptr;
-    ctx->rb_cap[lev] = 0;
+    if (all) {
+      ctx->rb_all = nullptr;
+      ctx->rb_all_cap = 0;
+    } else {
+      ctx->rb_host[lev] = nullptr;
+      ctx->rb_cap[lev] = 0;
+    }
     ctx->graph_stale = true;
     return ADG_OK;
   }
-  if (capacity_cells < (int64_t)ctx->hier.level_valid_count(lev))
+  if (capacity_cells < (int64_t)(all ? ctx->hier.n_valid() : ctx->hier.level_valid_count(lev)))
     return fail(ctx, ADG_ERR_ARG, "readback buffer smaller than the level's valid cells");
   cudaPointerAttributes pa{};
   if (cudaPointerGetAttributes(&pa, host) != cudaSuccess || pa.type != cudaMemoryTypeHost) {
@@ -1450,16 +1477,21 @@ int adg_set_readback(adg_ctx* ctx, int lev, double* host, int64_t capacity_cells
     for (cudaEvent_t& e : ctx->rb_ev) ADG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "readback event");
     ADG_CUDA(cudaEventCreateWithFlags(&ctx->rb_join, cudaEventDisableTiming), "readback event");
   }
-  ctx->rb_host[lev] = host;
-  ctx->rb_cap[lev] = capacity_cells;
+  if (all) {
+    ctx->rb_all = host;
+    ctx->rb_all_cap = capacity_cells;
+  } else {
+    ctx->rb_host[lev] = host;
+    ctx->rb_cap[lev] = capacity_cells;
+  }
   ctx->graph_stale = true;  // the step's graph now carries the copy
   return ADG_OK;
 }
 
 int adg_readback_active(adg_ctx* ctx, int lev, int* active) {
-  if (!ctx || !active || lev < 0) return ADG_ERR_ARG;
+  if (!ctx || !active || (lev < 0 && lev != ADG_ALL_LEVELS)) return ADG_ERR_ARG;
   readback_prune(ctx);
-  *active = lev < kMaxLevels && ctx->rb_host[lev] != nullptr;
+  *active = lev == ADG_ALL_LEVELS ? ctx->rb_all != nullptr : (lev < kMaxLevels && ctx->rb_host[lev] != nullptr);
   return ADG_OK;
 }
 

@@ -788,10 +788,10 @@ def run_ours(args, w):
     value = whole_job_rate(head["dof"], world, ms)
 
     # end to end through the C ABI with host buffers: every step copies the
-    # state of every level in from page-locked host memory, runs the step
-    # (graph replay) and reads every level back out (the step readback: each
-    # level's copy starts once the step has finished writing it, beside the
-    # step's tail); the host waits once per step for the result
+    # state of every level in from page-locked host memory (one packed copy),
+    # runs the step (graph replay) and reads every level back out (the step
+    # readback: each level's copy starts once the step has finished writing
+    # it, beside the step's tail); the host waits once per step for the result
     s = head["sim"]
     L, ctx = s._L, s.ctx
     e2e_steps = max(5, min(args.steps, 50))
@@ -803,45 +803,42 @@ def run_ours(args, w):
     def level_cells():
         return [s.level_cells(l) for l in range(s.num_levels())]
 
-    # host copies of every level sized for its largest layout (the level
-    # fully refined), registered for the step readback (adg_set_readback):
-    # each step's result lands in them beside the step's tail
+    # one page-locked host copy of every level packed in level order, sized
+    # for the largest layout (every level fully refined) and registered for
+    # the step readback (adg_set_readback): the state goes in with one copy
+    # and each level's result comes back beside the step's tail
     amr_levels = w.get("amr", {}).get("max_level", 0) + 1
-    full = [1] * amr_levels
+    full = 0
     for lev in range(amr_levels):
+        c = 1
         for d in range(w["D"]):
-            full[lev] *= w["n"][d] << lev
-    hosts = [G.PinnedArray((full[l], Q, Nps)) for l in range(amr_levels)]
-    ptrs = [h.array.ctypes.data for h in hosts]
-    cells = level_cells()
-    for l in range(len(cells)):
-        hosts[l].array[:cells[l]] = s.get_U_w(l)
-        s.set_readback(hosts[l], l)
+            c *= w["n"][d] << lev
+        full += c
+    host = G.PinnedArray((full, Q, Nps))
+    ptr = host.array.ctypes.data
+    check(L.adg_get_state(ctx, G.ADG_ALL_LEVELS, ptr, G.ADG_MEM_HOST), "adg_get_state")
+    check(L.adg_set_readback(ctx, G.ADG_ALL_LEVELS, ptr, full), "adg_set_readback")
     s.advance(1, use_graph=True)  # capture the step with its readback copies before timing
     s.synchronize()
-    cells = level_cells()
     h2d = d2h = 0
     t0 = time.perf_counter()
     d_before, _ = s.dof_updates()
     for _ in range(e2e_steps):
-        for l in range(len(cells)):
-            check(L.adg_set_state(ctx, l, ptrs[l], G.ADG_MEM_HOST_ASYNC), "adg_set_state")
-            h2d += cells[l] * Q * Nps * 8
+        n0 = sum(level_cells())
+        check(L.adg_set_state(ctx, G.ADG_ALL_LEVELS, ptr, G.ADG_MEM_HOST_ASYNC), "adg_set_state")
+        h2d += n0 * Q * Nps * 8
         check(L.adg_advance(ctx, 1, 1), "adg_advance")
-        cells = level_cells()
-        for l in range(len(cells)):
-            if not s.readback_active(l):  # not registered (cannot happen with full-size buffers)
-                check(L.adg_get_state(ctx, l, ptrs[l], G.ADG_MEM_HOST_ASYNC), "adg_get_state")
-            d2h += cells[l] * Q * Nps * 8
+        n1 = sum(level_cells())
+        if not s.readback_active(G.ADG_ALL_LEVELS):  # cannot happen with the full-size buffer
+            check(L.adg_get_state(ctx, G.ADG_ALL_LEVELS, ptr, G.ADG_MEM_HOST_ASYNC), "adg_get_state")
+        d2h += n1 * Q * Nps * 8
         check(L.adg_synchronize(ctx), "adg_synchronize")
     e2e_s = barrier_max(time.perf_counter() - t0)
     d_after, _ = s.dof_updates()
     e2e_val = (d_after - d_before) * world / e2e_s
-    for l in range(s.num_levels()):
-        s.set_readback(None, l)
+    check(L.adg_set_readback(ctx, G.ADG_ALL_LEVELS, None, 0), "adg_set_readback")
     s.synchronize()
-    for h in hosts:
-        h.free()
+    host.free()
     try:
         e2e_dev = e2e_device_patches(G, s, w, e2e_steps)
     except Exception as ex:  # torch absent or no device memory: report, do not fail the line

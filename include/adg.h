@@ -130,7 +130,10 @@ int adg_init(adg_ctx* ctx);
  * x-fastest order over the level's valid cells.  Setting a level that has a
  * finer level makes that level's coarse-fine ghosts stale; they are projected
  * again once, before the next kernel that reads them (a step, adg_ader,
- * adg_predictor, adg_tags) or by adg_fill_ghosts. */
+ * adg_predictor, adg_tags) or by adg_fill_ghosts.  lev = ADG_ALL_LEVELS:
+ * every level in one copy, packed in level order (level 0's cells, then
+ * level 1's, ...; counts from adg_level_cells). */
+#define ADG_ALL_LEVELS (-1)
 int adg_num_levels(const adg_ctx* ctx, int* nlev);
 int adg_level_cells(const adg_ctx* ctx, int lev, int64_t* ncells);
 int adg_get_state(adg_ctx* ctx, int lev, double* dst, int mem);
@@ -148,7 +151,10 @@ int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem);
  * the registration while the level's cells fit; one that removes the level
  * or grows it past the capacity drops it, and no copy of the new layout goes
  * into the buffer (adg_readback_active then reports 0 and the buffer does
- * not hold that step's state: read it with adg_get_state).  Steps of
+ * not hold that step's state: read it with adg_get_state).  lev =
+ * ADG_ALL_LEVELS registers one buffer for every level packed in level order
+ * (as adg_get_state with ADG_ALL_LEVELS; capacity = all levels' cells), each
+ * level copied into its place as soon as it is final.  Steps of
  * adg_time_kernels do not read back.  For a caller that keeps the state on
  * the host: the per-step output of U_w(l, q) at the end of a step of
  * AmrDG::evolve (after the limiter and the average down,

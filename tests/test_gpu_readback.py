@@ -105,3 +105,61 @@ def test_readback_argument_checks():
     s.set_readback(None, 0)
     assert not s.readback_active(0)
     p.free()
+
+
+def _packed(s):
+    return np.concatenate([s.get_U_w(lev) for lev in range(s.num_levels())])
+
+
+@pytest.mark.parametrize("tight", [False, True])
+def test_packed_readback_and_packed_copies(tight):
+    """ADG_ALL_LEVELS: one copy of every level packed in level order in and
+    out, and one packed readback buffer filled level by level inside the
+    step."""
+    case = "kh_p3_amr"
+    s = make_gpu_amr(case)
+    ref = make_gpu_amr(case)
+    L, ctx = s._L, s.ctx
+    Q, Nps = s.Q, s.Np_s
+
+    def cap():
+        if tight:
+            return sum(s.level_cells(lev) for lev in range(s.num_levels()))
+        return sum(_capacity(s, case, lev, False) for lev in range(AMR_CASES[case][7]["max_level"] + 1))
+
+    buf = G.PinnedArray((cap(), Q, Nps))
+    assert L.adg_set_readback(ctx, G.ADG_ALL_LEVELS, buf.array.ctypes.data, buf.array.shape[0]) == 0
+    v = ctypes.c_int()
+    drops = 0
+    for _ in range(12):
+        buf.array[:] = np.nan
+        # the packed state goes in with one copy (a no-op round trip here)
+        n = sum(s.level_cells(lev) for lev in range(s.num_levels()))
+        packed = np.ascontiguousarray(_packed(s))
+        assert packed.shape[0] == n
+        assert L.adg_set_state(ctx, G.ADG_ALL_LEVELS, packed.ctypes.data, G.ADG_MEM_HOST) == 0
+        s.advance(1)
+        ref.advance(1)
+        s.synchronize()
+        want = _packed(s)
+        got = np.empty_like(want)
+        assert L.adg_get_state(ctx, G.ADG_ALL_LEVELS, got.ctypes.data, G.ADG_MEM_HOST) == 0
+        assert np.array_equal(got, want)
+        assert L.adg_readback_active(ctx, G.ADG_ALL_LEVELS, ctypes.byref(v)) == 0
+        if v.value:
+            assert np.array_equal(buf.array[: want.shape[0]], want)
+            assert np.all(np.isnan(buf.array[want.shape[0]:]))
+        else:
+            assert tight and want.shape[0] > buf.array.shape[0]
+            drops += 1
+            buf.free()
+            buf = G.PinnedArray((cap(), Q, Nps))
+            assert L.adg_set_readback(ctx, G.ADG_ALL_LEVELS, buf.array.ctypes.data, buf.array.shape[0]) == 0
+    if not tight:
+        assert drops == 0
+    assert L.adg_set_readback(ctx, G.ADG_ALL_LEVELS, None, 0) == 0
+    s.synchronize()
+    buf.free()
+    # the packed round trips and the readback left the steps unchanged
+    for lev in range(ref.num_levels()):
+        assert np.array_equal(s.get_U_w(lev), ref.get_U_w(lev)), lev
