@@ -142,7 +142,8 @@ int adg_set_state(adg_ctx* ctx, int lev, const double* src, int mem);
  * capacity_cells * Q * Np_s doubles (at least the level's valid cells) that
  * receives level lev's state, as adg_get_state returns it (the level's
  * current valid cells, adg_level_cells), at the end of every step of
- * adg_advance.  The copy waits only for the step's last writer of that level
+ * adg_step and adg_advance (also the timed forms).  The copy waits only for
+ * the step's last writer of that level
  * (the corrector or limiter for the finest level, the average down onto it
  * for the others) and runs on its own stream beside the rest of the step;
  * the next step and anything queued after adg_advance are ordered after it,
