@@ -98,6 +98,7 @@ struct adg_seed {
   DevBuf<float> X, T;  // data set
   long long nsamp = 0;
   DevBuf<float> Z1, A1, Z2, A2, Z3, A3, Y, dY, dA, dZ, Xb, Tb;
+  DevBuf<float> red;  // partial sums of the split reductions (added in a fixed order)
   long long work_rows = 0;
   DevBuf<int> idx;
   DevBuf<double> loss;
@@ -110,7 +111,7 @@ struct adg_seed {
   bool packed = false;
   ~adg_seed() {
     DevBuf<float>* bufs[] = {&params, &grads, &am, &av, &x_mean, &x_istd, &y_mean, &y_std, &X, &T,
-                             &Z1, &A1, &Z2, &A2, &Z3, &A3, &Y, &dY, &dA, &dZ, &Xb, &Tb, &wpack};
+                             &Z1, &A1, &Z2, &A2, &Z3, &A3, &Y, &dY, &dA, &dZ, &Xb, &Tb, &wpack, &red};
     for (auto* b : bufs) b->release();
     idx.release();
     loss.release();
@@ -2454,18 +2455,22 @@ int adg_flops_per_element(int D, int P, double* algorithmic, double* issued) {
 // ===========================================================================
 namespace {
 
+// Few output tiles and a long K split K into slices whose partial sums go to
+// red (slice z at z M N) and are then added in slice order: the same result
+// on every run, unlike atomic accumulation.
 void sgemm(int TA, int TB, int M, int N, int K, const float* A, const float* B, float* C, const float* bias,
-           float* aux, int epi, cudaStream_t st) {
+           float* aux, int epi, cudaStream_t st, DevBuf<float>* red = nullptr) {
   dim3 grid((N + 63) / 64, (M + 63) / 64, 1);
   const int tiles = grid.x * grid.y;
-  if (epi == mlp::EPI_STORE && tiles < 64 && K >= 512) {  // few output tiles, long K: split K
-    grid.z = std::min(64, std::max(1, K / 256));
-    cudaMemsetAsync(C, 0, (size_t)M * N * sizeof(float), st);
-  }
-  if (!TA && !TB) mlp::k_sgemm<0, 0><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
-  else if (TA && !TB) mlp::k_sgemm<1, 0><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
-  else if (!TA && TB) mlp::k_sgemm<0, 1><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
-  else mlp::k_sgemm<1, 1><<<grid, 256, 0, st>>>(M, N, K, A, B, C, bias, aux, epi);
+  const size_t mn = (size_t)M * N;
+  if (red && epi == mlp::EPI_STORE && tiles < 64 && K >= 512)
+    grid.z = (unsigned)std::min<size_t>(std::min(64, std::max(1, K / 256)), red->n / std::max<size_t>(mn, 1));
+  float* out = grid.z > 1 ? red->p : C;
+  if (!TA && !TB) mlp::k_sgemm<0, 0><<<grid, 256, 0, st>>>(M, N, K, A, B, out, bias, aux, epi);
+  else if (TA && !TB) mlp::k_sgemm<1, 0><<<grid, 256, 0, st>>>(M, N, K, A, B, out, bias, aux, epi);
+  else if (!TA && TB) mlp::k_sgemm<0, 1><<<grid, 256, 0, st>>>(M, N, K, A, B, out, bias, aux, epi);
+  else mlp::k_sgemm<1, 1><<<grid, 256, 0, st>>>(M, N, K, A, B, out, bias, aux, epi);
+  if (grid.z > 1) mlp::k_sum_slices<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>((long long)mn, (int)grid.z, red->p, C);
 }
 
 float* P(adg_seed* s, int k) { return s->params.p + s->off[k]; }
@@ -2480,6 +2485,10 @@ cudaError_t seed_work(adg_seed* s, long long rows) {
     if (e != cudaSuccess) return e;
   }
   cudaError_t e = s->Y.ensure((size_t)rows * s->n_out);
+  if (e == cudaSuccess) {  // split-K slices of the weight gradients and the column-sum blocks
+    const size_t mn = std::max({(size_t)s->n_in * h, h * h, h * (size_t)s->n_out});
+    e = s->red.ensure(std::max(64 * mn, (size_t)128 * std::max(h, (size_t)s->n_out)));
+  }
   if (e == cudaSuccess) e = s->dY.ensure((size_t)rows * s->n_out);
   if (e == cudaSuccess) e = s->Xb.ensure((size_t)rows * s->n_in);
   if (e == cudaSuccess) e = s->Tb.ensure((size_t)rows * s->n_out);
@@ -2497,26 +2506,29 @@ void seed_forward_train(adg_seed* s, const float* X, int B, cudaStream_t st) {
 }
 
 // Backward from dY (in s->dY) into s->grads.
-void colsum(int M, int N, const float* X, float* out, cudaStream_t st) {
-  cudaMemsetAsync(out, 0, (size_t)N * sizeof(float), st);
+// Column sums of X[M x N] by row blocks into red, then the blocks added in
+// order into out.
+void colsum(int M, int N, const float* X, float* out, DevBuf<float>& red, cudaStream_t st) {
   dim3 grid((N + 127) / 128, std::max(1, std::min(128, M / 64)));
-  mlp::k_colsum<<<grid, 128, 0, st>>>(M, N, X, out);
+  grid.y = (unsigned)std::max<size_t>(1, std::min<size_t>(grid.y, red.n / std::max(N, 1)));
+  mlp::k_colsum<<<grid, 128, 0, st>>>(M, N, X, red.p);
+  mlp::k_sum_slices<<<(unsigned)((N + 255) / 256), 256, 0, st>>>((long long)N, (int)grid.y, red.p, out);
 }
 
 void seed_backward(adg_seed* s, const float* X, int B, cudaStream_t st) {
   using namespace mlp;
   const int h = s->h;
-  sgemm(1, 0, h, s->n_out, B, s->A3.p, s->dY.p, G(s, 6), nullptr, nullptr, EPI_STORE, st);
-  colsum(B, s->n_out, s->dY.p, G(s, 7), st);
+  sgemm(1, 0, h, s->n_out, B, s->A3.p, s->dY.p, G(s, 6), nullptr, nullptr, EPI_STORE, st, &s->red);
+  colsum(B, s->n_out, s->dY.p, G(s, 7), s->red, st);
   sgemm(0, 1, B, h, s->n_out, s->dY.p, P(s, 6), s->dZ.p, nullptr, s->Z3.p, EPI_GELU_BWD, st);  // dZ3
-  sgemm(1, 0, h, h, B, s->A2.p, s->dZ.p, G(s, 4), nullptr, nullptr, EPI_STORE, st);
-  colsum(B, h, s->dZ.p, G(s, 5), st);
+  sgemm(1, 0, h, h, B, s->A2.p, s->dZ.p, G(s, 4), nullptr, nullptr, EPI_STORE, st, &s->red);
+  colsum(B, h, s->dZ.p, G(s, 5), s->red, st);
   sgemm(0, 1, B, h, h, s->dZ.p, P(s, 4), s->dA.p, nullptr, s->Z2.p, EPI_GELU_BWD, st);  // dZ2
-  sgemm(1, 0, h, h, B, s->A1.p, s->dA.p, G(s, 2), nullptr, nullptr, EPI_STORE, st);
-  colsum(B, h, s->dA.p, G(s, 3), st);
+  sgemm(1, 0, h, h, B, s->A1.p, s->dA.p, G(s, 2), nullptr, nullptr, EPI_STORE, st, &s->red);
+  colsum(B, h, s->dA.p, G(s, 3), s->red, st);
   sgemm(0, 1, B, h, h, s->dA.p, P(s, 2), s->dZ.p, nullptr, s->Z1.p, EPI_GELU_BWD, st);  // dZ1
-  sgemm(1, 0, s->n_in, h, B, X, s->dZ.p, G(s, 0), nullptr, nullptr, EPI_STORE, st);
-  colsum(B, h, s->dZ.p, G(s, 1), st);
+  sgemm(1, 0, s->n_in, h, B, X, s->dZ.p, G(s, 0), nullptr, nullptr, EPI_STORE, st, &s->red);
+  colsum(B, h, s->dZ.p, G(s, 1), s->red, st);
 }
 
 // Inference with ping-pong activations a0, a1 (rows x h each).
@@ -2781,21 +2793,26 @@ int adg_seed_collect(adg_ctx* ctx, adg_seed* s, int target_sweeps) {
 static int seed_normalise(adg_seed* s) {
   const long long M = s->nsamp;
   auto moments = [&](DevBuf<float>& X, int F, std::vector<double>& mean, std::vector<double>& sd) -> cudaError_t {
+    constexpr int NB = 64;  // blocks per column; their partial sums are added in order here
     DevBuf<double> acc;
-    cudaError_t e = acc.ensure(2 * (size_t)F);
+    cudaError_t e = acc.ensure(2 * (size_t)F * NB);
     if (e != cudaSuccess) return e;
-    cudaMemsetAsync(acc.p, 0, 2 * F * sizeof(double), s->stream);
-    dim3 grid(64, F);
-    mlp::k_col_moments<<<grid, 256, 0, s->stream>>>(M, F, X.p, acc.p, acc.p + F);
-    std::vector<double> h(2 * F);
-    e = cudaMemcpyAsync(h.data(), acc.p, 2 * F * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+    dim3 grid(NB, F);
+    mlp::k_col_moments<<<grid, 256, 0, s->stream>>>(M, F, X.p, acc.p);
+    std::vector<double> h(2 * (size_t)F * NB);
+    e = cudaMemcpyAsync(h.data(), acc.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     acc.release();
     mean.resize(F);
     sd.resize(F);
     for (int f = 0; f < F; ++f) {
-      mean[f] = h[f] / M;
-      const double var = std::max(0.0, h[F + f] / M - mean[f] * mean[f]);
+      double sum = 0.0, sumsq = 0.0;
+      for (int b = 0; b < NB; ++b) {
+        sum += h[((size_t)f * NB + b) * 2];
+        sumsq += h[((size_t)f * NB + b) * 2 + 1];
+      }
+      mean[f] = sum / M;
+      const double var = std::max(0.0, sumsq / M - mean[f] * mean[f]);
       sd[f] = std::sqrt(var);
     }
     return e;

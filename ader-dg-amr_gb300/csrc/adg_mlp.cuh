@@ -30,8 +30,9 @@ __global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float*
   const int tid = threadIdx.x;
   const int tx = tid % 16, ty = tid / 16;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  // split-K: block z covers K range [kz0, kz1); partial sums are added
-  // atomically into C (which the caller zeroes) when gridDim.z > 1
+  // split-K: block z covers K range [kz0, kz1) and, when gridDim.z > 1,
+  // stores its partial sums in slice z of C (z M N floats; k_sum_slices adds
+  // them in order, so the result does not depend on block timing)
   const int kchunk = (((K + gridDim.z - 1) / gridDim.z) + BK - 1) / BK * BK;
   const int kz0 = blockIdx.z * kchunk, kz1 = min(K, kz0 + kchunk);
   float acc[4][4] = {};
@@ -76,7 +77,7 @@ __global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float*
       const size_t o = (size_t)gm * N + gn;
       float v = acc[i][j];
       if (gridDim.z > 1) {  // split-K partial sum (EPI_STORE only)
-        atomicAdd(&C[o], v);
+        C[(size_t)blockIdx.z * M * N + o] = v;
         continue;
       }
       if (epi == EPI_BIAS) {
@@ -93,16 +94,26 @@ __global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float*
   }
 }
 
-// out[n] += sum over this block's rows of X[m][n] (out zeroed by the caller);
-// grid.x covers columns, grid.y splits the rows.
-__global__ void k_colsum(int M, int N, const float* X, float* out) {
+// part[y][n] = sum over row block y of X[m][n]; grid.x covers columns,
+// grid.y splits the rows (k_sum_slices adds the blocks in order).
+__global__ void k_colsum(int M, int N, const float* X, float* part) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
   const int rows = (M + gridDim.y - 1) / gridDim.y;
   const int m0 = blockIdx.y * rows, m1 = min(M, m0 + rows);
   float s = 0.f;
   for (int m = m0; m < m1; ++m) s += X[(size_t)m * N + n];
-  atomicAdd(&out[n], s);
+  part[(size_t)blockIdx.y * N + n] = s;
+}
+
+// dst[i] = sum over s of src[s n + i], added in s order: split partial sums
+// reduced the same way on every run.
+__global__ void k_sum_slices(long long n, int ns, const float* __restrict__ src, float* __restrict__ dst) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float v = 0.f;
+  for (int s = 0; s < ns; ++s) v += src[(size_t)s * n + i];
+  dst[i] = v;
 }
 
 // dY = (2 / (M N)) (Y - T); loss partial sums into loss_acc (double).
@@ -147,8 +158,9 @@ __global__ void k_standardise(long long M, int F, float* X, const float* mean, c
   X[i] = (X[i] - mean[f]) * istd[f];
 }
 
-// Column mean and variance (double accumulation) over M rows.
-__global__ void k_col_moments(long long M, int F, const float* X, double* sum, double* sumsq) {
+// Column sums and sums of squares (double) over M rows, per block:
+// part[(f gridDim.x + block) 2 + {0, 1}], added in order by the host.
+__global__ void __launch_bounds__(256) k_col_moments(long long M, int F, const float* X, double* part) {
   const int f = blockIdx.y;
   double s = 0.0, s2 = 0.0;
   for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < M; m += (long long)gridDim.x * blockDim.x) {
@@ -160,9 +172,22 @@ __global__ void k_col_moments(long long M, int F, const float* X, double* sum, d
     s += __shfl_xor_sync(0xffffffffu, s, o);
     s2 += __shfl_xor_sync(0xffffffffu, s2, o);
   }
+  __shared__ double ws[8][2];
+  const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&sum[f], s);
-    atomicAdd(&sumsq[f], s2);
+    ws[w][0] = s;
+    ws[w][1] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      a += ws[k][0];
+      b += ws[k][1];
+    }
+    double* p = part + ((size_t)f * gridDim.x + blockIdx.x) * 2;
+    p[0] = a;
+    p[1] = b;
   }
 }
 

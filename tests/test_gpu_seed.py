@@ -127,6 +127,24 @@ def test_training_reduces_loss_and_seed_beats_unseeded_single_sweep():
     assert e_seed2_f32 < 10 * e_plain, (e_seed2_f32, e_plain)
 
 
+def test_training_is_reproducible_bit_for_bit():
+    """Collection, standardisation and training reduce in a fixed order
+    (split-K slices and column-sum blocks added in order, no atomics on the
+    parameters' path): two seeds trained alike on the same pairs end with
+    the same parameters, bit for bit."""
+    params = []
+    for _ in range(2):
+        seed = G.PredictorSeed(2, 3, hidden=128, rng_seed=9)
+        s = _kh(seed=6, amp=2e-3)
+        for k in range(6):
+            if k % 2 == 0:
+                seed.collect(s, target_sweeps=8)
+            s.time_integration()
+        seed.train(3, batch=4096, lr=1e-3)
+        params.append(np.asarray(seed.get_params()).copy())
+    assert np.array_equal(params[0], params[1])
+
+
 def test_zero_tolerance_falls_back_everywhere_to_the_plain_path():
     seed, _, _ = _trained_seed()
     a = _kh(n=32, seed=9)
