@@ -81,6 +81,22 @@ def test_readback_equals_get_state_after_every_step_amr(case, use_graph, tight):
     assert a.status() == 0
 
 
+@pytest.mark.parametrize("t_limit", [1, 2])
+def test_readback_after_the_limiter(t_limit):
+    """With the TVB limiter the finest level's last writer in a step is the
+    limiter (every step, or every other step, which runs without the graph):
+    the readback holds the limited state."""
+    case = "blast3d_p2_amr"
+    kw = dict(limiter_type="TVB", TVB_M=0.0, t_limit=t_limit)
+    a = make_gpu_amr(case, **kw)
+    b = make_gpu_amr(case, **kw)
+    _run(a, case, 6, True, False)
+    b.advance(6)
+    for lev in range(a.num_levels()):
+        assert np.array_equal(a.get_U_w(lev), b.get_U_w(lev)), lev
+    assert a.status() == 0
+
+
 def test_readback_single_level():
     a = make_gpu("kh_p3")
     b = make_gpu("kh_p3")
