@@ -873,7 +873,11 @@ def run_ours(args, w):
                       "the per-step CUDA-event intervals that are summed)"},
         "leaf_value": head["leaf_dof_per_s"] * world,
         "e2e": {"value": e2e_val, "unit": "DOF-updates/s", "h2d_bytes_per_step": h2d // e2e_steps,
-                "d2h_bytes_per_step": d2h // e2e_steps},
+                "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps,
+                "path": "per step: adg_set_state(ADG_ALL_LEVELS) from page-locked host memory (one copy), "
+                        "adg_advance(1 step, graph) with the packed step readback (adg_set_readback: each "
+                        "level copied to the host buffer once the step has written it), adg_synchronize; "
+                        "host-timed"},
         "e2e_device_patches": e2e_dev,
         "roofline": roof,
         "kernel_ms": {"plain": km_plain, "headline": km_head},
